@@ -1,0 +1,202 @@
+/* include/mprgp_gpu.h -- C ABI of the GB300 MPRGP solver (libmprgp_gb300.so).
+ *
+ * The reference (simba518/MPRGP) is a header-only C++ template library with
+ * no FFI: callers instantiate MATH::MPRGPDecoupledCon<double>::solve and its
+ * siblings directly (src/MPRGPSolver/MPRGPSolver.h:503-626).  This header is
+ * the thin boundary that replaces those instantiations; the C++ template
+ * façade in include/mprgp/MPRGPSolver.h keeps the reference's class names and
+ * signatures and forwards to the functions below.  Every function is plain
+ * C: pointers, sizes and status codes, no C++ or torch types.
+ *
+ * Conventions
+ *   - A QP instance has nv vertices and n = 3*nv unknowns (x, y, z per vertex).
+ *   - A is given as 3x3-block CSR ("BSR"): row_ptr[nv+1], cols[nnzb] (vertex
+ *     indices), vals[9*nnzb], each block row-major.  It must be symmetric
+ *     positive definite, as the reference requires.
+ *   - Plane constraints are per vertex, in the reference's VVVec4d form
+ *     (MprgpFemSolver.h:107, MPRGPUtility.h:120-154): plane (nx, ny, nz, p)
+ *     on vertex v means nx*x_v + ny*y_v + nz*z_v + p >= 0, i.e. the row of J
+ *     is n at the vertex's three columns and c = -p.  plane_ptr[nv+1] lists
+ *     the planes of each vertex (CSR by vertex); at most 3 per vertex.
+ *   - Bound constraints are per unknown: L[n] (and U[n] for a box).
+ *   - Returned codes follow the reference: 0 converged, -1 not converged
+ *     (MPRGPSolver.h:390, :445); negative values below -1 are errors.
+ */
+#ifndef MPRGP_GPU_H
+#define MPRGP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MPRGP_OK 0
+#define MPRGP_NOT_CONVERGED (-1) /* reference result_code -1 */
+#define MPRGP_BREAKDOWN (-2)     /* NaN in a step length */
+#define MPRGP_OOM (-3)           /* device allocation failed / admission cap */
+#define MPRGP_TIMEOUT (-4)       /* a bounded device wait ran out */
+#define MPRGP_INVALID (-5)       /* bad argument or unsupported shape */
+#define MPRGP_CUDA_ERROR (-6)    /* CUDA runtime error */
+#define MPRGP_NO_DEVICE (-7)     /* no CUDA device / extension unusable */
+#define MPRGP_BUSY (-8)          /* resource in use (server slot table full) */
+
+/* ---- projector kinds (which reference façade the solve mirrors) -------- */
+#define MPRGP_KIND_LOWER 0     /* MPRGPLowerBound   (MPRGPSolver.h:503-517) */
+#define MPRGP_KIND_BOX 1       /* MPRGPBoxBound     (MPRGPSolver.h:520-535) */
+#define MPRGP_KIND_DECOUPLED 2 /* MPRGPDecoupledCon (MPRGPSolver.h:538-590) */
+#define MPRGP_KIND_PLANES 3    /* MPRGPGeneralCon   (MPRGPSolver.h:593-626),
+                                  per-vertex plane blocks solved exactly */
+
+/* ---- algorithm --------------------------------------------------------- */
+#define MPRGP_ALG_DEFAULT 0  /* what the façade of `kind` uses */
+#define MPRGP_ALG_MONOTONE 1 /* MPRGPMonotonic::solve (MPRGPSolver.h:412-454) */
+#define MPRGP_ALG_PLAIN 2    /* MPRGP::solve         (MPRGPSolver.h:356-396) */
+
+/* ---- preconditioner ---------------------------------------------------- */
+#define MPRGP_PRECOND_DEFAULT 0  /* what the façade of `kind` uses */
+#define MPRGP_PRECOND_NONE 1     /* the façade's preconditioned=false: z = phi */
+#define MPRGP_PRECOND_INFACE 2   /* DiagonalInFacePreconSolver (Precondition.h:36-69) */
+#define MPRGP_PRECOND_DECOUPLE 3 /* DiagonalDecouplePreconSolver (Precondition.h:72-110) */
+
+/* ---- precision form ---------------------------------------------------- */
+#define MPRGP_PREC_FP64 0  /* plain FP64 everywhere */
+#define MPRGP_PREC_MIXED 1 /* A stored/multiplied in FP32 (FP32 accumulate) for
+                              CG and power-method products; FP64 for dots,
+                              steps, projection, residual refinement and the
+                              stopping test */
+
+typedef struct mprgp_options {
+  double tol;          /* absolute tolerance on ||phi+beta|| (tolerance_factor) */
+  int max_it;          /* max_iterations */
+  int kind;            /* MPRGP_KIND_* */
+  int algorithm;       /* MPRGP_ALG_* */
+  int precond;         /* MPRGP_PRECOND_* */
+  int precision;       /* MPRGP_PREC_* */
+  int project_x0;      /* 1: x <- P(x) first (the solve(A,B,J,c,x) overloads) */
+  int use_ev;          /* 1: start the power method from the stored vector */
+  uint64_t seed;       /* seed of the power method's start vector */
+  double wait_limit_s; /* bound on any device-side wait (0 = 5 s) */
+} mprgp_options;
+
+typedef struct mprgp_stats {
+  int code;        /* 0 converged, -1 not converged, < -1 error */
+  int iterations;  /* iterations_out */
+  int num_cg, num_exp, num_prop;
+  int power_iters; /* specRad's iteration count */
+  int active;      /* COUNT_CONSTRAINTS(face) (MPRGPUtility.h:98-106) */
+  int ev_updated;  /* 1 if the power method converged and stored its vector */
+  double residual; /* residual_out */
+  double alpha_bar, spec_rad;
+  long long spmv_fp64, spmv_fp32; /* matrix passes by precision */
+  long long phases;               /* device phases executed */
+  double device_ms;               /* kernel time of the solve */
+} mprgp_stats;
+
+/* ---- library ------------------------------------------------------------ */
+int mprgp_version(void);
+const char *mprgp_status_string(int status);
+/* Text of the last failure on the calling thread (for diagnostics). */
+const char *mprgp_last_error(void);
+void mprgp_default_options(mprgp_options *opt);
+int mprgp_device_count(int *count);
+
+/* ---- context: one device, one stream ------------------------------------ */
+typedef struct mprgp_context mprgp_context;
+int mprgp_context_create(int device, mprgp_context **out);
+int mprgp_context_destroy(mprgp_context *ctx);
+void *mprgp_context_stream(mprgp_context *ctx); /* the cudaStream_t it launches on */
+int mprgp_context_sync(mprgp_context *ctx);
+/* SM count and resident engine CTAs per SM (the persistent grid's shape). */
+int mprgp_context_info(mprgp_context *ctx, int *nsm, int *blocks_per_sm);
+
+/* ---- problem: one QP instance resident in device memory ----------------- */
+/* Replaces the reference's FixedSparseMatrix<T> + projector objects
+ * (MPRGPSolver.h:459-500, MPRGPProjection.h): A, b, the constraints, x and
+ * the power-method vector stay on the device between solves (warm starts). */
+typedef struct mprgp_problem mprgp_problem;
+int mprgp_problem_create(mprgp_context *ctx, int nv, mprgp_problem **out);
+int mprgp_problem_destroy(mprgp_problem *prob);
+/* precisions: bit 0 keep FP64 values, bit 1 keep an FP32 copy. on_device: the
+ * pointers are device pointers (0 = host). */
+int mprgp_problem_set_matrix(mprgp_problem *prob, int nnzb, const int *row_ptr, const int *cols,
+                             const double *vals, int precisions, int on_device);
+int mprgp_problem_set_rhs(mprgp_problem *prob, const double *b, int on_device);
+int mprgp_problem_set_planes(mprgp_problem *prob, const int *plane_ptr, const double *planes,
+                             int on_device);
+int mprgp_problem_set_bounds(mprgp_problem *prob, const double *L, const double *U);
+int mprgp_problem_set_x(mprgp_problem *prob, const double *x, int on_device);
+int mprgp_problem_get_x(mprgp_problem *prob, double *x, int on_device);
+/* face codes as the reference's projector.getFace(): one per constraint row
+ * (planes, in plane_ptr order) or one per unknown (bounds). */
+int mprgp_problem_num_constraints(mprgp_problem *prob, int *m);
+int mprgp_problem_get_face(mprgp_problem *prob, unsigned char *face);
+int mprgp_problem_set_ev(mprgp_problem *prob, const double *ev);
+int mprgp_problem_get_ev(mprgp_problem *prob, double *ev, int *valid);
+/* Device-resident solve: x (set_x) is solved in place.  Mirrors
+ * MPRGPxxx<double>::solve(A, B, projector, x, tol, max_it, name, ev). */
+int mprgp_problem_solve(mprgp_problem *prob, const mprgp_options *opt, mprgp_stats *stats);
+/* Step trace of the next solves (diagnostics): capacity records of 4 doubles
+ * {event, iteration, residual, value}; event 1 CG commit / 2 CG exit (value
+ * f(P(y)) - f(x)), 3 expansion, 4 proportioning, 5 loop top (value =
+ * proportional test).  capacity 0 turns it off. */
+int mprgp_problem_set_trace(mprgp_problem *prob, int capacity);
+int mprgp_problem_get_trace(mprgp_problem *prob, double *out, int capacity, int *count);
+/* y = A x with device pointers (FixedSparseMatrix::multiply, MPRGPSolver.h:469-473).
+ * precision: MPRGP_PREC_FP64 or MPRGP_PREC_MIXED (FP32 values, FP32 accumulate). */
+int mprgp_problem_spmv(mprgp_problem *prob, const double *x_dev, double *y_dev, int precision);
+/* Device bytes held by a problem of this shape (admission accounting). */
+size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions);
+
+/* ---- one-call solve with host buffers ------------------------------------ */
+/* Uploads A, b, constraints and x, solves, downloads x (and face).  This is
+ * the entry the C++ façade calls for MPRGPDecoupledCon/GeneralCon/BoxBound/
+ * LowerBound::solve.  plane_ptr/planes for kinds DECOUPLED/PLANES, L/U for
+ * LOWER/BOX (U ignored for LOWER). ev may be NULL; if non-NULL it is the
+ * reference's `Vec *ev` (length n): used as the power start when opt->use_ev
+ * is set, and overwritten when the power method converges. */
+int mprgp_solve_bsr(mprgp_context *ctx, int nv, int nnzb, const int *row_ptr, const int *cols,
+                    const double *vals, const double *b, const int *plane_ptr,
+                    const double *planes, const double *L, const double *U,
+                    const mprgp_options *opt, double *x, unsigned char *face, double *ev,
+                    mprgp_stats *stats);
+
+/* ---- batched: many instances advance in one persistent launch ----------- */
+int mprgp_solve_batch(mprgp_context *ctx, int count, mprgp_problem *const *probs,
+                      const mprgp_options *opts, mprgp_stats *stats);
+
+/* ---- beam generator (synthetic implicit-Euler FEM QPs) ------------------- */
+typedef struct mprgp_beam_params {
+  int a, b, c;          /* cube counts along x, y (up), z */
+  double edge;          /* cube edge [m] */
+  double young, poisson, rho;
+  double dt;            /* time step h */
+  double gravity;       /* signed y acceleration, e.g. -9.8 */
+  double lift;          /* lowest layer placed at y = -lift */
+  double v0_sigma;      /* v0 ~ N(0, sigma^2) per component */
+  int extra_planes_max; /* extra planes: per facet vertex (mode 1) or global (mode 0), */
+  int extra_planes_min; /*   seeded in [min, max] */
+  double active_frac;   /* mode 1: fraction of candidate vertices given facets;
+                           mode 0: plane penetration at x0 as a fraction of lift */
+  uint64_t seed;
+  double plane_band;    /* a vertex gets a global plane if its gap at x0 < band */
+  double max_tilt;      /* plane normals: uniform on the cap within max_tilt of +y */
+  int plane_mode;       /* 2: corner walls x,z (default), 1: contact facets,
+                           0: global tilted planes */
+  int facet_layers;     /* facets go to vertices of the lowest facet_layers layers */
+} mprgp_beam_params;
+void mprgp_beam_default(mprgp_beam_params *p);
+int mprgp_beam_sizes(const mprgp_beam_params *p, int *nv, int *nnzb, int *nplanes);
+/* Fills BSR A = M + h^2 K (linear elasticity, lumped mass, Kuhn 6-tet cubes),
+ * b = M(x0 + h v0) + h^2 M g + h^2 K X, x0 (unprojected), and the planes:
+ * the floor y >= 0 on every vertex, then each global plane (normal uniform
+ * on the upper hemisphere) on the vertices within plane_band of it. */
+int mprgp_beam_build(const mprgp_beam_params *p, int *row_ptr, int *cols, double *vals,
+                     double *b, double *x0, int *plane_ptr, double *planes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPRGP_GPU_H */

@@ -1,0 +1,76 @@
+"""Builds libmprgp_gb300.so in-tree with nvcc for sm_103a.
+
+Three translation units (engine.cu, capi.cu, beam.cpp) are compiled in
+parallel and linked into mprgp_gb300/_build/libmprgp_gb300.so.  The same
+recipe runs on the x86_64 build host and the aarch64 GPU host: no
+architecture-specific host flags.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libmprgp_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+SOURCES = ["engine.cu", "capi.cu", "beam.cpp"]
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build")
+    return path
+
+
+def _compile(src: str, ptxas_verbose: bool) -> str:
+    obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+    cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj, "-std=c++17", "-O3",
+           "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+    if src.endswith(".cu"):
+        cmd += ARCH + ["-lineinfo"]
+        if ptxas_verbose:
+            cmd += ["-Xptxas", "-v"]
+    else:
+        cmd += ["-x", "c++"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+    if ptxas_verbose and res.stderr:
+        sys.stderr.write(res.stderr)
+    return obj
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps.append(os.path.join(ROOT, "include", "mprgp_gpu.h"))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False, ptxas_verbose: bool = False) -> str:
+    """Compiles the library if any source is newer; returns its path."""
+    if not force and not ptxas_verbose and not _stale():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, ptxas_verbose), SOURCES))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart_static"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, ptxas_verbose="-v" in sys.argv))

@@ -1,0 +1,760 @@
+// Host side of the C ABI (include/mprgp_gpu.h): device memory for each QP
+// instance, uploads, and launches of the persistent engine.
+//
+// Every failure is reported as a status code; nothing falls back to a CPU
+// path.  A problem keeps A (SELL-32, FP64 and/or FP32), b, the constraints,
+// x, the face and the power-method vector resident between solves.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mprgp_gpu.h"
+#include "engine.h"
+
+namespace mprgp {
+cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
+cudaError_t engine_max_blocks_per_sm(int *n);
+void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
+                        const int *slice_off, int *out_cols, double *out64, float *out32,
+                        double *dinv, cudaStream_t st);
+void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
+                         double *indn, const double *dinv, cudaStream_t st);
+void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
+                 cudaStream_t st);
+}  // namespace mprgp
+
+using namespace mprgp;
+
+struct mprgp_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Ctl *ctl = nullptr;
+  int nsm = 0, bps = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  mprgp_problem *scratch = nullptr;  // reused by mprgp_solve_bsr
+  // per-launch arrays (grown on demand)
+  InstDesc *d_desc = nullptr;
+  int *d_prefix = nullptr;
+  int cap_inst = 0;
+};
+
+struct mprgp_problem {
+  mprgp_context *ctx = nullptr;
+  int nv = 0, nnzb = 0, m = 0, nslices = 0, slots = 0;
+  int cons = 0;  // 0 none, 1 planes, 2 bounds (lower), 3 bounds (box)
+  int has64 = 0, has32 = 0;
+  int xc = 0, ev_valid = 0, planes_dirty = 0;
+  int *slice_off = nullptr, *cols = nullptr;
+  double *v64 = nullptr;
+  float *v32 = nullptr;
+  double *dinv = nullptr, *b = nullptr;
+  int *plane_ptr = nullptr;
+  double *planes_raw = nullptr, *planes = nullptr, *pl_nn = nullptr, *pl_indn = nullptr;
+  double *L = nullptr, *U = nullptr;
+  unsigned char *face = nullptr;
+  int face_len = 0;
+  double *vec = nullptr, *ev = nullptr, *part = nullptr;
+  unsigned int *cnt = nullptr;
+  InstState *st = nullptr;
+  double *trace = nullptr;
+  int trace_cap = 0, trace_n = 0;
+  std::vector<int> h_plane_ptr;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *what) {
+  g_last_error = what;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return MPRGP_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MPRGP_NO_DEVICE;
+  return MPRGP_CUDA_ERROR;
+}
+#define CK(call)                                       \
+  do {                                                 \
+    cudaError_t _e = (call);                           \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+template <typename T>
+int dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return MPRGP_OK;
+  CK(cudaMalloc((void **)p, count * sizeof(T)));
+  return MPRGP_OK;
+}
+template <typename T>
+void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+int nitems_of(int nv) { return (nv + kThreads - 1) / kThreads; }
+
+void free_problem_arrays(mprgp_problem *p) {
+  dfree(p->slice_off); dfree(p->cols); dfree(p->v64); dfree(p->v32);
+  dfree(p->dinv); dfree(p->b); dfree(p->plane_ptr); dfree(p->planes_raw);
+  dfree(p->planes); dfree(p->pl_nn); dfree(p->pl_indn); dfree(p->L); dfree(p->U);
+  dfree(p->face); dfree(p->vec); dfree(p->ev); dfree(p->part); dfree(p->cnt); dfree(p->st);
+  dfree(p->trace);
+}
+
+int resolve_options(const mprgp_problem *p, const mprgp_options *o, int *kind, int *alg,
+                    int *pre) {
+  *kind = o->kind;
+  if (*kind < MPRGP_KIND_LOWER || *kind > MPRGP_KIND_PLANES)
+    return fail(MPRGP_INVALID, "unknown kind");
+  if ((*kind >= MPRGP_KIND_DECOUPLED && p->cons != 1) ||
+      (*kind == MPRGP_KIND_LOWER && p->cons < 2) || (*kind == MPRGP_KIND_BOX && p->cons != 3))
+    return fail(MPRGP_INVALID, "constraints not set for this kind");
+  // Façade defaults (MPRGPSolver.h:503-626): BoxBound uses plain MPRGP, the
+  // others MPRGPMonotonic; DecoupledCon uses DiagonalDecouplePreconSolver,
+  // the others DiagonalInFacePreconSolver.
+  *alg = o->algorithm == MPRGP_ALG_DEFAULT
+             ? (*kind == MPRGP_KIND_BOX ? ALG_PLAIN : ALG_MONOTONE)
+             : (o->algorithm == MPRGP_ALG_PLAIN ? ALG_PLAIN : ALG_MONOTONE);
+  if (o->algorithm < 0 || o->algorithm > MPRGP_ALG_PLAIN) return fail(MPRGP_INVALID, "algorithm");
+  switch (o->precond) {
+    case MPRGP_PRECOND_DEFAULT:
+      *pre = *kind == MPRGP_KIND_DECOUPLED ? PRE_DECOUPLE : PRE_INFACE;
+      break;
+    case MPRGP_PRECOND_NONE: *pre = PRE_NONE; break;
+    case MPRGP_PRECOND_INFACE: *pre = PRE_INFACE; break;
+    case MPRGP_PRECOND_DECOUPLE:
+      if (*kind != MPRGP_KIND_DECOUPLED && *kind != MPRGP_KIND_PLANES)
+        return fail(MPRGP_INVALID, "DECOUPLE preconditioner needs plane constraints");
+      *pre = PRE_DECOUPLE;
+      break;
+    default: return fail(MPRGP_INVALID, "precond");
+  }
+  if (o->precision == MPRGP_PREC_MIXED && (!p->has32 || !p->has64))
+    return fail(MPRGP_INVALID, "mixed precision needs both FP64 and FP32 copies of A");
+  if (o->precision == MPRGP_PREC_FP64 && !p->has64)
+    return fail(MPRGP_INVALID, "FP64 solve needs the FP64 copy of A");
+  if (o->precision != MPRGP_PREC_FP64 && o->precision != MPRGP_PREC_MIXED)
+    return fail(MPRGP_INVALID, "precision");
+  if (!(o->tol >= 0.0) || o->max_it < 0) return fail(MPRGP_INVALID, "tol/max_it");
+  return MPRGP_OK;
+}
+
+// Prepares the desc and initial state of one instance.
+int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *d,
+            InstState *s) {
+  int kind, alg, pre;
+  int rc = resolve_options(p, o, &kind, &alg, &pre);
+  if (rc) return rc;
+  if (!p->b) return fail(MPRGP_INVALID, "rhs not set");
+  if (!p->cols) return fail(MPRGP_INVALID, "matrix not set");
+  cudaStream_t st = p->ctx->stream;
+  if (p->cons == 1 && p->planes_dirty) {
+    launch_planes_setup(p->nv, p->plane_ptr, p->planes_raw, p->planes, p->pl_nn, p->pl_indn,
+                        p->dinv, st);
+    CK(cudaGetLastError());
+    p->planes_dirty = 0;
+  }
+  std::memset(d, 0, sizeof(*d));
+  d->A.nslices = p->nslices;
+  d->A.slice_off = p->slice_off;
+  d->A.cols = p->cols;
+  d->A.v64 = p->v64;
+  d->A.v32 = p->v32;
+  d->nv = p->nv;
+  d->nitems = nitems_of(p->nv);
+  d->item_begin = item_begin;
+  d->m = p->m;
+  d->kind = kind;
+  d->alg = alg;
+  d->pre = pre;
+  d->prec = (alg == ALG_MONOTONE) ? o->precision : PREC_FP64;
+  d->max_it = o->max_it;
+  d->tol = o->tol < 1e-30 ? 1e-30 : o->tol;  // setParameters (MPRGPSolver.h:34-39)
+  d->seed = o->seed;
+  d->b = p->b;
+  d->dinv = p->dinv;
+  d->plane_ptr = p->plane_ptr;
+  d->planes = p->planes;
+  d->pl_nn = p->pl_nn;
+  d->pl_indn = p->pl_indn;
+  d->L = p->L;
+  d->U = p->U;
+  d->face = p->face;
+  const size_t n = 3 * (size_t)p->nv;
+  for (int i = 0; i < kNumBuf; ++i) d->buf[i] = p->vec + (size_t)i * n;
+  d->ev = p->ev;
+  d->part = p->part;
+  d->cnt = p->cnt;
+  d->st = p->st;
+  d->trace = p->trace;
+  d->trace_cap = p->trace_cap;
+  std::memset(s, 0, sizeof(*s));
+  s->xc = p->xc;
+  s->code = -1;
+  s->ev_valid = (o->use_ev && p->ev_valid) ? 1 : 0;
+  if (o->project_x0) {
+    s->phase = PH_PROJ0;
+  } else if (s->ev_valid) {
+    s->phase = PH_POW;
+    s->pow_src = -1;
+    s->pow_scale = 1.0;
+  } else {
+    s->phase = PH_POW_RAND;
+  }
+  // Power phases use buffers that are otherwise idle until PH_INIT.
+  return MPRGP_OK;
+}
+
+void fill_stats(const InstState &s, double ms, mprgp_stats *out) {
+  if (!out) return;
+  out->code = s.code;
+  out->iterations = s.iters_out;
+  out->num_cg = s.num_cg;
+  out->num_exp = s.num_exp;
+  out->num_prop = s.num_prop;
+  out->power_iters = s.power_iters;
+  out->active = s.active;
+  out->ev_updated = s.ev_upd;
+  out->residual = s.residual;
+  out->alpha_bar = s.alpha_bar;
+  out->spec_rad = s.spec_rad;
+  out->spmv_fp64 = s.spmv64;
+  out->spmv_fp32 = s.spmv32;
+  out->phases = s.phases;
+  out->device_ms = ms;
+}
+
+int ensure_launch_arrays(mprgp_context *c, int ninst) {
+  if (ninst <= c->cap_inst) return MPRGP_OK;
+  dfree(c->d_desc);
+  dfree(c->d_prefix);
+  int cap = std::max(ninst, 16);
+  int rc = dalloc(&c->d_desc, cap);
+  if (rc) return rc;
+  rc = dalloc(&c->d_prefix, cap + 1);
+  if (rc) return rc;
+  c->cap_inst = cap;
+  return MPRGP_OK;
+}
+
+// Launches the engine over `n` prepared instances until all are done.
+int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
+               mprgp_stats *stats) {
+  int rc = ensure_launch_arrays(c, n);
+  if (rc) return rc;
+  std::vector<InstDesc> desc(n);
+  std::vector<InstState> st(n);
+  std::vector<int> prefix(n + 1, 0);
+  double wait_s = 0.0;
+  long long phase_bound = 0;
+  for (int i = 0; i < n; ++i) {
+    mprgp_problem *p = probs[i];
+    if (!p || p->ctx != c) return fail(MPRGP_INVALID, "problem/context mismatch");
+    prefix[i + 1] = prefix[i] + nitems_of(p->nv);
+    rc = prepare(p, &opts[i], prefix[i], &desc[i], &st[i]);
+    if (rc) return rc;
+    wait_s = std::max(wait_s, opts[i].wait_limit_s);
+    // Each MPRGP iteration takes at most 4 phases (CG: spmv, candidate,
+    // optional delta^T A delta and residual replacement; expansion 3;
+    // proportioning 2); the power method at most 1003.
+    phase_bound = std::max(phase_bound, 1100LL + 8LL * ((long long)opts[i].max_it + 2));
+  }
+  if (wait_s <= 0.0) wait_s = 5.0;
+  cudaStream_t s = c->stream;
+  for (int i = 0; i < n; ++i) {
+    CK(cudaMemcpyAsync(probs[i]->st, &st[i], sizeof(InstState), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(probs[i]->cnt, 0, sizeof(unsigned int), s));
+  }
+  CK(cudaMemcpyAsync(c->d_desc, desc.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_prefix, prefix.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  Ctl ctl0;
+  std::memset(&ctl0, 0, sizeof(ctl0));
+  ctl0.active = n;
+  ctl0.snap[0] = ctl0.snap[1] = n;
+  CK(cudaMemcpyAsync(c->ctl, &ctl0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  EngineArgs args;
+  args.desc = c->d_desc;
+  args.item_prefix = c->d_prefix;
+  args.ninst = n;
+  args.total_items = prefix[n];
+  args.max_phases = (int)std::min<long long>(phase_bound, INT_MAX);
+  args.wait_ns = (long long)(wait_s * 1e9);
+  args.total_ns = (long long)(std::max(60.0, 20.0 * wait_s) * 1e9);
+  args.ctl = c->ctl;
+  const int grid = std::max(1, std::min(prefix[n], c->nsm * c->bps));
+  CK(cudaEventRecord(c->e0, s));
+  CK(launch_engine(args, grid, s));
+  CK(cudaEventRecord(c->e1, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  Ctl ctl1;
+  CK(cudaMemcpy(&ctl1, c->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i)
+    CK(cudaMemcpyAsync(&st[i], probs[i]->st, sizeof(InstState), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int worst = MPRGP_OK;
+  for (int i = 0; i < n; ++i) {
+    InstState &x = st[i];
+    if (ctl1.err) x.code = ctl1.err;
+    else if (x.phase != PH_DONE) x.code = MPRGP_TIMEOUT;
+    probs[i]->xc = x.xc;
+    probs[i]->trace_n = x.trace_n;
+    if (x.ev_upd && x.code > MPRGP_BREAKDOWN) probs[i]->ev_valid = 1;
+    fill_stats(x, ms, stats ? &stats[i] : nullptr);
+    if (x.code < worst) worst = x.code;
+  }
+  if (ctl1.err) return fail(ctl1.err, "device wait limit reached");
+  return worst < MPRGP_NOT_CONVERGED ? worst : MPRGP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mprgp_version(void) { return 10000; }
+
+const char *mprgp_status_string(int s) {
+  switch (s) {
+    case MPRGP_OK: return "ok";
+    case MPRGP_NOT_CONVERGED: return "not converged";
+    case MPRGP_BREAKDOWN: return "breakdown";
+    case MPRGP_OOM: return "out of device memory";
+    case MPRGP_TIMEOUT: return "device wait limit reached";
+    case MPRGP_INVALID: return "invalid argument";
+    case MPRGP_CUDA_ERROR: return "CUDA error";
+    case MPRGP_NO_DEVICE: return "no CUDA device";
+    case MPRGP_BUSY: return "busy";
+    default: return "unknown status";
+  }
+}
+
+const char *mprgp_last_error(void) { return g_last_error.c_str(); }
+
+void mprgp_default_options(mprgp_options *o) {
+  std::memset(o, 0, sizeof(*o));
+  o->tol = 1e-3;  // MPRGPDecoupledCon::solve defaults (MPRGPSolver.h:546)
+  o->max_it = 1000;
+  o->kind = MPRGP_KIND_DECOUPLED;
+  o->algorithm = MPRGP_ALG_DEFAULT;
+  o->precond = MPRGP_PRECOND_DEFAULT;
+  o->precision = MPRGP_PREC_FP64;
+  o->project_x0 = 0;
+  o->use_ev = 0;
+  o->seed = 0x5eedULL;
+  o->wait_limit_s = 5.0;
+}
+
+int mprgp_device_count(int *count) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (count) *count = (e == cudaSuccess) ? n : 0;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+  return MPRGP_OK;
+}
+
+int mprgp_context_create(int device, mprgp_context **out) {
+  if (!out) return fail(MPRGP_INVALID, "out");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(MPRGP_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= n) return fail(MPRGP_INVALID, "device");
+  CK(cudaSetDevice(device));
+  int coop = 0;
+  CK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device));
+  if (!coop) return fail(MPRGP_NO_DEVICE, "device lacks cooperative launch");
+  auto *c = new mprgp_context();
+  c->device = device;
+  CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+  CK(engine_max_blocks_per_sm(&c->bps));
+  if (c->bps < 1) {
+    delete c;
+    return fail(MPRGP_NO_DEVICE, "engine kernel cannot be resident");
+  }
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&c->e0));
+  CK(cudaEventCreate(&c->e1));
+  CK(cudaMalloc((void **)&c->ctl, sizeof(Ctl)));
+  CK(cudaMemset(c->ctl, 0, sizeof(Ctl)));
+  *out = c;
+  return MPRGP_OK;
+}
+
+int mprgp_context_destroy(mprgp_context *c) {
+  if (!c) return MPRGP_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->scratch) mprgp_problem_destroy(c->scratch);
+  dfree(c->ctl);
+  dfree(c->d_desc);
+  dfree(c->d_prefix);
+  cudaEventDestroy(c->e0);
+  cudaEventDestroy(c->e1);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return MPRGP_OK;
+}
+
+void *mprgp_context_stream(mprgp_context *c) { return c ? (void *)c->stream : nullptr; }
+
+int mprgp_context_sync(mprgp_context *c) {
+  if (!c) return fail(MPRGP_INVALID, "ctx");
+  CK(cudaStreamSynchronize(c->stream));
+  return MPRGP_OK;
+}
+
+int mprgp_context_info(mprgp_context *c, int *nsm, int *blocks_per_sm) {
+  if (!c) return fail(MPRGP_INVALID, "ctx");
+  if (nsm) *nsm = c->nsm;
+  if (blocks_per_sm) *blocks_per_sm = c->bps;
+  return MPRGP_OK;
+}
+
+size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {
+  const size_t nsl = (size_t)(nv + kSlice - 1) / kSlice;
+  const size_t slots = (size_t)nnzb / 1 + nsl * 8;  // padding allowance
+  size_t by = (nsl + 1) * 4 + slots * kSlice * 4;
+  if (precisions & 1) by += slots * kSlice * 9 * 8;
+  if (precisions & 2) by += slots * kSlice * 9 * 4;
+  const size_t n = 3 * (size_t)nv;
+  by += n * 8 * (kNumBuf + 3);  // vectors, dinv, b, ev
+  by += (size_t)nplanes * (8 * 4 * 2 + 8 * 2 + 1) + (size_t)(nv + 1) * 4 + n * 16 + n;
+  by += (size_t)nitems_of(nv) * kPart * 8 + sizeof(InstState) + 64;
+  return by;
+}
+
+int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
+  if (!c || !out || nv <= 0) return fail(MPRGP_INVALID, "problem_create");
+  *out = nullptr;
+  CK(cudaSetDevice(c->device));
+  auto *p = new mprgp_problem();
+  p->ctx = c;
+  p->nv = nv;
+  p->nslices = (nv + kSlice - 1) / kSlice;
+  const size_t n = 3 * (size_t)nv;
+  int rc = 0;
+  if ((rc = dalloc(&p->vec, n * kNumBuf)) || (rc = dalloc(&p->ev, n)) ||
+      (rc = dalloc(&p->b, n)) || (rc = dalloc(&p->dinv, n)) ||
+      (rc = dalloc(&p->part, (size_t)nitems_of(nv) * kPart)) || (rc = dalloc(&p->cnt, 1)) ||
+      (rc = dalloc(&p->st, 1)) || (rc = dalloc(&p->slice_off, p->nslices + 1))) {
+    free_problem_arrays(p);
+    delete p;
+    return rc;
+  }
+  cudaMemsetAsync(p->vec, 0, n * kNumBuf * sizeof(double), c->stream);
+  *out = p;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_destroy(mprgp_problem *p) {
+  if (!p) return MPRGP_OK;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  free_problem_arrays(p);
+  delete p;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, const int *cols,
+                             const double *vals, int precisions, int on_device) {
+  if (!p || nnzb <= 0 || !row_ptr || !cols || !vals || (precisions & 3) == 0)
+    return fail(MPRGP_INVALID, "set_matrix");
+  mprgp_context *c = p->ctx;
+  cudaStream_t s = c->stream;
+  const int nv = p->nv;
+  std::vector<int> h_ptr(nv + 1);
+  if (on_device) {
+    CK(cudaMemcpy(h_ptr.data(), row_ptr, sizeof(int) * (nv + 1), cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(h_ptr.data(), row_ptr, sizeof(int) * (nv + 1));
+  }
+  if (h_ptr[0] != 0 || h_ptr[nv] != nnzb) return fail(MPRGP_INVALID, "row_ptr ends");
+  for (int r = 0; r < nv; ++r)
+    if (h_ptr[r + 1] < h_ptr[r]) return fail(MPRGP_INVALID, "row_ptr not monotone");
+  if (!on_device)
+    for (int q = 0; q < nnzb; ++q)
+      if (cols[q] < 0 || cols[q] >= nv) return fail(MPRGP_INVALID, "column out of range");
+  std::vector<int> off(p->nslices + 1, 0);
+  for (int sl = 0; sl < p->nslices; ++sl) {
+    int w = 0;
+    for (int r = sl * kSlice; r < std::min(nv, (sl + 1) * kSlice); ++r)
+      w = std::max(w, h_ptr[r + 1] - h_ptr[r]);
+    off[sl + 1] = off[sl] + w;
+  }
+  const int slots = off[p->nslices];
+  if (slots != p->slots || (precisions & 1) != p->has64 || ((precisions >> 1) & 1) != p->has32) {
+    dfree(p->cols);
+    dfree(p->v64);
+    dfree(p->v32);
+    int rc = dalloc(&p->cols, (size_t)slots * kSlice);
+    if (!rc && (precisions & 1)) rc = dalloc(&p->v64, (size_t)slots * kSlice * 9);
+    if (!rc && (precisions & 2)) rc = dalloc(&p->v32, (size_t)slots * kSlice * 9);
+    if (rc) return rc;
+    p->slots = slots;
+    p->has64 = precisions & 1;
+    p->has32 = (precisions >> 1) & 1;
+  }
+  CK(cudaMemcpyAsync(p->slice_off, off.data(), sizeof(int) * (p->nslices + 1),
+                     cudaMemcpyHostToDevice, s));
+  const int *d_ptr = row_ptr, *d_cols = cols;
+  const double *d_vals = vals;
+  int *t_ptr = nullptr, *t_cols = nullptr;
+  double *t_vals = nullptr;
+  if (!on_device) {
+    int rc = dalloc(&t_ptr, nv + 1);
+    if (!rc) rc = dalloc(&t_cols, nnzb);
+    if (!rc) rc = dalloc(&t_vals, (size_t)nnzb * 9);
+    if (rc) { dfree(t_ptr); dfree(t_cols); dfree(t_vals); return rc; }
+    CK(cudaMemcpyAsync(t_ptr, row_ptr, sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(t_cols, cols, sizeof(int) * nnzb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(t_vals, vals, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+    d_ptr = t_ptr;
+    d_cols = t_cols;
+    d_vals = t_vals;
+  }
+  launch_bsr_to_sell(nv, d_ptr, d_cols, d_vals, p->slice_off, p->cols, p->v64, p->v32, p->dinv, s);
+  cudaError_t e = cudaGetLastError();
+  if (!on_device) {
+    cudaStreamSynchronize(s);
+    dfree(t_ptr);
+    dfree(t_cols);
+    dfree(t_vals);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
+  p->nnzb = nnzb;
+  p->planes_dirty = 1;  // 1/diag(J D^-1 J^T) depends on D
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_rhs(mprgp_problem *p, const double *b, int on_device) {
+  if (!p || !b) return fail(MPRGP_INVALID, "set_rhs");
+  CK(cudaMemcpyAsync(p->b, b, sizeof(double) * 3 * (size_t)p->nv,
+                     on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                     p->ctx->stream));
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const double *planes,
+                             int on_device) {
+  if (!p || !plane_ptr) return fail(MPRGP_INVALID, "set_planes");
+  const int nv = p->nv;
+  std::vector<int> h(nv + 1);
+  if (on_device) CK(cudaMemcpy(h.data(), plane_ptr, sizeof(int) * (nv + 1), cudaMemcpyDeviceToHost));
+  else std::memcpy(h.data(), plane_ptr, sizeof(int) * (nv + 1));
+  if (h[0] != 0) return fail(MPRGP_INVALID, "plane_ptr[0] != 0");
+  for (int v = 0; v < nv; ++v) {
+    const int k = h[v + 1] - h[v];
+    if (k < 0 || k > kMaxPlanes) return fail(MPRGP_INVALID, "0..3 planes per vertex");
+  }
+  const int m = h[nv];
+  if (m > 0 && !planes) return fail(MPRGP_INVALID, "planes");
+  cudaStream_t s = p->ctx->stream;
+  if (m != p->m || p->cons != 1) {
+    dfree(p->plane_ptr); dfree(p->planes_raw); dfree(p->planes); dfree(p->pl_nn);
+    dfree(p->pl_indn); dfree(p->face);
+    int rc = dalloc(&p->plane_ptr, nv + 1);
+    if (!rc) rc = dalloc(&p->planes_raw, 4 * (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(&p->planes, 4 * (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(&p->pl_nn, (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(&p->pl_indn, (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(&p->face, (size_t)std::max(m, 1));
+    if (rc) return rc;
+  }
+  CK(cudaMemcpyAsync(p->plane_ptr, h.data(), sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
+  if (m > 0)
+    CK(cudaMemcpyAsync(p->planes_raw, planes, sizeof(double) * 4 * (size_t)m,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(p->face, 0, std::max(m, 1), s));
+  p->m = m;
+  p->face_len = m;
+  p->cons = 1;
+  p->planes_dirty = 1;
+  p->h_plane_ptr.swap(h);
+  CK(cudaStreamSynchronize(s));  // host staging vector `h` is released next
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_bounds(mprgp_problem *p, const double *L, const double *U) {
+  if (!p || !L) return fail(MPRGP_INVALID, "set_bounds");
+  const size_t n = 3 * (size_t)p->nv;
+  cudaStream_t s = p->ctx->stream;
+  if (p->cons < 2) {
+    dfree(p->face);
+    int rc = dalloc(&p->L, n);
+    if (!rc) rc = dalloc(&p->U, n);
+    if (!rc) rc = dalloc(&p->face, n);
+    if (rc) return rc;
+  }
+  CK(cudaMemcpyAsync(p->L, L, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (U) CK(cudaMemcpyAsync(p->U, U, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(p->face, 0, n, s));
+  CK(cudaStreamSynchronize(s));
+  p->cons = U ? 3 : 2;
+  p->face_len = (int)n;
+  p->m = (int)n;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_x(mprgp_problem *p, const double *x, int on_device) {
+  if (!p || !x) return fail(MPRGP_INVALID, "set_x");
+  const size_t n = 3 * (size_t)p->nv;
+  CK(cudaMemcpyAsync(p->vec + (size_t)(B_X0 + p->xc) * n, x, sizeof(double) * n,
+                     on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                     p->ctx->stream));
+  return MPRGP_OK;
+}
+
+int mprgp_problem_get_x(mprgp_problem *p, double *x, int on_device) {
+  if (!p || !x) return fail(MPRGP_INVALID, "get_x");
+  const size_t n = 3 * (size_t)p->nv;
+  CK(cudaMemcpyAsync(x, p->vec + (size_t)(B_X0 + p->xc) * n, sizeof(double) * n,
+                     on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                     p->ctx->stream));
+  if (!on_device) CK(cudaStreamSynchronize(p->ctx->stream));
+  return MPRGP_OK;
+}
+
+int mprgp_problem_num_constraints(mprgp_problem *p, int *m) {
+  if (!p || !m) return fail(MPRGP_INVALID, "num_constraints");
+  *m = p->face_len;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_get_face(mprgp_problem *p, unsigned char *face) {
+  if (!p || !face) return fail(MPRGP_INVALID, "get_face");
+  if (p->face_len == 0) return MPRGP_OK;
+  CK(cudaMemcpyAsync(face, p->face, p->face_len, cudaMemcpyDeviceToHost, p->ctx->stream));
+  CK(cudaStreamSynchronize(p->ctx->stream));
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_ev(mprgp_problem *p, const double *ev) {
+  if (!p) return fail(MPRGP_INVALID, "set_ev");
+  if (!ev) { p->ev_valid = 0; return MPRGP_OK; }
+  CK(cudaMemcpyAsync(p->ev, ev, sizeof(double) * 3 * (size_t)p->nv, cudaMemcpyHostToDevice,
+                     p->ctx->stream));
+  p->ev_valid = 1;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_get_ev(mprgp_problem *p, double *ev, int *valid) {
+  if (!p) return fail(MPRGP_INVALID, "get_ev");
+  if (valid) *valid = p->ev_valid;
+  if (ev && p->ev_valid) {
+    CK(cudaMemcpyAsync(ev, p->ev, sizeof(double) * 3 * (size_t)p->nv, cudaMemcpyDeviceToHost,
+                       p->ctx->stream));
+    CK(cudaStreamSynchronize(p->ctx->stream));
+  }
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_trace(mprgp_problem *p, int capacity) {
+  if (!p || capacity < 0) return fail(MPRGP_INVALID, "set_trace");
+  dfree(p->trace);
+  p->trace_cap = 0;
+  p->trace_n = 0;
+  if (capacity == 0) return MPRGP_OK;
+  int rc = dalloc(&p->trace, 4 * (size_t)capacity);
+  if (rc) return rc;
+  p->trace_cap = capacity;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_get_trace(mprgp_problem *p, double *out, int capacity, int *count) {
+  if (!p) return fail(MPRGP_INVALID, "get_trace");
+  const int n = std::min(p->trace_n, p->trace_cap);
+  if (count) *count = n;
+  if (out && n > 0) {
+    CK(cudaMemcpy(out, p->trace, sizeof(double) * 4 * std::min(n, capacity),
+                  cudaMemcpyDeviceToHost));
+  }
+  return MPRGP_OK;
+}
+
+int mprgp_problem_solve(mprgp_problem *p, const mprgp_options *opt, mprgp_stats *stats) {
+  if (!p || !opt) return fail(MPRGP_INVALID, "solve");
+  CK(cudaSetDevice(p->ctx->device));
+  mprgp_problem *arr[1] = {p};
+  const int rc = run_engine(p->ctx, 1, arr, opt, stats);
+  if (rc == MPRGP_OK && stats) return stats->code;
+  return rc;
+}
+
+int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int precision) {
+  if (!p || !x_dev || !y_dev || !p->cols) return fail(MPRGP_INVALID, "spmv");
+  const bool f32 = precision == MPRGP_PREC_MIXED;
+  if ((f32 && !p->has32) || (!f32 && !p->has64)) return fail(MPRGP_INVALID, "spmv precision");
+  SellMatrix A;
+  A.nslices = p->nslices;
+  A.slice_off = p->slice_off;
+  A.cols = p->cols;
+  A.v64 = p->v64;
+  A.v32 = p->v32;
+  launch_spmv(A, p->nv, f32, x_dev, y_dev, p->ctx->stream);
+  CK(cudaGetLastError());
+  return MPRGP_OK;
+}
+
+int mprgp_solve_batch(mprgp_context *c, int count, mprgp_problem *const *probs,
+                      const mprgp_options *opts, mprgp_stats *stats) {
+  if (!c || count <= 0 || !probs || !opts) return fail(MPRGP_INVALID, "solve_batch");
+  CK(cudaSetDevice(c->device));
+  return run_engine(c, count, probs, opts, stats);
+}
+
+int mprgp_solve_bsr(mprgp_context *c, int nv, int nnzb, const int *row_ptr, const int *cols,
+                    const double *vals, const double *b, const int *plane_ptr,
+                    const double *planes, const double *L, const double *U,
+                    const mprgp_options *opt, double *x, unsigned char *face, double *ev,
+                    mprgp_stats *stats) {
+  if (!c || !opt || !x || !b) return fail(MPRGP_INVALID, "solve_bsr");
+  CK(cudaSetDevice(c->device));
+  if (c->scratch && c->scratch->nv != nv) {
+    mprgp_problem_destroy(c->scratch);
+    c->scratch = nullptr;
+  }
+  if (!c->scratch) {
+    int rc = mprgp_problem_create(c, nv, &c->scratch);
+    if (rc) return rc;
+  }
+  mprgp_problem *p = c->scratch;
+  const int prec = opt->precision == MPRGP_PREC_MIXED ? 3 : 1;
+  int rc = mprgp_problem_set_matrix(p, nnzb, row_ptr, cols, vals, prec, 0);
+  if (!rc) rc = mprgp_problem_set_rhs(p, b, 0);
+  if (!rc) {
+    if (opt->kind >= MPRGP_KIND_DECOUPLED) rc = mprgp_problem_set_planes(p, plane_ptr, planes, 0);
+    else rc = mprgp_problem_set_bounds(p, L, opt->kind == MPRGP_KIND_BOX ? U : nullptr);
+  }
+  p->xc = 0;
+  if (!rc) rc = mprgp_problem_set_x(p, x, 0);
+  p->ev_valid = 0;
+  if (!rc && ev && opt->use_ev) rc = mprgp_problem_set_ev(p, ev);
+  if (rc) return rc;
+  mprgp_stats local;
+  mprgp_problem *arr[1] = {p};
+  rc = run_engine(c, 1, arr, opt, &local);
+  if (rc < MPRGP_NOT_CONVERGED) {
+    if (stats) *stats = local;
+    return rc;
+  }
+  rc = mprgp_problem_get_x(p, x, 0);
+  if (!rc && face) rc = mprgp_problem_get_face(p, face);
+  if (!rc && ev && local.ev_updated) rc = mprgp_problem_get_ev(p, ev, nullptr);
+  if (stats) *stats = local;
+  if (rc) return rc;
+  return local.code;
+}
+
+}  // extern "C"

@@ -1,0 +1,1465 @@
+// Persistent MPRGP engine for sm_103a.
+//
+// Each macro-phase every CTA walks its share of the item list (256 vertex
+// rows of one instance per item), runs that instance's current phase on those
+// rows, and writes one partial-sum record per item.  The CTA that finishes an
+// instance's last item reduces the records in item order and advances the
+// instance's state machine.  A bounded grid barrier ends the macro-phase.
+//
+// Row kernels restate the per-vertex arithmetic of the reference projectors
+// and preconditioners (src/MPRGPSolver/MPRGPProjection.h,
+// MPRGPPrecondition.h); the state machine restates MPRGPMonotonic::solve and
+// MPRGP::solve (MPRGPSolver.h:148-454).  Every constraint row touches one
+// vertex, so all projector work is local to a row and fuses into the SpMV
+// epilogues; only the reductions cross rows.
+#include <cfloat>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace mprgp {
+
+constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:9)
+
+// ------------------------------------------------------------ primitives --
+__device__ __forceinline__ long long gtimer() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Vectors written earlier in this kernel are read through L2 (ld.global.cg):
+// another SM may have produced them and L1 is not coherent.
+__device__ __forceinline__ void ld3(const double *b, int v, double o[3]) {
+  const double *q = b + 3 * (size_t)v;
+  o[0] = __ldcg(q);
+  o[1] = __ldcg(q + 1);
+  o[2] = __ldcg(q + 2);
+}
+__device__ __forceinline__ void st3(double *b, int v, const double o[3]) {
+  double *q = b + 3 * (size_t)v;
+  q[0] = o[0];
+  q[1] = o[1];
+  q[2] = o[2];
+}
+__device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  unsigned long long z = x;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+// Seeded stand-in for Eigen's setRandom() (MPRGPSolver.h:51): uniform [-1,1).
+__device__ __forceinline__ double seeded_uniform(unsigned long long seed, unsigned long long i) {
+  const unsigned long long h = mix64(seed * 0x9E3779B97F4A7C15ull + i);
+  return 2.0 * ((double)(h >> 11) * 1.1102230246251565e-16) - 1.0;
+}
+
+// ------------------------------------------------------------ SpMV rows --
+// One thread per block row.  The nine block entries and the column of slot j
+// are lane-contiguous in the SELL layout, so each load instruction of a warp
+// is one coalesced line; x is gathered per neighbour vertex.  VT is the value
+// type of A and of the accumulator (FP32 accumulation for the FP32 copy).
+struct SrcV {
+  const double *p;
+  __device__ __forceinline__ void operator()(int c, double o[3]) const { ld3(p, c, o); }
+};
+struct SrcScale {  // p / s   (the power method's tmpOut /= norm)
+  const double *p;
+  double s;
+  __device__ __forceinline__ void operator()(int c, double o[3]) const {
+    ld3(p, c, o);
+    o[0] /= s;
+    o[1] /= s;
+    o[2] /= s;
+  }
+};
+struct SrcPNew {  // z - beta p   (CGStep's p = z - beta*p)
+  const double *z, *p;
+  double beta;
+  __device__ __forceinline__ void operator()(int c, double o[3]) const {
+    double zz[3], pp[3];
+    ld3(z, c, zz);
+    ld3(p, c, pp);
+    o[0] = zz[0] - beta * pp[0];
+    o[1] = zz[1] - beta * pp[1];
+    o[2] = zz[2] - beta * pp[2];
+  }
+};
+
+template <typename VT, typename Src>
+__device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
+                                         const Src &src, double out[3]) {
+  const int s = v >> 5, lane = v & 31;
+  const int j0 = __ldg(A.slice_off + s), j1 = __ldg(A.slice_off + s + 1);
+  VT a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll 2
+  for (int j = j0; j < j1; ++j) {
+    const int c = __ldg(A.cols + (size_t)j * kSlice + lane);
+    const VT *q = vals + (size_t)j * (9 * kSlice) + lane;
+    const VT m0 = __ldg(q), m1 = __ldg(q + 32), m2 = __ldg(q + 64);
+    const VT m3 = __ldg(q + 96), m4 = __ldg(q + 128), m5 = __ldg(q + 160);
+    const VT m6 = __ldg(q + 192), m7 = __ldg(q + 224), m8 = __ldg(q + 256);
+    double xv[3];
+    src(c, xv);
+    const VT x0 = (VT)xv[0], x1 = (VT)xv[1], x2 = (VT)xv[2];
+    a0 = fma(m0, x0, a0); a0 = fma(m1, x1, a0); a0 = fma(m2, x2, a0);
+    a1 = fma(m3, x0, a1); a1 = fma(m4, x1, a1); a1 = fma(m5, x2, a1);
+    a2 = fma(m6, x0, a2); a2 = fma(m7, x1, a2); a2 = fma(m8, x2, a2);
+  }
+  out[0] = (double)a0;
+  out[1] = (double)a1;
+  out[2] = (double)a2;
+}
+
+// Two products with one pass over A (both FP64).
+template <typename S1, typename S2>
+__device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &s1, const S2 &s2,
+                                          double o1[3], double o2[3]) {
+  const int s = v >> 5, lane = v & 31;
+  const int j0 = __ldg(A.slice_off + s), j1 = __ldg(A.slice_off + s + 1);
+  double a0 = 0, a1 = 0, a2 = 0, b0 = 0, b1 = 0, b2 = 0;
+  for (int j = j0; j < j1; ++j) {
+    const int c = __ldg(A.cols + (size_t)j * kSlice + lane);
+    const double *q = A.v64 + (size_t)j * (9 * kSlice) + lane;
+    double m[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) m[e] = __ldg(q + 32 * e);
+    double x[3], y[3];
+    s1(c, x);
+    s2(c, y);
+    a0 = fma(m[0], x[0], a0); a0 = fma(m[1], x[1], a0); a0 = fma(m[2], x[2], a0);
+    a1 = fma(m[3], x[0], a1); a1 = fma(m[4], x[1], a1); a1 = fma(m[5], x[2], a1);
+    a2 = fma(m[6], x[0], a2); a2 = fma(m[7], x[1], a2); a2 = fma(m[8], x[2], a2);
+    b0 = fma(m[0], y[0], b0); b0 = fma(m[1], y[1], b0); b0 = fma(m[2], y[2], b0);
+    b1 = fma(m[3], y[0], b1); b1 = fma(m[4], y[1], b1); b1 = fma(m[5], y[2], b1);
+    b2 = fma(m[6], y[0], b2); b2 = fma(m[7], y[1], b2); b2 = fma(m[8], y[2], b2);
+  }
+  o1[0] = a0; o1[1] = a1; o1[2] = a2;
+  o2[0] = b0; o2[1] = b1; o2[2] = b2;
+}
+
+template <typename Src>
+__device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int v, const Src &src,
+                                         double out[3]) {
+  if (fp32) spmv_row<float>(D.A, D.A.v32, v, src, out);
+  else spmv_row<double>(D.A, D.A.v64, v, src, out);
+}
+
+// --------------------------------------------------- vertex constraints --
+struct VCons {
+  int k, base;
+  double n[kMaxPlanes][3], c[kMaxPlanes], nn[kMaxPlanes], indn[kMaxPlanes];
+  double lo[3], hi[3];
+};
+
+__device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
+  if (D.kind >= KIND_DECOUPLED) {
+    const int b = __ldg(D.plane_ptr + v), e = __ldg(D.plane_ptr + v + 1);
+    C.base = b;
+    C.k = e - b;
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j) {
+      if (j < C.k) {
+        const double *q = D.planes + 4 * (size_t)(b + j);
+        C.n[j][0] = __ldg(q);
+        C.n[j][1] = __ldg(q + 1);
+        C.n[j][2] = __ldg(q + 2);
+        C.c[j] = __ldg(q + 3);
+        C.nn[j] = __ldg(D.pl_nn + b + j);
+        C.indn[j] = __ldg(D.pl_indn + b + j);
+      } else {
+        C.n[j][0] = C.n[j][1] = C.n[j][2] = C.c[j] = 0.0;
+        C.nn[j] = 1.0;
+        C.indn[j] = 0.0;
+      }
+    }
+  } else {
+    C.base = 3 * v;
+    C.k = 3;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      C.lo[d] = __ldg(D.L + 3 * (size_t)v + d);
+      C.hi[d] = (D.kind == KIND_BOX) ? __ldg(D.U + 3 * (size_t)v + d) : DBL_MAX;
+    }
+  }
+}
+
+// Face codes of the vertex's constraint rows, 2 bits each.
+__device__ __forceinline__ int load_face(const InstDesc &D, const VCons &C) {
+  int f = 0;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    if (j < C.k) f |= (int)__ldcg(D.face + C.base + j) << (2 * j);
+  return f;
+}
+__device__ __forceinline__ int fcode(int f, int j) { return (f >> (2 * j)) & 3; }
+
+// DECIDE_FACE (MPRGPProjection.h:78-90, 187-201, 283-297).  Returns the sum
+// of the codes (COUNT_CONSTRAINTS, MPRGPUtility.h:98-106).
+__device__ __forceinline__ int decide_face(const InstDesc &D, const VCons &C, const double x[3],
+                                           int &f) {
+  f = 0;
+  int cnt = 0;
+  if (D.kind >= KIND_DECOUPLED) {
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j) {
+      if (j < C.k) {
+        const int a = fabs(dot3(C.n[j], x) - C.c[j]) < kEps ? 1 : 0;
+        f |= a << (2 * j);
+        cnt += a;
+        D.face[C.base + j] = (unsigned char)a;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int a = 0;
+      if (fabs(x[d] - C.lo[d]) < kEps) a = 2;
+      else if (D.kind == KIND_BOX && fabs(x[d] - C.hi[d]) < kEps) a = 1;
+      f |= a << (2 * d);
+      cnt += a;
+      D.face[C.base + d] = (unsigned char)a;
+    }
+  }
+  return cnt;
+}
+
+// Small SPD solve on the planes selected by `mask` (<= 3), Cramer's rule.
+__device__ __forceinline__ bool solve_subset(const double G[3][3], const double q[3], int mask,
+                                             double lam[3]) {
+  lam[0] = lam[1] = lam[2] = 0.0;
+  int idx[3], s = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (mask & (1 << i)) idx[s++] = i;
+  if (s == 1) {
+    const int a = idx[0];
+    if (!(G[a][a] > 0.0)) return false;
+    lam[a] = q[a] / G[a][a];
+  } else if (s == 2) {
+    const int a = idx[0], b = idx[1];
+    const double det = G[a][a] * G[b][b] - G[a][b] * G[b][a];
+    if (!(det > 0.0)) return false;
+    lam[a] = (q[a] * G[b][b] - G[a][b] * q[b]) / det;
+    lam[b] = (G[a][a] * q[b] - G[b][a] * q[a]) / det;
+  } else if (s == 3) {
+    const double c00 = G[1][1] * G[2][2] - G[1][2] * G[2][1];
+    const double c01 = G[1][2] * G[2][0] - G[1][0] * G[2][2];
+    const double c02 = G[1][0] * G[2][1] - G[1][1] * G[2][0];
+    const double det = G[0][0] * c00 + G[0][1] * c01 + G[0][2] * c02;
+    if (!(det > 0.0)) return false;
+    const double c10 = G[0][2] * G[2][1] - G[0][1] * G[2][2];
+    const double c11 = G[0][0] * G[2][2] - G[0][2] * G[2][0];
+    const double c12 = G[0][1] * G[2][0] - G[0][0] * G[2][1];
+    const double c20 = G[0][1] * G[1][2] - G[0][2] * G[1][1];
+    const double c21 = G[0][2] * G[1][0] - G[0][0] * G[1][2];
+    const double c22 = G[0][0] * G[1][1] - G[0][1] * G[1][0];
+    lam[0] = (c00 * q[0] + c10 * q[1] + c20 * q[2]) / det;
+    lam[1] = (c01 * q[0] + c11 * q[1] + c21 * q[2]) / det;
+    lam[2] = (c02 * q[0] + c12 * q[1] + c22 * q[2]) / det;
+  }
+  return true;
+}
+
+// min 0.5 l^T G l - q^T l, l >= 0 over the planes in `allow` (bit mask), by
+// enumerating supports in order of size, then mask value; the first support
+// that satisfies KKT wins.  Same procedure as the oracle's per-block solver
+// for solveQP(G, q, I, 0, l) (SimpleQP.h:17-48).
+__device__ __forceinline__ void nonneg_qp3(const double G[3][3], const double q[3], int allow,
+                                           double lam[3]) {
+  double scale = 1e-300;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (allow & (1 << i)) scale = fmax(scale, fabs(q[i]));
+  const double tol = 1e-12 * scale;
+  double best_viol = DBL_MAX, best[3] = {0.0, 0.0, 0.0};
+  // Supports are subsets of `allow`; visit them by popcount, then value.
+  for (int size = 0; size <= 3; ++size) {
+    for (int mask = 0; mask < 8; ++mask) {
+      if ((mask & ~allow) || __popc(mask) != size) continue;
+      double t[3];
+      if (!solve_subset(G, q, mask, t)) continue;
+      double viol = 0.0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        if (!(allow & (1 << i))) continue;
+        if (mask & (1 << i)) {
+          viol = fmax(viol, -t[i]);
+        } else {
+          const double gr = G[i][0] * t[0] + G[i][1] * t[1] + G[i][2] * t[2] - q[i];
+          viol = fmax(viol, -gr);
+        }
+      }
+      if (viol <= tol) {
+        lam[0] = fmax(t[0], 0.0);
+        lam[1] = fmax(t[1], 0.0);
+        lam[2] = fmax(t[2], 0.0);
+        return;
+      }
+      if (viol < best_viol) {
+        best_viol = viol;
+        best[0] = t[0];
+        best[1] = t[1];
+        best[2] = t[2];
+      }
+    }
+  }
+  lam[0] = fmax(best[0], 0.0);
+  lam[1] = fmax(best[1], 0.0);
+  lam[2] = fmax(best[2], 0.0);
+}
+
+__device__ __forceinline__ void gram(const VCons &C, double G[3][3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) G[a][b] = dot3(C.n[a], C.n[b]);
+}
+
+// project (MPRGPProjection.h:56-62, 163-169, 333-348, 412-430).
+__device__ void project_v(const InstDesc &D, const VCons &C, const double x[3], double y[3]) {
+  y[0] = x[0];
+  y[1] = x[1];
+  y[2] = x[2];
+  if (D.kind == KIND_DECOUPLED) {
+    double lam[kMaxPlanes];
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      lam[j] = (j < C.k) ? fmax((C.c[j] - dot3(C.n[j], x)) / C.nn[j], 0.0) : 0.0;
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      if (j < C.k)
+        for (int d = 0; d < 3; ++d) y[d] += C.n[j][d] * lam[j];
+  } else if (D.kind == KIND_PLANES) {
+    if (C.k == 0) return;
+    double G[3][3], q[3], lam[3];
+    gram(C, G);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) q[j] = (j < C.k) ? C.c[j] - dot3(C.n[j], x) : 0.0;
+    nonneg_qp3(G, q, (1 << C.k) - 1, lam);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (j < C.k)
+        for (int d = 0; d < 3; ++d) y[d] += C.n[j][d] * lam[j];
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) y[d] = fmin(fmax(x[d], C.lo[d]), C.hi[d]);
+  }
+}
+
+// PHI (MPRGPProjection.h:63-65, 170-172, 349-367, 431-449).
+__device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3],
+                      double phi[3]) {
+  phi[0] = g[0];
+  phi[1] = g[1];
+  phi[2] = g[2];
+  if (D.kind == KIND_DECOUPLED) {
+    double lam[kMaxPlanes];
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      lam[j] = (j < C.k && fcode(f, j)) ? -dot3(C.n[j], g) / C.nn[j] : 0.0;
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      if (j < C.k)
+        for (int d = 0; d < 3; ++d) phi[d] += C.n[j][d] * lam[j];
+  } else if (D.kind == KIND_PLANES) {
+    int act = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      if (j < C.k && fcode(f, j)) act |= 1 << j;
+    if (!act) return;
+    double G[3][3], q[3], lam[3];
+    gram(C, G);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? -dot3(C.n[j], g) : 0.0;
+    if (!solve_subset(G, q, act, lam)) return;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (act & (1 << j))
+        for (int d = 0; d < 3; ++d) phi[d] += C.n[j][d] * lam[j];
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (fcode(f, d)) phi[d] = 0.0;
+  }
+}
+
+// BETA (MPRGPProjection.h:66-77, 173-186, 368-383, 450-467).
+__device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[3],
+                       const double phi[3], double beta[3]) {
+  if (D.kind == KIND_DECOUPLED) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) beta[d] = g[d] - phi[d];
+    double lam[kMaxPlanes];
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j) {
+      double l = (j < C.k) ? dot3(C.n[j], beta) : 0.0;
+      if (j < C.k && fcode(f, j)) l = fmax(0.0, l / C.nn[j]);
+      lam[j] = l;  // rows off the face keep (J beta)_i, as the reference does
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      if (j < C.k)
+        for (int d = 0; d < 3; ++d) beta[d] -= C.n[j][d] * lam[j];
+  } else if (D.kind == KIND_PLANES) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) beta[d] = g[d] - phi[d];
+    int act = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      if (j < C.k && fcode(f, j)) act |= 1 << j;
+    if (!act) return;
+    double G[3][3], q[3], lam[3];
+    gram(C, G);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? dot3(C.n[j], beta) : 0.0;
+    nonneg_qp3(G, q, act, lam);
+    double gp[3] = {beta[0], beta[1], beta[2]};
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (act & (1 << j))
+        for (int d = 0; d < 3; ++d) gp[d] += C.n[j][d] * (-lam[j]);
+    beta[0] = gp[0];
+    beta[1] = gp[1];
+    beta[2] = gp[2];
+  } else {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int fc = fcode(f, d);
+      if (fc == 0) beta[d] = 0.0;
+      else if (fc == 1) beta[d] = fmax(g[d], 0.0);
+      else beta[d] = fmin(g[d], 0.0);
+    }
+  }
+}
+
+// Preconditioner solve (MPRGPPrecondition.h:52-64, 91-105).
+__device__ void precond_v(const InstDesc &D, const VCons &C, int f, int v, const double g[3],
+                          const double phi[3], double z[3]) {
+  if (D.pre == PRE_NONE || (D.pre == PRE_DECOUPLE && D.m == 0)) {
+    z[0] = phi[0];
+    z[1] = phi[1];
+    z[2] = phi[2];
+    return;
+  }
+  double di[3];
+  di[0] = __ldg(D.dinv + 3 * (size_t)v);
+  di[1] = __ldg(D.dinv + 3 * (size_t)v + 1);
+  di[2] = __ldg(D.dinv + 3 * (size_t)v + 2);
+  if (D.pre == PRE_INFACE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) z[d] = phi[d] * di[d];
+    return;
+  }
+  double Dg[3] = {di[0] * g[0], di[1] * g[1], di[2] * g[2]};
+  double t[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int j = 0; j < kMaxPlanes; ++j) {
+    if (j < C.k && fcode(f, j)) {
+      const double lam = C.indn[j] * dot3(C.n[j], Dg);
+      for (int d = 0; d < 3; ++d) t[d] += C.n[j][d] * lam;
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) z[d] = Dg[d] - di[d] * t[d];
+}
+
+// Per-row term of PHITPHI (MPRGPProjection.h:91-106, 202-221, 384-393): for
+// planes (x - P(x - abar phi)) . phi, scaled and clamped once in the finalizer.
+__device__ double phitphi_v(const InstDesc &D, const VCons &C, double abar, const double x[3],
+                            const double phi[3]) {
+  if (D.kind >= KIND_DECOUPLED) {
+    const double xa[3] = {x[0] - abar * phi[0], x[1] - abar * phi[1], x[2] - abar * phi[2]};
+    double px[3];
+    project_v(D, C, xa, px);
+    return (x[0] - px[0]) * phi[0] + (x[1] - px[1]) * phi[1] + (x[2] - px[2]) * phi[2];
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double t = 0.0;
+    if (phi[d] > 0.0 && x[d] > C.lo[d]) t = fmin((x[d] - C.lo[d]) / abar, phi[d]);
+    else if (D.kind == KIND_BOX && phi[d] < 0.0 && x[d] < C.hi[d])
+      t = fmax((x[d] - C.hi[d]) / abar, phi[d]);
+    s += t * phi[d];
+  }
+  return s;
+}
+
+// isFeasible with the eps slack (MPRGPProjection.h:108-116, 223-232, 298-310).
+__device__ __forceinline__ int infeasible_v(const InstDesc &D, const VCons &C, const double y[3]) {
+  if (D.kind >= KIND_DECOUPLED) {
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j)
+      if (j < C.k && dot3(C.n[j], y) < C.c[j] - kEps) return 1;
+    return 0;
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (y[d] < C.lo[d] - kEps) return 1;
+    if (D.kind == KIND_BOX && y[d] > C.hi[d] + kEps) return 1;
+  }
+  return 0;
+}
+
+// stepLimit (MPRGPProjection.h:34-53, 139-162, 263-282), per-row minimum.
+__device__ double ratio_v(const InstDesc &D, const VCons &C, const double x[3], const double p[3]) {
+  double r = DBL_MAX;
+  if (D.kind >= KIND_DECOUPLED) {
+#pragma unroll
+    for (int j = 0; j < kMaxPlanes; ++j) {
+      if (j >= C.k) continue;
+      const double jd = dot3(C.n[j], p), jx = dot3(C.n[j], x);
+      if (jd > kEps && jx > C.c[j]) r = fmin(r, (jx - C.c[j]) / jd);
+    }
+    return r;
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (p[d] > kEps && x[d] > C.lo[d]) r = fmin(r, (x[d] - C.lo[d]) / p[d]);
+    else if (D.kind == KIND_BOX && p[d] < -kEps && x[d] < C.hi[d])
+      r = fmin(r, (x[d] - C.hi[d]) / p[d]);
+  }
+  return r;
+}
+
+__device__ __forceinline__ double *B(const InstDesc &D, int i) { return D.buf[i]; }
+
+// Shared epilogue once g is final for a row and the face is re-decided:
+// DECIDE_FACE(x); PHI(g); z = precond; p = z; then the loop top's BETA and
+// the sums |phi+beta|^2, beta.beta, PHITPHI, z.g, COUNT_CONSTRAINTS.
+__device__ void epilogue_full(const InstDesc &D, const InstState &S, const VCons &C, int v,
+                              const double x[3], const double g[3], double *part) {
+  int f;
+  const int act = decide_face(D, C, x, f);
+  double phi[3], z[3], beta[3];
+  phi_v(D, C, f, g, phi);
+  precond_v(D, C, f, v, g, phi, z);
+  beta_v(D, C, f, g, phi, beta);
+  st3(B(D, B_G0 + S.gc), v, g);
+  st3(B(D, B_Z0 + S.zc), v, z);
+  st3(B(D, B_P0 + S.pc), v, z);
+  st3(B(D, B_BT0 + S.bc), v, beta);
+  const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
+  part[0] += dot3(gp, gp);
+  part[1] += dot3(beta, beta);
+  part[2] += phitphi_v(D, C, S.alpha_bar, x, phi);
+  part[3] += dot3(z, g);
+  part[4] += (double)act;
+}
+
+// ------------------------------------------------------------- row work --
+__device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, int v,
+                                       double *part) {
+  const bool f32 = D.prec == PREC_MIXED;
+  if (S.phase == PH_POW_RAND) {
+    double t[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) t[d] = seeded_uniform(D.seed, 3ull * v + d);
+    st3(B(D, B_W1), v, t);
+    part[0] += dot3(t, t);
+    return;
+  }
+  const int k = S.pow_k;
+  const double *src = S.pow_src < 0 ? D.ev : B(D, S.pow_src);
+  double u[3];
+  ld3(src, v, u);
+  u[0] /= S.pow_scale;
+  u[1] /= S.pow_scale;
+  u[2] /= S.pow_scale;
+  if (S.phase == PH_POW_LAST || k >= 1) {
+    double t[3];
+    ld3(B(D, B_T0 + ((k - 1) & 1)), v, t);
+    const double d[3] = {u[0] - t[0], u[1] - t[1], u[2] - t[2]};
+    part[0] += dot3(d, d);
+  }
+  if (S.phase == PH_POW_LAST) return;
+  st3(B(D, B_T0 + (k & 1)), v, u);
+  double w[3];
+  spmv_any(D, f32, v, SrcScale{src, S.pow_scale}, w);
+  st3(B(D, (k & 1) ? B_W1 : B_W), v, w);
+  part[1] += dot3(w, w);
+}
+
+__device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int v,
+                                      double *part) {
+  VCons C;
+  load_cons(D, v, C);
+  if (S.phase == PH_PROJ0 || S.phase == PH_FINAL) {
+    double x[3], y[3];
+    ld3(B(D, B_X0 + S.xc), v, x);
+    project_v(D, C, x, y);
+    st3(B(D, B_X0 + S.xc), v, y);
+    return;
+  }
+  // PH_INIT, PH_EXP_C, PH_PL_EXP_B: g = A x - b, then the full epilogue.
+  if (S.phase == PH_INIT && S.ev_upd) {
+    double t[3];
+    ld3(B(D, S.ev_src), v, t);
+    st3(D.ev, v, t);
+  }
+  double x[3], ax[3];
+  ld3(B(D, B_X0 + S.xc), v, x);
+  spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
+  const double g[3] = {ax[0] - __ldg(D.b + 3 * (size_t)v), ax[1] - __ldg(D.b + 3 * (size_t)v + 1),
+                       ax[2] - __ldg(D.b + 3 * (size_t)v + 2)};
+  epilogue_full(D, S, C, v, x, g, part);
+}
+
+__device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, int v,
+                                         double *part) {
+  const bool f32 = D.prec == PREC_MIXED;
+  double p[3], ap[3], g[3];
+  ld3(B(D, B_G0 + S.gc), v, g);
+  if (S.phase == PH_CG_ENTRY || (S.phase == PH_PL_SPMV && S.p_is_z)) {
+    const double *pp = B(D, B_P0 + S.pc);
+    ld3(pp, v, p);
+    if (S.phase == PH_CG_ENTRY && !S.g_cons) {
+      double ax[3];
+      spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
+      double e[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) e[d] = (ax[d] - __ldg(D.b + 3 * (size_t)v + d)) - g[d];
+      st3(B(D, B_E), v, e);
+      part[2] += dot3(p, e);
+    }
+    spmv_any(D, f32 && S.phase != PH_PL_SPMV, v, SrcV{pp}, ap);
+  } else {
+    const double *zz = B(D, B_Z0 + S.zc), *po = B(D, B_P0 + S.pc);
+    double z[3];
+    ld3(zz, v, z);
+    ld3(po, v, p);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) p[d] = z[d] - S.beta_cg * p[d];
+    st3(B(D, B_P0 + (S.pc ^ 1)), v, p);
+    spmv_any(D, f32 && S.phase != PH_PL_SPMV, v, SrcPNew{zz, po, S.beta_cg}, ap);
+    if (S.e_nz && S.phase == PH_CG_SPMV) {
+      double e[3];
+      ld3(B(D, B_E), v, e);
+      part[2] += dot3(p, e);
+    }
+  }
+  st3(B(D, B_AP), v, ap);
+  part[0] += dot3(p, ap);
+  part[1] += dot3(p, g);
+  if (S.phase == PH_PL_SPMV) {
+    VCons C;
+    load_cons(D, v, C);
+    double x[3];
+    ld3(B(D, B_X0 + S.xc), v, x);
+    part[kMinSlot] = fmin(part[kMinSlot], ratio_v(D, C, x, p));
+  }
+}
+
+// Candidate y = x - alpha p: feasibility, the f(P(y)) correction terms and
+// the CG state that committing y would produce (CGMonotonicStep, :287-313).
+__device__ __noinline__ void row_cg_yf(const InstDesc &D, const InstState &S, int v,
+                                       double *part) {
+  VCons C;
+  load_cons(D, v, C);
+  const int f = load_face(D, C);
+  double x[3], p[3], ap[3], g[3];
+  ld3(B(D, B_X0 + S.xc), v, x);
+  ld3(B(D, B_P0 + S.pc), v, p);
+  ld3(B(D, B_AP), v, ap);
+  ld3(B(D, B_G0 + S.gc), v, g);
+  double y[3], gy[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    y[d] = x[d] - S.alpha * p[d];
+    gy[d] = g[d] - S.alpha * ap[d];
+  }
+  st3(B(D, B_X0 + (S.xc ^ 1)), v, y);
+  st3(B(D, B_G0 + (S.gc ^ 1)), v, gy);
+  double py[3];
+  project_v(D, C, y, py);
+  const double dl[3] = {py[0] - y[0], py[1] - y[1], py[2] - y[2]};
+  st3(B(D, B_W), v, dl);
+  if (dl[0] != 0.0 || dl[1] != 0.0 || dl[2] != 0.0) {
+    double gt[3] = {gy[0], gy[1], gy[2]};
+    if (S.e_nz) {
+      double e[3];
+      ld3(B(D, B_E), v, e);
+      gt[0] += e[0];
+      gt[1] += e[1];
+      gt[2] += e[2];
+    }
+    part[0] += dot3(dl, gt);
+    part[1] += 1.0;
+  }
+  part[2] += (double)infeasible_v(D, C, y);
+  double phi[3], z[3], beta[3];
+  phi_v(D, C, f, gy, phi);
+  precond_v(D, C, f, v, gy, phi, z);
+  beta_v(D, C, f, gy, phi, beta);
+  st3(B(D, B_Z0 + (S.zc ^ 1)), v, z);
+  st3(B(D, B_BT0 + (S.bc ^ 1)), v, beta);
+  const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
+  part[3] += dot3(z, ap);
+  part[4] += dot3(z, gy);
+  part[5] += dot3(gp, gp);
+  part[6] += dot3(beta, beta);
+  part[7] += phitphi_v(D, C, S.alpha_bar, y, phi);
+}
+
+// delta^T A delta over the rows where P(y) moved y (rare).
+__device__ __noinline__ void row_cg_dad(const InstDesc &D, const InstState &S, int v,
+                                        double *part) {
+  (void)S;
+  double dl[3];
+  ld3(B(D, B_W), v, dl);
+  if (dl[0] == 0.0 && dl[1] == 0.0 && dl[2] == 0.0) return;
+  double ad[3];
+  spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_W)}, ad);
+  part[0] += dot3(dl, ad);
+}
+
+// FP64 residual replacement for the mixed form: g = A64 x - b with the face
+// kept, then phi, z, beta and the sums for the current x.
+__device__ __noinline__ void row_ru(const InstDesc &D, const InstState &S, int v, double *part) {
+  VCons C;
+  load_cons(D, v, C);
+  const int f = load_face(D, C);
+  double x[3], ax[3], ap[3];
+  ld3(B(D, B_X0 + S.xc), v, x);
+  ld3(B(D, B_AP), v, ap);
+  spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
+  const double g[3] = {ax[0] - __ldg(D.b + 3 * (size_t)v), ax[1] - __ldg(D.b + 3 * (size_t)v + 1),
+                       ax[2] - __ldg(D.b + 3 * (size_t)v + 2)};
+  double phi[3], z[3], beta[3];
+  phi_v(D, C, f, g, phi);
+  precond_v(D, C, f, v, g, phi, z);
+  beta_v(D, C, f, g, phi, beta);
+  st3(B(D, B_G0 + S.gc), v, g);
+  st3(B(D, B_Z0 + S.zc), v, z);
+  st3(B(D, B_BT0 + S.bc), v, beta);
+  const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
+  part[0] += dot3(gp, gp);
+  part[1] += dot3(beta, beta);
+  part[2] += phitphi_v(D, C, S.alpha_bar, x, phi);
+  part[3] += dot3(z, g);
+  part[4] += dot3(z, ap);
+}
+
+__device__ __noinline__ void row_exp(const InstDesc &D, const InstState &S, int v, double *part) {
+  VCons C;
+  load_cons(D, v, C);
+  if (S.phase == PH_EXP_A) {  // y = P(x)
+    double x[3], y[3];
+    ld3(B(D, B_X0 + S.xc), v, x);
+    project_v(D, C, x, y);
+    st3(B(D, B_X0 + (S.xc ^ 1)), v, y);
+    return;
+  }
+  if (S.phase == PH_EXP_B) {  // g = A y - b; DECIDE_FACE(y); PHI; x = P(y - abar phi)
+    const double *yb = B(D, B_X0 + (S.xc ^ 1));
+    double y[3], ay[3];
+    ld3(yb, v, y);
+    spmv_row<double>(D.A, D.A.v64, v, SrcV{yb}, ay);
+    const double g[3] = {ay[0] - __ldg(D.b + 3 * (size_t)v),
+                         ay[1] - __ldg(D.b + 3 * (size_t)v + 1),
+                         ay[2] - __ldg(D.b + 3 * (size_t)v + 2)};
+    st3(B(D, B_G0 + S.gc), v, g);
+    int f;
+    decide_face(D, C, y, f);
+    double phi[3];
+    phi_v(D, C, f, g, phi);
+    const double yn[3] = {y[0] - S.alpha_bar * phi[0], y[1] - S.alpha_bar * phi[1],
+                          y[2] - S.alpha_bar * phi[2]};
+    part[0] += (double)infeasible_v(D, C, yn);
+    double x[3];
+    project_v(D, C, yn, x);
+    st3(B(D, B_X0 + S.xc), v, x);
+    return;
+  }
+  // PH_PL_EXP_A (ExpStep, :196-218): xt = x - af p; g -= af AP;
+  // DECIDE_FACE(xt); PHI(g); x = P(xt - abar phi).
+  double x[3], p[3], ap[3], g[3];
+  ld3(B(D, B_X0 + S.xc), v, x);
+  ld3(B(D, B_P0 + S.pc), v, p);
+  ld3(B(D, B_AP), v, ap);
+  ld3(B(D, B_G0 + S.gc), v, g);
+  double xt[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    xt[d] = x[d] - S.alpha * p[d];
+    g[d] -= S.alpha * ap[d];
+  }
+  st3(B(D, B_G0 + S.gc), v, g);
+  int f;
+  decide_face(D, C, xt, f);
+  double phi[3];
+  phi_v(D, C, f, g, phi);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) xt[d] -= S.alpha_bar * phi[d];
+  double xn[3];
+  project_v(D, C, xt, xn);
+  st3(B(D, B_X0 + S.xc), v, xn);
+}
+
+__device__ __noinline__ void row_prop(const InstDesc &D, const InstState &S, int v,
+                                      double *part) {
+  const double *db = B(D, B_BT0 + S.bc);
+  if (S.phase == PH_PROP_A || S.phase == PH_PL_PROP_A) {
+    double dd[3], ad[3], g[3];
+    ld3(db, v, dd);
+    if (S.phase == PH_PROP_A) {  // g = A x - B and AD = A D in one pass
+      double ax[3];
+      spmv2_row(D.A, v, SrcV{B(D, B_X0 + S.xc)}, SrcV{db}, ax, ad);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) g[d] = ax[d] - __ldg(D.b + 3 * (size_t)v + d);
+      st3(B(D, B_G0 + S.gc), v, g);
+    } else {
+      ld3(B(D, B_G0 + S.gc), v, g);
+      spmv_row<double>(D.A, D.A.v64, v, SrcV{db}, ad);
+    }
+    st3(B(D, B_W), v, ad);
+    part[0] += dot3(g, dd);
+    part[1] += dot3(dd, ad);
+    return;
+  }
+  // PH_PROP_B (PropStep, :219-243): x = P(x - alpha D); g -= alpha AD.
+  VCons C;
+  load_cons(D, v, C);
+  double x[3], dd[3], ad[3], g[3];
+  ld3(B(D, B_X0 + S.xc), v, x);
+  ld3(db, v, dd);
+  ld3(B(D, B_W), v, ad);
+  ld3(B(D, B_G0 + S.gc), v, g);
+  double xt[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    xt[d] = x[d] - S.alpha * dd[d];
+    g[d] -= S.alpha * ad[d];
+  }
+  double xn[3];
+  project_v(D, C, xt, xn);
+  if (xn[0] != xt[0] || xn[1] != xt[1] || xn[2] != xt[2]) part[5] += 1.0;
+  st3(B(D, B_X0 + S.xc), v, xn);
+  epilogue_full(D, S, C, v, xn, g, part);
+}
+
+__device__ __noinline__ void row_pl_cg(const InstDesc &D, const InstState &S, int v,
+                                       double *part) {
+  // CGStep (:182-195) then the loop top's BETA and sums.
+  VCons C;
+  load_cons(D, v, C);
+  const int f = load_face(D, C);
+  double x[3], p[3], ap[3], g[3];
+  ld3(B(D, B_X0 + S.xc), v, x);
+  ld3(B(D, B_P0 + S.pc), v, p);
+  ld3(B(D, B_AP), v, ap);
+  ld3(B(D, B_G0 + S.gc), v, g);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    x[d] -= S.alpha * p[d];
+    g[d] -= S.alpha * ap[d];
+  }
+  st3(B(D, B_X0 + S.xc), v, x);
+  st3(B(D, B_G0 + S.gc), v, g);
+  double phi[3], z[3], beta[3];
+  phi_v(D, C, f, g, phi);
+  precond_v(D, C, f, v, g, phi, z);
+  beta_v(D, C, f, g, phi, beta);
+  st3(B(D, B_Z0 + S.zc), v, z);
+  st3(B(D, B_BT0 + S.bc), v, beta);
+  const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
+  part[0] += dot3(gp, gp);
+  part[1] += dot3(beta, beta);
+  part[2] += phitphi_v(D, C, S.alpha_bar, x, phi);
+  part[3] += dot3(z, g);
+  part[5] += dot3(z, ap);
+}
+
+__device__ void row_op(const InstDesc &D, const InstState &S, int v, double *part) {
+  switch (S.phase) {
+    case PH_POW_RAND:
+    case PH_POW:
+    case PH_POW_LAST: row_power(D, S, v, part); break;
+    case PH_PROJ0:
+    case PH_FINAL:
+    case PH_INIT:
+    case PH_EXP_C:
+    case PH_PL_EXP_B: row_init(D, S, v, part); break;
+    case PH_CG_ENTRY:
+    case PH_CG_SPMV:
+    case PH_PL_SPMV: row_cg_spmv(D, S, v, part); break;
+    case PH_CG_YF: row_cg_yf(D, S, v, part); break;
+    case PH_CG_DAD: row_cg_dad(D, S, v, part); break;
+    case PH_RU: row_ru(D, S, v, part); break;
+    case PH_EXP_A:
+    case PH_EXP_B:
+    case PH_PL_EXP_A: row_exp(D, S, v, part); break;
+    case PH_PROP_A:
+    case PH_PROP_B:
+    case PH_PL_PROP_A: row_prop(D, S, v, part); break;
+    case PH_PL_CG: row_pl_cg(D, S, v, part); break;
+    default: break;
+  }
+}
+
+// ------------------------------------------------------ state transitions --
+__device__ __forceinline__ double ptp_value(const InstDesc &D, const InstState &S, double s) {
+  if (D.kind >= KIND_DECOUPLED) {  // ((x-px).phi)*(1/abar), clamped at 0
+    const double v = s * (1.0 / S.alpha_bar);
+    return v > 0.0 ? v : 0.0;
+  }
+  return s;
+}
+
+// Step trace record {event, iteration, residual, value}: 1 CG commit and
+// 2 CG exit (value f(P(y)) - f(x)), 3 expansion, 4 proportioning, 5 loop top
+// (value = proportional).  The CPU oracle records the same events.
+__device__ __forceinline__ void trace(const InstDesc &D, InstState &S, int ev, double val) {
+  if (D.trace && S.trace_n < D.trace_cap) {
+    double *r = D.trace + 4 * (size_t)S.trace_n;
+    r[0] = ev;
+    r[1] = S.iteration;
+    r[2] = S.residual;
+    r[3] = val;
+    S.trace_n++;
+  }
+}
+
+__device__ void go_final(const InstDesc &D, InstState &S) {
+  if (D.alg == ALG_MONOTONE) {
+    S.phase = PH_FINAL;
+  } else {  // MPRGP::solve has no final projection
+    S.code = S.residual <= D.tol ? 0 : -1;
+    S.phase = PH_DONE;
+  }
+}
+
+// Top of MPRGPMonotonic::solve's loop (:416-440) after a step that ended with
+// the loop-top sums s[0..4].
+__device__ void outer_top(const InstDesc &D, InstState &S, const double *s) {
+  S.active = (int)s[4];
+  if (S.iteration >= D.max_it) { go_final(D, S); return; }
+  S.residual = sqrt(s[0]);
+  if (S.residual <= D.tol) {
+    if (D.alg == ALG_PLAIN) S.iters_out = S.iteration;
+    go_final(D, S);
+    return;
+  }
+  S.zg = s[3];
+  S.prop = (s[1] <= ptp_value(D, S, s[2])) ? 1 : 0;  // gamma = 1
+  trace(D, S, 5, S.prop);
+  if (D.alg == ALG_PLAIN) {
+    S.phase = S.prop ? PH_PL_SPMV : PH_PL_PROP_A;
+    return;
+  }
+  if (S.prop) {
+    S.cg_prop = 1;
+    S.ru_ref = S.residual;
+    S.phase = PH_CG_ENTRY;
+  } else if (!S.y_valid || !S.y_feas) {
+    S.phase = PH_EXP_A;
+  } else {
+    S.phase = PH_PROP_A;
+  }
+}
+
+// The while-condition of CGMonotonicStep (:288-289) and what follows it.
+__device__ void cg_decide(const InstDesc &D, InstState &S, double dfy, double corr) {
+  const bool cont = S.cg_prop && S.residual > D.tol && (dfy <= 0.0) && S.iteration < D.max_it;
+  if (cont) {
+    S.xc ^= 1;
+    S.gc ^= 1;
+    S.zc ^= 1;
+    S.bc ^= 1;
+    S.iteration++;
+    S.num_cg++;
+    S.fx_off = -corr;  // fx := f(P(y)) while x := y
+    S.beta_cg = S.s_zap / S.pd;
+    S.residual = sqrt(S.s_gp2);
+    S.cg_prop = (S.s_bb <= ptp_value(D, S, S.s_ptp)) ? 1 : 0;
+    S.zg = S.s_zg;
+    trace(D, S, 1, dfy);
+    if (D.prec == PREC_MIXED && (S.residual <= D.tol || S.residual < 0.1 * S.ru_ref)) {
+      S.phase = PH_RU;
+      return;
+    }
+    if (S.residual <= D.tol) { go_final(D, S); return; }  // loop exits, then `break`
+    S.phase = PH_CG_SPMV;
+    return;
+  }
+  trace(D, S, 2, dfy);
+  if (S.residual <= D.tol) { go_final(D, S); return; }
+  if (S.cg_prop || !S.y_valid || !S.y_feas) S.phase = PH_EXP_A;
+  else S.phase = PH_PROP_A;
+}
+
+__device__ void advance(const InstDesc &D, InstState &S, const double *s) {
+  S.phases++;
+  const int phase_in = S.phase;
+  const double eps = D.tol;  // specRad(A, ev, tol): eps = tol (MPRGPSolver.h:28)
+  switch (S.phase) {
+    case PH_PROJ0:
+      if (S.ev_valid) {  // start from the stored vector, as given (not normalised)
+        S.pow_k = 0;
+        S.pow_src = -1;
+        S.pow_scale = 1.0;
+        S.phase = PH_POW;
+      } else {
+        S.phase = PH_POW_RAND;
+      }
+      break;
+    case PH_POW_RAND:
+      S.pow_k = 0;
+      S.pow_src = B_W1;
+      S.pow_scale = sqrt(s[0]);  // tmp.normalize()
+      S.phase = PH_POW;
+      break;
+    case PH_POW: {
+      const int k = S.pow_k;
+      const double nrm = sqrt(s[1]);
+      if (D.prec == PREC_MIXED) S.spmv32++; else S.spmv64++;
+      if (k >= 1 && sqrt(s[0]) <= eps) {  // iteration k-1 converged
+        S.spec_rad = S.pow_nrm_prev;
+        S.ev_upd = 1;
+        S.ev_src = B_T0 + ((k - 1) & 1);
+        S.power_iters = k - 1;
+        S.phase = PH_INIT;
+        break;
+      }
+      if (nrm < kEps) {
+        S.spec_rad = kEps;
+        S.ev_upd = 1;
+        S.ev_src = B_T0 + (k & 1);
+        S.power_iters = k;
+        S.phase = PH_INIT;
+        break;
+      }
+      S.pow_nrm_prev = nrm;
+      S.pow_scale = nrm;
+      S.pow_src = (k & 1) ? B_W1 : B_W;
+      if (k == 1000) {
+        S.pow_k = 1001;
+        S.phase = PH_POW_LAST;
+      } else {
+        S.pow_k = k + 1;
+      }
+      break;
+    }
+    case PH_POW_LAST:
+      S.spec_rad = S.pow_nrm_prev;
+      if (sqrt(s[0]) <= eps) {
+        S.ev_upd = 1;
+        S.ev_src = B_T0 + (1000 & 1);
+        S.power_iters = 1000;
+      } else {
+        S.power_iters = 1001;
+      }
+      S.phase = PH_INIT;
+      break;
+    case PH_INIT:
+      S.spmv64++;
+      S.iteration = 0;
+      S.g_cons = 1;
+      S.e_nz = 0;
+      S.p_is_z = 1;
+      outer_top(D, S, s);
+      break;
+    case PH_CG_ENTRY:
+    case PH_CG_SPMV:
+      if (S.phase == PH_CG_SPMV) S.pc ^= 1;
+      if (D.prec == PREC_MIXED) S.spmv32++; else S.spmv64++;
+      if (S.phase == PH_CG_ENTRY) {
+        S.fx_off = 0.0;
+        if (!S.g_cons) { S.e_nz = 1; S.spmv64++; }
+      }
+      S.pd = s[0];
+      S.pg = s[1];
+      S.pe = S.e_nz ? s[2] : 0.0;
+      S.alpha = S.zg / S.pd;
+      S.phase = PH_CG_YF;
+      break;
+    case PH_CG_YF: {
+      const double a = S.alpha;
+      S.dfy = -a * (S.pg + S.pe) + 0.5 * a * a * S.pd;  // f(y) - f(x)
+      S.corr = s[0];
+      S.y_valid = 1;
+      S.y_feas = (s[2] == 0.0) ? 1 : 0;
+      S.s_zap = s[3];
+      S.s_zg = s[4];
+      S.s_gp2 = s[5];
+      S.s_bb = s[6];
+      S.s_ptp = s[7];
+      if (s[1] > 0.0) {
+        S.phase = PH_CG_DAD;
+      } else {
+        cg_decide(D, S, S.dfy + S.fx_off, 0.0);
+      }
+      break;
+    }
+    case PH_CG_DAD: {
+      S.spmv64++;
+      const double corr = S.corr + 0.5 * s[0];  // f(P(y)) - f(y)
+      cg_decide(D, S, S.dfy + corr + S.fx_off, corr);
+      break;
+    }
+    case PH_RU:
+      S.spmv64++;
+      S.e_nz = 0;
+      S.g_cons = 1;
+      S.residual = sqrt(s[0]);
+      S.cg_prop = (s[1] <= ptp_value(D, S, s[2])) ? 1 : 0;
+      S.zg = s[3];
+      S.beta_cg = s[4] / S.pd;
+      S.ru_ref = S.residual;
+      if (S.residual <= D.tol) go_final(D, S);
+      else S.phase = PH_CG_SPMV;
+      break;
+    case PH_EXP_A:
+      S.phase = PH_EXP_B;
+      break;
+    case PH_EXP_B:
+      S.spmv64++;
+      S.y_valid = 1;
+      S.y_feas = (s[0] == 0.0) ? 1 : 0;
+      S.phase = PH_EXP_C;
+      break;
+    case PH_EXP_C:
+      S.spmv64++;
+      S.num_exp++;
+      S.iteration++;
+      S.g_cons = 1;
+      S.e_nz = 0;
+      trace(D, S, 3, 0.0);
+      outer_top(D, S, s);
+      break;
+    case PH_PROP_A:
+    case PH_PL_PROP_A:
+      S.spmv64 += (S.phase == PH_PROP_A) ? 2 : 1;
+      S.alpha = s[0] / s[1];
+      S.phase = PH_PROP_B;
+      break;
+    case PH_PROP_B:
+      S.num_prop++;
+      S.iteration++;
+      S.g_cons = (s[5] == 0.0) ? 1 : 0;
+      S.e_nz = 0;
+      S.p_is_z = 1;
+      trace(D, S, 4, 0.0);
+      outer_top(D, S, s);
+      break;
+    case PH_FINAL:
+      S.code = S.residual <= D.tol ? 0 : -1;
+      S.iters_out = S.iteration;
+      S.phase = PH_DONE;
+      break;
+    case PH_PL_SPMV: {
+      S.spmv64++;
+      if (!S.p_is_z) S.pc ^= 1;
+      S.p_is_z = 0;
+      S.pd = s[0];
+      const double acg = S.zg / S.pd;
+      double af = s[kMinSlot];
+      if (D.kind >= KIND_DECOUPLED) {  // BaseGeneralConProjector starts from alpha_cg + eps
+        const double a0 = (acg == DBL_MAX) ? acg : acg + kEps;
+        af = fmin(a0, af);
+      }
+      if (acg <= af) {
+        S.alpha = acg;
+        S.phase = PH_PL_CG;
+      } else {
+        S.alpha = af;
+        S.phase = PH_PL_EXP_A;
+      }
+      break;
+    }
+    case PH_PL_CG:
+      S.num_cg++;
+      S.iteration++;
+      S.beta_cg = s[5] / S.pd;
+      {
+        double t[5] = {s[0], s[1], s[2], s[3], (double)S.active};
+        outer_top(D, S, t);
+      }
+      break;
+    case PH_PL_EXP_A:
+      S.phase = PH_PL_EXP_B;
+      break;
+    case PH_PL_EXP_B:
+      S.spmv64++;
+      S.num_exp++;
+      S.iteration++;
+      S.p_is_z = 1;
+      outer_top(D, S, s);
+      break;
+    default:
+      S.phase = PH_DONE;
+      break;
+  }
+  if (S.phase == PH_INIT && phase_in != PH_INIT) S.alpha_bar = 2.0 / S.spec_rad;  // :28
+  // A NaN step length in a proportioning or plain step means the iteration
+  // broke down (p^T A p or D^T A D was 0); the monotone CG step tolerates it
+  // the way the reference does (its comparisons fail and it expands).
+  if ((S.phase == PH_PROP_B || S.phase == PH_PL_CG || S.phase == PH_PL_EXP_A) &&
+      !(S.alpha == S.alpha)) {
+    S.code = -2;
+    S.phase = PH_DONE;
+  }
+}
+
+// -------------------------------------------------------- reductions -----
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-reduce part[kPart] in a fixed order; thread k < kPart gets slot k.
+__device__ double block_reduce(double *part, double (*red)[kThreads / 32]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kPart; ++k) {
+    const double v = (k == kMinSlot) ? warp_min(part[k]) : warp_sum(part[k]);
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < kPart) {
+    const int k = threadIdx.x;
+    r = red[k][0];
+    for (int w = 1; w < kThreads / 32; ++w) r = (k == kMinSlot) ? fmin(r, red[k][w]) : r + red[k][w];
+  }
+  __syncthreads();
+  return r;
+}
+
+__device__ bool grid_barrier(Ctl *ctl, long long wait_ns, int &active_out) {
+  __shared__ int s_ok, s_active;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *vgen = &ctl->gen;
+    volatile int *verr = &ctl->err;
+    const unsigned int g = *vgen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&ctl->count, 1u);
+    int ok = 1;
+    if (arrived == gridDim.x - 1) {
+      ctl->snap[(g + 1) & 1] = *(volatile int *)&ctl->active;
+      atomicExch(&ctl->count, 0u);
+      __threadfence();
+      atomicAdd(&ctl->gen, 1u);
+    } else {
+      const long long t0 = gtimer();
+      while (*vgen == g) {
+        if (*verr) { ok = 0; break; }
+        if (gtimer() - t0 > wait_ns) {
+          atomicCAS(&ctl->err, 0, -4);  // MPRGP_TIMEOUT
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_ok = ok && (*verr == 0);
+    s_active = *(volatile int *)&ctl->snap[(g + 1) & 1];
+  }
+  __syncthreads();
+  active_out = s_active;
+  return s_ok;
+}
+
+__device__ __forceinline__ int find_instance(const int *prefix, int n, int item) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(prefix + mid) <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
+  __shared__ InstDesc sD;
+  __shared__ InstState sS;
+  __shared__ double red[kPart][kThreads / 32];
+  __shared__ double sums[kPart];
+  __shared__ int s_last;
+  Ctl *ctl = args.ctl;
+  const long long t_start = gtimer();
+  for (int ph = 0; ph < args.max_phases; ++ph) {
+    for (int item = blockIdx.x; item < args.total_items; item += gridDim.x) {
+      const int inst = find_instance(args.item_prefix, args.ninst, item);
+      if (threadIdx.x == 0) {
+        sD = args.desc[inst];
+        const int *src = reinterpret_cast<const int *>(sD.st);
+        int *dst = reinterpret_cast<int *>(&sS);
+        for (int w = 0; w < (int)(sizeof(InstState) / 4); ++w) dst[w] = __ldcg(src + w);
+      }
+      __syncthreads();
+      if (sS.phase == PH_DONE) {
+        __syncthreads();
+        continue;
+      }
+      const int local = item - sD.item_begin;
+      const int v = local * kThreads + threadIdx.x;
+      double part[kPart];
+#pragma unroll
+      for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+      if (v < sD.nv) row_op(sD, sS, v, part);
+      const double r = block_reduce(part, red);
+      if (threadIdx.x < kPart) {
+        sD.part[(size_t)local * kPart + threadIdx.x] = r;
+        __threadfence();
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int old = atomicAdd(sD.cnt, 1u);
+        s_last = (old == (unsigned int)sD.nitems - 1u);
+      }
+      __syncthreads();
+      if (s_last) {
+        __threadfence();
+        double acc[kPart];
+#pragma unroll
+        for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+        for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
+#pragma unroll
+          for (int k = 0; k < kPart; ++k) {
+            const double x = __ldcg(sD.part + (size_t)it * kPart + k);
+            acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+          }
+        }
+        const double t = block_reduce(acc, red);
+        if (threadIdx.x < kPart) sums[threadIdx.x] = t;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          InstState S = sS;
+          advance(sD, S, sums);
+          *sD.st = S;
+          *sD.cnt = 0u;
+          if (S.phase == PH_DONE) atomicSub(&ctl->active, 1);
+          __threadfence();
+        }
+      }
+      __syncthreads();
+    }
+    int active;
+    if (!grid_barrier(ctl, args.wait_ns, active)) return;
+    if (active == 0) return;
+    if (gtimer() - t_start > args.total_ns) {
+      if (threadIdx.x == 0) atomicCAS(&ctl->err, 0, -4);  // MPRGP_TIMEOUT
+      return;
+    }
+  }
+}
+
+// ------------------------------------------------------ setup kernels -----
+// BSR (row_ptr, cols, 9 values per block, row-major) -> SELL-32, plus
+// D^-1 = 1/diag(A) (getDiagonal, MPRGPUtility.h:503-515).
+__global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
+                                   const int *__restrict__ cols, const double *__restrict__ vals,
+                                   const int *__restrict__ slice_off, int *out_cols,
+                                   double *out64, float *out32, double *dinv) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = r >> 5, lane = r & 31;
+  const int nslices = (nv + kSlice - 1) / kSlice;
+  if (s >= nslices) return;
+  const int j0 = slice_off[s], w = slice_off[s + 1] - j0;
+  const int b = (r < nv) ? row_ptr[r] : 0;
+  const int len = (r < nv) ? row_ptr[r + 1] - b : 0;
+  double dg[3] = {0.0, 0.0, 0.0};
+  for (int j = 0; j < w; ++j) {
+    const size_t slot = (size_t)(j0 + j);
+    int c;
+    double m[9];
+    if (j < len) {
+      c = cols[b + j];
+      for (int e = 0; e < 9; ++e) m[e] = vals[9 * (size_t)(b + j) + e];
+      if (c == r) {
+        dg[0] = m[0];
+        dg[1] = m[4];
+        dg[2] = m[8];
+      }
+    } else {
+      c = (r < nv) ? r : 0;
+      for (int e = 0; e < 9; ++e) m[e] = 0.0;
+    }
+    out_cols[slot * kSlice + lane] = c;
+    for (int e = 0; e < 9; ++e) {
+      if (out64) out64[(slot * 9 + e) * kSlice + lane] = m[e];
+      if (out32) out32[(slot * 9 + e) * kSlice + lane] = (float)m[e];
+    }
+  }
+  if (r < nv)
+    for (int d = 0; d < 3; ++d) dinv[3 * (size_t)r + d] = 1.0 / dg[d];
+}
+
+// Planes (n, p) with n.x + p >= 0 -> rows (n, c = -p) of J x >= c, with
+// diag(J J^T) and 1/diag(J D^-1 J^T) (MPRGPPrecondition.h:81-89).
+__global__ void planes_setup_kernel(int nv, const int *__restrict__ plane_ptr,
+                                    const double *__restrict__ in, double *out, double *nn,
+                                    double *indn, const double *__restrict__ dinv) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  for (int q = plane_ptr[v]; q < plane_ptr[v + 1]; ++q) {
+    const double n0 = in[4 * (size_t)q], n1 = in[4 * (size_t)q + 1], n2 = in[4 * (size_t)q + 2];
+    out[4 * (size_t)q] = n0;
+    out[4 * (size_t)q + 1] = n1;
+    out[4 * (size_t)q + 2] = n2;
+    out[4 * (size_t)q + 3] = -in[4 * (size_t)q + 3];
+    nn[q] = n0 * n0 + n1 * n1 + n2 * n2;
+    if (dinv) {
+      const double t = n0 * n0 * dinv[3 * (size_t)v] + n1 * n1 * dinv[3 * (size_t)v + 1] +
+                       n2 * n2 * dinv[3 * (size_t)v + 2];
+      indn[q] = 1.0 / t;
+    }
+  }
+}
+
+// Standalone y = A x (FixedSparseMatrix::multiply, MPRGPSolver.h:469-473).
+template <typename VT>
+__global__ void __launch_bounds__(256) spmv_kernel(SellMatrix A, const VT *__restrict__ vals,
+                                                   int nv, const double *__restrict__ x,
+                                                   double *__restrict__ y) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double o[3];
+  spmv_row<VT>(A, vals, v, SrcV{x}, o);
+  st3(y, v, o);
+}
+
+// Host-side launch helpers (declared in capi.cu).
+cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream) {
+  void *params[] = {(void *)&args};
+  return cudaLaunchCooperativeKernel((const void *)engine_kernel, dim3(grid), dim3(kThreads),
+                                     params, 0, stream);
+}
+cudaError_t engine_max_blocks_per_sm(int *n) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, engine_kernel, kThreads, 0);
+}
+void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
+                        const int *slice_off, int *out_cols, double *out64, float *out32,
+                        double *dinv, cudaStream_t st) {
+  const int nslices = (nv + kSlice - 1) / kSlice;
+  const int threads = nslices * kSlice;
+  bsr_to_sell_kernel<<<(threads + 255) / 256, 256, 0, st>>>(nv, row_ptr, cols, vals, slice_off,
+                                                            out_cols, out64, out32, dinv);
+}
+void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
+                         double *indn, const double *dinv, cudaStream_t st) {
+  planes_setup_kernel<<<(nv + 255) / 256, 256, 0, st>>>(nv, plane_ptr, in, out, nn, indn, dinv);
+}
+void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
+                 cudaStream_t st) {
+  if (fp32) spmv_kernel<float><<<(nv + 255) / 256, 256, 0, st>>>(A, A.v32, nv, x, y);
+  else spmv_kernel<double><<<(nv + 255) / 256, 256, 0, st>>>(A, A.v64, nv, x, y);
+}
+
+}  // namespace mprgp

@@ -1,0 +1,126 @@
+// Shared host/device layout of the persistent MPRGP engine.
+//
+// One engine launch advances any number of QP instances ("instances") in
+// lockstep macro-phases.  A macro-phase walks a work list of items -- 256
+// consecutive vertex rows of one instance -- across the whole grid, then one
+// bounded grid barrier separates it from the next.  Each instance carries its
+// own state machine (InstState), which restates the control flow of the
+// reference's MPRGPMonotonic::solve / MPRGP::solve (MPRGPSolver.h:356-454).
+// The CTA that completes the last item of an instance in a phase reduces that
+// instance's per-item partial sums (fixed order: deterministic) and advances
+// its state; the other CTAs read the new state after the barrier.
+#pragma once
+#include <cstdint>
+
+namespace mprgp {
+
+constexpr int kThreads = 256;       // threads per CTA = vertex rows per item
+constexpr int kSlice = 32;          // SELL slice height (one warp)
+constexpr int kPart = 10;           // partial sums per item (slot kMinSlot is a min)
+constexpr int kMinSlot = 9;
+constexpr int kMaxPlanes = 3;       // plane constraints per vertex
+
+enum Kind : int { KIND_LOWER = 0, KIND_BOX = 1, KIND_DECOUPLED = 2, KIND_PLANES = 3 };
+enum Alg : int { ALG_MONOTONE = 1, ALG_PLAIN = 2 };
+enum Pre : int { PRE_NONE = 1, PRE_INFACE = 2, PRE_DECOUPLE = 3 };
+enum Prec : int { PREC_FP64 = 0, PREC_MIXED = 1 };
+
+// Vector buffers of one instance, each 3*nv doubles.
+enum Buf : int {
+  B_X0 = 0, B_X1, B_G0, B_G1, B_Z0, B_Z1, B_P0, B_P1, B_BT0, B_BT1,
+  B_AP, B_W, B_E, B_T0, B_T1, B_W1, kNumBuf
+};
+
+enum Phase : int {
+  PH_DONE = 0,
+  PH_PROJ0,     // x = P(x)
+  PH_POW_RAND,  // seeded start vector, |t|^2
+  PH_POW,       // t_k = src/scale; w = A t_k; |w|^2, |t_k - t_{k-1}|^2
+  PH_POW_LAST,  // |w_1000/|w_1000| - t_1000|
+  PH_INIT,      // g = Ax - b; face; phi; z; p = z; loop-top sums
+  PH_CG_ENTRY,  // Ap (and the true gradient when g is stale); p.Ap
+  PH_CG_SPMV,   // p' = z - beta p on the fly; Ap'; p'.Ap'
+  PH_CG_YF,     // y = x - alpha p, f(P(y)) - f(x), speculative next CG state
+  PH_CG_DAD,    // delta^T A delta for an infeasible y (delta = P(y) - y)
+  PH_EXP_A,     // y = P(x)
+  PH_EXP_B,     // g = Ay - b; face(y); x = P(y - abar phi)
+  PH_EXP_C,     // g = Ax - b; face(x); phi; z; p = z; loop-top sums
+  PH_PROP_A,    // g = Ax - b and AD = A beta in one pass; g.D, D.AD
+  PH_PROP_B,    // x = P(x - alpha D); g -= alpha AD; face; phi; z; p = z
+  PH_RU,        // mixed form: FP64 residual replacement g = A64 x - b
+  PH_FINAL,     // x = P(x)
+  PH_PL_SPMV,   // plain MPRGP: Ap, p.Ap, ratio test alpha_f
+  PH_PL_CG,     // plain CG step + loop-top sums
+  PH_PL_EXP_A,  // plain expansion: x = P(x - af p - abar phi)
+  PH_PL_EXP_B,  // g = Ax - b; face; phi; z; p = z; loop-top sums
+  PH_PL_PROP_A, // AD = A D; g.D, D.AD
+  kNumPhases
+};
+
+// SELL-32 copy of a 3x3-block CSR matrix: slices of 32 block rows; slot j of
+// slice s holds, for lanes t = 0..31, one block per row.  cols[(off+j)*32+t]
+// and vals[((off+j)*9+e)*32+t] with e the row-major entry of the block, so a
+// warp reads each of the nine entries as one coalesced 256 B (FP64) line.
+struct SellMatrix {
+  int nslices;
+  const int *slice_off;  // nslices + 1, in slots
+  const int *cols;       // vertex index; padding points at a valid row, value 0
+  const double *v64;
+  const float *v32;
+};
+
+struct InstState {
+  int phase, pow_k, iteration, num_cg, num_exp, num_prop, power_iters, code;
+  int xc, gc, zc, pc, bc;            // double-buffer selectors
+  int prop, cg_prop, y_valid, y_feas, g_cons, e_nz, ev_upd, ev_src, p_is_z, active;
+  int pow_src, iters_out, ev_valid, trace_n;
+  double alpha_bar, spec_rad, residual, pd, pg, pe, alpha, beta_cg, zg, fx_off;
+  double dfy, corr, pow_scale, pow_nrm_prev, ru_ref;
+  double s_zap, s_zg, s_gp2, s_bb, s_ptp;  // speculative CG sums
+  long long spmv64, spmv32, phases;
+};
+
+struct InstDesc {
+  SellMatrix A;
+  int nv, nitems, item_begin, m;
+  int kind, alg, pre, prec;
+  int max_it, pad1;
+  double tol;
+  unsigned long long seed;
+  const double *b, *dinv;
+  const int *plane_ptr;       // nv + 1 (planes kinds)
+  const double *planes;       // 4 per row: nx, ny, nz, c   (J x >= c)
+  const double *pl_nn;        // |n|^2 = diag(J J^T)
+  const double *pl_indn;      // 1 / (n . D^-1 n) = 1 / diag(J D^-1 J^T)
+  const double *L, *U;        // bounds kinds
+  unsigned char *face;        // one per constraint row / per unknown
+  double *buf[kNumBuf];
+  double *ev;
+  double *part;               // nitems * kPart
+  unsigned int *cnt;          // items finished in the current phase
+  InstState *st;
+  double *trace;              // optional step trace, 4 doubles per record
+  int trace_cap, pad2;
+};
+
+struct Ctl {
+  unsigned int count;   // barrier arrivals
+  unsigned int gen;     // barrier generation
+  int err;              // first error code (0 = none)
+  int err_where;        // phase of the first error
+  int active;           // instances not yet DONE
+  int snap[2];          // `active` as seen at each barrier release
+  int pad;
+};
+
+struct EngineArgs {
+  const InstDesc *desc;
+  const int *item_prefix;  // ninst + 1
+  int ninst, total_items;
+  int max_phases;          // quantum / hard bound on macro-phases
+  long long wait_ns;       // bound on a barrier wait
+  long long total_ns;      // bound on the whole launch
+  Ctl *ctl;
+};
+
+}  // namespace mprgp

@@ -1,0 +1,200 @@
+"""Test-side bindings: the CPU oracle (oracle/), the QuadProg++ pin
+(oracle/_ref/) and problem conversions.  Only tests, bench.py's CPU leg and
+__graft_entry__.smoke() use these."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+QP_REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libquadprog_ref.so")
+
+_orc = None
+_qp = None
+_P = C.c_void_p
+
+
+def build_oracle() -> None:
+    subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_oracle.sh")], check=True,
+                   capture_output=True)
+
+
+def oracle():
+    global _orc
+    if _orc is None:
+        if not os.path.exists(ORACLE_LIB) or _stale(ORACLE_LIB):
+            build_oracle()
+        L = C.CDLL(ORACLE_LIB)
+        L.oracle_solve.restype = C.c_int
+        L.oracle_solve.argtypes = [C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, _P,
+                                   _P, _P, _P, C.c_double, C.c_int, C.c_uint64, _P, C.c_int,
+                                   C.c_int, _P, _P, _P]
+        L.oracle_projector_op.restype = C.c_int
+        L.oracle_projector_op.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P,
+                                          _P, _P, C.c_double, _P, _P]
+        L.oracle_spmv.restype = None
+        L.oracle_spmv.argtypes = [C.c_int, _P, _P, _P, _P, _P]
+        L.oracle_spec_rad.restype = C.c_double
+        L.oracle_spec_rad.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_uint64,
+                                      C.POINTER(C.c_int)]
+        L.oracle_seeded_uniform.restype = C.c_double
+        L.oracle_seeded_uniform.argtypes = [C.c_uint64, C.c_uint64]
+        _orc = L
+    return _orc
+
+
+def _stale(lib_path: str) -> bool:
+    t = os.path.getmtime(lib_path)
+    d = os.path.join(ROOT, "oracle")
+    return any(os.path.getmtime(os.path.join(d, f)) > t for f in os.listdir(d)
+               if f.endswith((".h", ".cpp")))
+
+
+def quadprog_ref():
+    """The reference's own QuadProg++ (built from its sources), or None."""
+    global _qp
+    if _qp is None:
+        if not os.path.exists(QP_REF_LIB):
+            ref = os.environ.get("MPRGP_REFERENCE_ROOT", "/root/reference")
+            if os.path.isdir(ref):
+                subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), ref],
+                               check=True, capture_output=True)
+        if not os.path.exists(QP_REF_LIB):
+            return None
+        L = C.CDLL(QP_REF_LIB)
+        L.ref_solve_qp.restype = C.c_double
+        L.ref_solve_qp.argtypes = [C.c_int, _P, _P, C.c_int, _P, _P, _P]
+        _qp = L
+    return _qp
+
+
+def ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def solve_qp_ref(A, b, J, c0):
+    """min 0.5 x^T A x - b^T x  s.t.  J x >= c0 with the reference's QuadProg++."""
+    L = quadprog_ref()
+    A = np.ascontiguousarray(A, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    J = np.ascontiguousarray(J, np.float64).reshape(-1, len(b))
+    c0 = np.ascontiguousarray(c0, np.float64)
+    x = np.zeros(len(b))
+    f = L.ref_solve_qp(len(b), ptr(A), ptr(b), J.shape[0], ptr(J), ptr(c0), ptr(x))
+    return x, f
+
+
+class Csr:
+    def __init__(self, ptr_, idx, val, rows, cols):
+        self.ptr = np.ascontiguousarray(ptr_, np.int32)
+        self.idx = np.ascontiguousarray(idx, np.int32)
+        self.val = np.ascontiguousarray(val, np.float64)
+        self.rows, self.cols = rows, cols
+
+    @staticmethod
+    def from_dense(M):
+        M = np.asarray(M, np.float64)
+        rows, cols = M.shape
+        ptr_, idx, val = [0], [], []
+        for r in range(rows):
+            nz = np.nonzero(M[r])[0]
+            idx.extend(nz.tolist())
+            val.extend(M[r, nz].tolist())
+            ptr_.append(len(idx))
+        return Csr(ptr_, idx, val, rows, cols)
+
+    def dense(self):
+        M = np.zeros((self.rows, self.cols))
+        for r in range(self.rows):
+            for k in range(self.ptr[r], self.ptr[r + 1]):
+                M[r, self.idx[k]] += self.val[k]
+        return M
+
+    def matvec(self, x):
+        y = np.zeros(self.rows)
+        rows = np.repeat(np.arange(self.rows), np.diff(self.ptr))
+        np.add.at(y, rows, self.val * x[self.idx])
+        return y
+
+
+STAT_KEYS = ["code", "iterations", "num_cg", "num_exp", "num_prop", "power_iters", "residual",
+             "alpha_bar", "spec_rad", "spmv"]
+
+KIND = {"lower": 0, "box": 1, "decoupled": 2, "general": 3,
+        "plain_lower": 10, "plain_decoupled": 12, "plain_general": 13}
+
+
+def oracle_solve(kind, A: Csr, b, x, J: Csr | None = None, c=None, L=None, U=None, tol=1e-3,
+                 max_it=1000, seed=0x5EED, preconditioned=True, project_x0=True, ev=None):
+    """Runs the restated reference solve; returns (x, face, stats dict, ev)."""
+    O = oracle()
+    n = A.rows
+    x = np.ascontiguousarray(x, np.float64).copy()
+    st = np.zeros(10)
+    kind_i = KIND[kind] if isinstance(kind, str) else kind
+    m = J.rows if J is not None else n
+    face = np.zeros(max(m, 1), np.uint8)
+    if J is None:
+        J = Csr([0], [], [], 0, n)
+        c = np.zeros(0)
+    evbuf = None if ev is None else np.ascontiguousarray(ev, np.float64).copy()
+    code = O.oracle_solve(kind_i, int(preconditioned), n, ptr(A.ptr), ptr(A.idx), ptr(A.val),
+                          ptr(np.ascontiguousarray(b, np.float64)), J.rows, ptr(J.ptr),
+                          ptr(J.idx), ptr(J.val), ptr(np.ascontiguousarray(c, np.float64)),
+                          ptr(None if L is None else np.ascontiguousarray(L, np.float64)),
+                          ptr(None if U is None else np.ascontiguousarray(U, np.float64)),
+                          tol, max_it, seed, ptr(evbuf), 0 if evbuf is None else len(evbuf),
+                          int(project_x0), ptr(x), ptr(face), ptr(st))
+    stats = dict(zip(STAT_KEYS, st.tolist()))
+    stats["code"] = code
+    return x, face[:m], stats, evbuf
+
+
+def qp_from_beam(qp):
+    """(A CSR, b, J CSR, c) of a mprgp_gb300.BeamQP in the reference's (A, B, J, c) form."""
+    import mprgp_gb300 as M
+    aptr, aidx, aval = M.bsr_to_csr(qp.nv, qp.row_ptr, qp.cols, qp.vals)
+    A = Csr(aptr, aidx, aval, qp.n, qp.n)
+    jptr, jidx, jval, c = M.planes_to_J(qp.nv, qp.plane_ptr, qp.planes)
+    J = Csr(jptr, jidx, jval, len(c), qp.n)
+    return A, qp.b.copy(), J, c
+
+
+def decide_face_planes(J: Csr, c, x, eps=1e-9):
+    """DECIDE_FACE (MPRGPProjection.h:283-297) evaluated on the host."""
+    return (np.abs(J.matvec(x) - c) < eps).astype(np.uint8)
+
+
+def projected_gradient_norm(kind, A: Csr, b, x, J: Csr, c):
+    """||phi + beta|| at x with a freshly decided face, via the oracle's projector."""
+    O = oracle()
+    g = A.matvec(x) - b
+    n = A.rows
+    phi = np.zeros(n)
+    beta = np.zeros(n)
+    kind_i = KIND[kind] % 10
+    O.oracle_projector_op(kind_i, 2, n, J.rows, ptr(J.ptr), ptr(J.idx), ptr(J.val), ptr(c),
+                          ptr(x), ptr(g), None, 0.0, ptr(phi), None)
+    O.oracle_projector_op(kind_i, 3, n, J.rows, ptr(J.ptr), ptr(J.idx), ptr(J.val), ptr(c),
+                          ptr(x), ptr(g), ptr(phi), 0.0, ptr(beta), None)
+    return float(np.linalg.norm(phi + beta))
+
+
+def oracle_trace(on: bool):
+    O = oracle()
+    O.oracle_set_trace.argtypes = [C.c_int]
+    O.oracle_set_trace(int(on))
+
+
+def oracle_get_trace() -> np.ndarray:
+    O = oracle()
+    O.oracle_get_trace.restype = C.c_int
+    O.oracle_get_trace.argtypes = [_P, C.c_int]
+    n = O.oracle_get_trace(None, 0)
+    out = np.zeros((max(n, 1), 4))
+    O.oracle_get_trace(ptr(out), n)
+    return out[:n]

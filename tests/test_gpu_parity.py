@@ -1,0 +1,133 @@
+"""GPU parity: the CUDA solver through the C ABI against the CPU oracle
+(a restatement of the reference's MPRGP) on the same seeded inputs.
+
+Tolerances: x agrees with the oracle to ||dx||/||x|| <= 1e-8 when both sides
+are converged to a tight 1e-12*||b||; the active set (DECIDE_FACE of the final
+x, MPRGPProjection.h:283-297) must be identical; the spectral radius from the
+power method agrees to 1e-10 relative (FP64, same seeded start vector).
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+import mprgp_gb300 as M
+
+pytestmark = pytest.mark.gpu
+
+SEED = 0x5EED
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def gpu_solve(ctx, qp, kind, tol, max_it=20000, precision=M.PREC_FP64, **kw):
+    opt = M.default_options(tol=tol, max_it=max_it, kind=kind, project_x0=1, seed=SEED,
+                            precision=precision, **kw)
+    return ctx.solve_bsr(qp, opt, qp.x0)
+
+
+def test_spmv_matches_oracle(ctx):
+    torch = pytest.importorskip("torch")
+    qp = M.beam(5, 4, 9, extra_planes_max=2, seed=3)
+    A, b, J, c = H.qp_from_beam(qp)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(qp.n)
+    y_ref = A.matvec(x)
+    pr = M.Problem(ctx, qp.nv)
+    pr.set_matrix(qp.row_ptr, qp.cols, qp.vals, precisions=3)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.zeros(qp.n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    pr.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_FP64)
+    ctx.sync()
+    assert rel(yd.cpu().numpy(), y_ref) < 1e-14
+    pr.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_MIXED)
+    ctx.sync()
+    assert rel(yd.cpu().numpy(), y_ref) < 1e-5  # FP32 values, FP32 accumulation
+    pr.close()
+
+
+@pytest.mark.parametrize("kind_name,kind,extra", [("decoupled", M.KIND_DECOUPLED, 0),
+                                                  ("general", M.KIND_PLANES, 2)])
+def test_solve_parity_small(ctx, kind_name, kind, extra):
+    qp = M.beam(4, 4, 16, extra_planes_max=extra, seed=1)
+    A, b, J, c = H.qp_from_beam(qp)
+    tol = 1e-12 * np.linalg.norm(b)
+    xo, fo, so, _ = H.oracle_solve(kind_name, A, b, qp.x0, J, c, tol=tol, max_it=20000, seed=SEED)
+    xg, fg, sg = gpu_solve(ctx, qp, kind, tol)
+    assert so["code"] == 0 and sg.code == 0, (so, sg.as_dict())
+    assert rel(xg, xo) <= 1e-8
+    assert np.array_equal(H.decide_face_planes(J, c, xg), H.decide_face_planes(J, c, xo))
+    assert sg.power_iters == so["power_iters"]
+    assert abs(sg.spec_rad - so["spec_rad"]) <= 1e-10 * so["spec_rad"]
+    assert (J.matvec(xg) - c).min() >= -1e-9
+    # default reference tolerance 1e-8 ||b||: both converge, same active set
+    tol8 = 1e-8 * np.linalg.norm(b)
+    xg8, _, sg8 = gpu_solve(ctx, qp, kind, tol8)
+    assert sg8.code == 0 and sg8.residual <= tol8
+    assert H.projected_gradient_norm(kind_name, A, b, xg8, J, c) <= 1.01 * tol8
+    assert np.array_equal(H.decide_face_planes(J, c, xg8), H.decide_face_planes(J, c, xo))
+
+
+def test_mixed_precision_small(ctx):
+    qp = M.beam(4, 4, 16, extra_planes_max=2, seed=2)
+    A, b, J, c = H.qp_from_beam(qp)
+    tol = 1e-12 * np.linalg.norm(b)
+    xo, _, so, _ = H.oracle_solve("general", A, b, qp.x0, J, c, tol=tol, max_it=20000, seed=SEED)
+    tol8 = 1e-8 * np.linalg.norm(b)
+    xm, _, sm = gpu_solve(ctx, qp, M.KIND_PLANES, tol8, precision=M.PREC_MIXED)
+    assert sm.code == 0
+    assert sm.spmv_fp32 > 0
+    # the FP64-refined stopping test certifies the true projected gradient
+    assert H.projected_gradient_norm("general", A, b, xm, J, c) <= 1.01 * tol8
+    assert rel(xm, xo) <= 1e-6
+    assert np.array_equal(H.decide_face_planes(J, c, xm), H.decide_face_planes(J, c, xo))
+
+
+def _bounds_problem(seed=4):
+    qp = M.beam(3, 3, 8, seed=seed)
+    n = qp.n
+    L = np.full(n, -1e30)
+    L[1::3] = 0.0            # y >= 0 as a lower bound
+    U = np.full(n, 1e30)
+    U[0::3] = qp.x0[0::3] + 0.0005  # x may not move right by more than 0.5 mm
+    return qp, L, U
+
+
+@pytest.mark.parametrize("kind_name,kind", [("lower", M.KIND_LOWER), ("box", M.KIND_BOX)])
+def test_bounds_parity(ctx, kind_name, kind):
+    qp, L, U = _bounds_problem()
+    A, b, _, _ = H.qp_from_beam(qp)
+    x0 = np.clip(qp.x0, L, U)
+    tol = 1e-12 * np.linalg.norm(b)
+    Uo = U if kind_name == "box" else None
+    xo, fo, so, _ = H.oracle_solve(kind_name, A, b, x0, L=L, U=Uo, tol=tol, max_it=20000,
+                                   seed=SEED)
+    opt = M.default_options(tol=tol, max_it=20000, kind=kind, seed=SEED)
+    xg, fg, sg = ctx.solve_bsr(qp, opt, x0, L=L, U=Uo)
+    assert so["code"] == 0 and sg.code == 0, (so, sg.as_dict())
+    assert rel(xg, xo) <= 1e-8
+    assert np.array_equal(fg, fo)
+
+
+def test_batch_equals_single(ctx):
+    qps = [M.beam(a, b, c, extra_planes_max=e, seed=s)
+           for (a, b, c, e, s) in [(4, 4, 6, 0, 5), (3, 5, 7, 2, 6), (6, 4, 9, 1, 7)]]
+    probs, opts, singles = [], [], []
+    for qp in qps:
+        tol = 1e-10 * np.linalg.norm(qp.b)
+        kind = M.KIND_PLANES if qp.params["extra_planes_max"] else M.KIND_DECOUPLED
+        opt = M.default_options(tol=tol, max_it=20000, kind=kind, project_x0=1, seed=SEED)
+        xs, _, ss = ctx.solve_bsr(qp, opt, qp.x0)
+        singles.append((xs, ss))
+        pr = M.load_beam(ctx, qp)
+        probs.append(pr)
+        opts.append(opt)
+    stats = ctx.solve_batch(probs, opts)
+    for pr, st, (xs, ss) in zip(probs, stats, singles):
+        assert st.code == 0
+        xb = pr.get_x()
+        assert np.array_equal(xb, xs)          # deterministic reductions
+        assert st.iterations == ss.iterations
+        pr.close()
