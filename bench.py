@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""MPRGP QP solves/s on GB300 (one JSON line on rank 0).
+
+Workload (default): one implicit-Euler FEM beam QP of 32x32x128 Kuhn-tet cubes
+(140,481 vertices, 421,443 DOF, 2,031,169 3x3 blocks; E=1e5, nu=0.45,
+rho=1000, h=0.01), contact with the floor and two walls (up to 3 planes per
+vertex), solved to ||g_P|| <= 1e-8 ||b||.  Synthetic, seeded inputs.
+
+A step is one full solve (power method + MPRGP) of that QP:
+  value  solves/s with A, b, planes and x0 resident in HBM (x reset per step
+         by a device copy), L2 flushed between steps;
+  e2e    the same solve through the C ABI entry mprgp_solve_bsr with pinned
+         host buffers: upload of A/b/planes/x0, solve, download of x and face.
+--impl reference times the CPU restatement of the reference MPRGP (oracle/)
+on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (a, b, c, extra planes, plane mode, young, poisson, v0 sigma)
+    "c1": (32, 32, 128, 2, 2, 1e5, 0.45, 0.1),
+    "c0": (4, 4, 16, 0, 2, 1e5, 0.45, 0.1),
+    "c3": (48, 48, 144, 2, 2, 1e6, 0.49, 0.1),
+}
+REL_TOL = 1e-8
+SEED = 0x5EED
+FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload_qp(name):
+    import mprgp_gb300 as M
+    a, b, c, extra, mode, E, nu, sig = WORKLOADS[name]
+    qp = M.beam(a, b, c, extra_planes_max=extra, extra_planes_min=extra, plane_mode=mode,
+                young=E, poisson=nu, v0_sigma=sig, seed=1)
+    return qp
+
+
+def workload_desc(name, qp):
+    a, b, c, extra, mode, E, nu, sig = WORKLOADS[name]
+    return {"workload": f"beam {a}x{b}x{c} cubes, 6 Kuhn tets each: {qp.nv} vertices, "
+                        f"{qp.n} DOF, {qp.nnzb} 3x3 blocks; floor + walls x,z "
+                        f"({len(qp.planes)} plane rows); E={E:g} nu={nu} rho=1000 h=0.01; "
+                        f"tol 1e-8*||b||",
+            "config": name}
+
+
+def spmv_bytes(qp, s_a):
+    """Algorithmic bytes of one y = A x: A (values + block column), row pointers, x, y."""
+    return qp.nnzb * (9 * s_a + 4) + (qp.nv + 1) * 4 + qp.n * 8 + qp.n * 8
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(name, form):
+    """Per-launch DRAM bytes of the engine kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "engine_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    e = d.get(f"{name}:{form}")
+    return None if e is None else e
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [t.strip() for t in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    smax = float(p[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(qp, threads=1):
+    """One full solve of the same QP by the CPU restatement of the reference."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers as H
+    A, b, J, c = H.qp_from_beam(qp)
+    H.oracle().oracle_set_threads(threads)
+    tol = REL_TOL * float(np.linalg.norm(b))
+    t = time.perf_counter()
+    x, face, st, _ = H.oracle_solve("general", A, b, qp.x0, J, c, tol=tol, max_it=20000,
+                                    seed=SEED)
+    dt = time.perf_counter() - t
+    return dt, st
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_gb300(args):
+    import torch
+    import mprgp_gb300 as M
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    M.build()
+    qp = workload_qp(args.config)
+    tol = REL_TOL * float(np.linalg.norm(qp.b))
+    ctx = M.Context(local)
+    mixed = args.form == "mixed"
+    prec = M.PREC_MIXED if mixed else M.PREC_FP64
+    opt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=1, seed=SEED,
+                            precision=prec)
+    prob = M.load_beam(ctx, qp, precisions=3 if mixed else 1)
+    x0_dev = torch.from_numpy(qp.x0).cuda()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def one_step():
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        prob.set_x(x0_dev.data_ptr(), on_device=True)
+        st = prob.solve(opt)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), st
+
+    for _ in range(args.warmup):
+        one_step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    times, stats = [], []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ms, st = one_step()
+            times.append(ms)
+            stats.append(st)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    total_ms = sum(times)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    st = stats[-1]
+    for s in stats:
+        if s.code != 0:
+            raise RuntimeError(f"solve did not converge: {s.as_dict()}")
+    value = world * args.steps / (total_ms / 1e3)
+    # roofline of the engine kernel (the only kernel of a resident solve)
+    bytes64, bytes32 = spmv_bytes(qp, 8), spmv_bytes(qp, 4)
+    alg_bytes = st.spmv_fp64 * bytes64 + st.spmv_fp32 * bytes32
+    dev_ms = statistics.mean(s.device_ms for s in stats)
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (dev_ms / 1e3) / 1e9
+    traffic = committed_traffic(args.config, args.form)
+    line = {
+        "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
+        "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if not mixed else "f32 A (f32 accumulate) + f64 steps/projection/residual",
+        "data": "synthetic (seeded beam QP, no dataset)",
+        "config": dict(workload_desc(args.config, qp), form=args.form + "-" + ("mixed" if mixed else "fp64"),
+                       l2="flushed between solves (256 MB device write)",
+                       parallelism="replicas" if world > 1 else "single GPU"),
+        "latency_ms": {"p50": round(float(np.percentile(times, 50)), 4),
+                       "p99": round(float(np.percentile(times, 99)), 4)},
+        "solve": {"iterations": st.iterations, "cg": st.num_cg, "exp": st.num_exp,
+                  "prop": st.num_prop, "power_iters": st.power_iters, "active": st.active,
+                  "residual": st.residual, "tol": tol, "spmv_fp64": st.spmv_fp64,
+                  "spmv_fp32": st.spmv_fp32, "phases": st.phases},
+        "roofline": {"bound": "hbm", "kernel": "mprgp::engine_kernel",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": traffic,
+                     "bytes_per_launch": alg_bytes, "launch_ms": round(dev_ms, 4),
+                     "bytes_rule": "per matrix pass: nnzb*(9*s_A+4) + (nv+1)*4 + n*8 + n*8"},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "wall_s_timed": round(wall, 3),
+    }
+    if not args.no_e2e:
+        line["e2e"] = run_e2e(ctx, qp, opt, args, world, mixed)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        dt, cst = cpu_baseline(qp, 1)
+        line["cpu_baseline"] = {
+            "value": round(1.0 / dt, 5), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"one full solve of the same QP by the CPU restatement (oracle/), "
+                      f"serial like the reference; {dt:.2f} s, {int(cst['iterations'])} "
+                      f"iterations, code {int(cst['code'])}"}
+    prob.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_e2e(ctx, qp, opt, args, world, mixed):
+    """Solves through mprgp_solve_bsr from pinned host memory, copies inside the timing."""
+    import torch
+    import mprgp_gb300 as M
+
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t, t.numpy()
+
+    keep = []
+    arrs = {}
+    for k in ("row_ptr", "cols", "vals", "b", "x0", "plane_ptr", "planes"):
+        t, a = pinned(getattr(qp, k))
+        keep.append(t)
+        arrs[k] = a
+    hq = M.BeamQP(qp.nv, arrs["row_ptr"], arrs["cols"], arrs["vals"], arrs["b"], arrs["x0"],
+                  arrs["plane_ptr"], arrs["planes"], qp.params)
+    xout_t, _ = pinned(np.zeros(qp.n))
+    h2d = sum(a.nbytes for a in arrs.values())
+    d2h = qp.n * 8 + len(qp.planes)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        x, face, st = ctx.solve_bsr(hq, opt, hq.x0)
+        dt = time.perf_counter() - t
+        if st.code != 0:
+            raise RuntimeError(f"e2e solve did not converge: {st.as_dict()}")
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    return {"value": round(world * args.steps / total, 4), "unit": "solves/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": round(1e3 * total / args.steps, 3),
+            "path": "mprgp_solve_bsr (C ABI) from pinned host buffers",
+            "gpu_launches_per_step": 3}
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    import mprgp_gb300 as M
+    M.build()
+    threads = os.cpu_count() or 1
+    qp = workload_qp(args.config)
+    for _ in range(args.warmup):
+        cpu_baseline(qp, threads)
+    times, st = [], None
+    for _ in range(args.steps):
+        dt, st = cpu_baseline(qp, threads)
+        times.append(dt)
+    total = sum(times)
+    v = args.steps / total
+    line = {
+        "impl": "reference",
+        "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
+        "value": round(v, 5), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded beam QP, no dataset)",
+        "config": workload_desc(args.config, qp),
+        "latency_ms": {"p50": round(1e3 * float(np.percentile(times, 50)), 2),
+                       "p99": round(1e3 * float(np.percentile(times, 99)), 2)},
+        "cpu_baseline": {"value": round(v, 5), "unit": "solves/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "full solves of the workload QP by the CPU restatement of "
+                                   "the reference MPRGP (oracle/), OpenMP SpMV/dots on all "
+                                   f"host threads; last solve {int(st['iterations'])} iterations"},
+        "e2e": {"value": round(v, 5), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -66,6 +66,10 @@ struct mprgp_problem {
   InstState *st = nullptr;
   double *trace = nullptr;
   int trace_cap = 0, trace_n = 0;
+  // device staging for host BSR uploads (grow-only)
+  int *stage_ptr = nullptr, *stage_cols = nullptr;
+  double *stage_vals = nullptr;
+  size_t stage_nnzb = 0;
   std::vector<int> h_plane_ptr;
 };
 
@@ -109,7 +113,7 @@ void free_problem_arrays(mprgp_problem *p) {
   dfree(p->dinv); dfree(p->b); dfree(p->plane_ptr); dfree(p->planes_raw);
   dfree(p->planes); dfree(p->pl_nn); dfree(p->pl_indn); dfree(p->L); dfree(p->U);
   dfree(p->face); dfree(p->vec); dfree(p->ev); dfree(p->part); dfree(p->cnt); dfree(p->st);
-  dfree(p->trace);
+  dfree(p->trace); dfree(p->stage_ptr); dfree(p->stage_cols); dfree(p->stage_vals);
 }
 
 int resolve_options(const mprgp_problem *p, const mprgp_options *o, int *kind, int *alg,
@@ -510,28 +514,28 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
                      cudaMemcpyHostToDevice, s));
   const int *d_ptr = row_ptr, *d_cols = cols;
   const double *d_vals = vals;
-  int *t_ptr = nullptr, *t_cols = nullptr;
-  double *t_vals = nullptr;
   if (!on_device) {
-    int rc = dalloc(&t_ptr, nv + 1);
-    if (!rc) rc = dalloc(&t_cols, nnzb);
-    if (!rc) rc = dalloc(&t_vals, (size_t)nnzb * 9);
-    if (rc) { dfree(t_ptr); dfree(t_cols); dfree(t_vals); return rc; }
-    CK(cudaMemcpyAsync(t_ptr, row_ptr, sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(t_cols, cols, sizeof(int) * nnzb, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(t_vals, vals, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
-    d_ptr = t_ptr;
-    d_cols = t_cols;
-    d_vals = t_vals;
+    if (!p->stage_ptr) {
+      int rc = dalloc(&p->stage_ptr, nv + 1);
+      if (rc) return rc;
+    }
+    if ((size_t)nnzb > p->stage_nnzb) {
+      dfree(p->stage_cols);
+      dfree(p->stage_vals);
+      int rc = dalloc(&p->stage_cols, nnzb);
+      if (!rc) rc = dalloc(&p->stage_vals, (size_t)nnzb * 9);
+      if (rc) return rc;
+      p->stage_nnzb = nnzb;
+    }
+    CK(cudaMemcpyAsync(p->stage_ptr, row_ptr, sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p->stage_cols, cols, sizeof(int) * nnzb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(p->stage_vals, vals, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+    d_ptr = p->stage_ptr;
+    d_cols = p->stage_cols;
+    d_vals = p->stage_vals;
   }
   launch_bsr_to_sell(nv, d_ptr, d_cols, d_vals, p->slice_off, p->cols, p->v64, p->v32, p->dinv, s);
   cudaError_t e = cudaGetLastError();
-  if (!on_device) {
-    cudaStreamSynchronize(s);
-    dfree(t_ptr);
-    dfree(t_cols);
-    dfree(t_vals);
-  }
   if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
   p->nnzb = nnzb;
   p->planes_dirty = 1;  // 1/diag(J D^-1 J^T) depends on D

@@ -29,13 +29,45 @@ __device__ __forceinline__ long long gtimer() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Vectors written earlier in this kernel are read through L2 (ld.global.cg):
-// another SM may have produced them and L1 is not coherent.
+// Read-only inputs of a launch (A, b, D^-1, planes): non-volatile ld.global.nc
+// so the compiler may overlap them freely.
+__device__ __forceinline__ double ldro(const double *p) {
+  double r;
+  asm("ld.global.nc.f64 %0, [%1];" : "=d"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float ldro(const float *p) {
+  float r;
+  asm("ld.global.nc.f32 %0, [%1];" : "=f"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ int ldro(const int *p) {
+  int r;
+  asm("ld.global.nc.s32 %0, [%1];" : "=r"(r) : "l"(p));
+  return r;
+}
+// Vectors written by other CTAs in earlier phases are read with plain loads:
+// every phase boundary is a grid barrier whose gpu-scope acquire (followed
+// by bar.sync) makes those writes visible, as for cooperative groups.
 __device__ __forceinline__ void ld3(const double *b, int v, double o[3]) {
   const double *q = b + 3 * (size_t)v;
-  o[0] = __ldcg(q);
-  o[1] = __ldcg(q + 1);
-  o[2] = __ldcg(q + 2);
+  o[0] = q[0];
+  o[1] = q[1];
+  o[2] = q[2];
+}
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int *p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;"
+               : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ void st3(double *b, int v, const double o[3]) {
   double *q = b + 3 * (size_t)v;
@@ -68,16 +100,6 @@ struct SrcV {
   const double *p;
   __device__ __forceinline__ void operator()(int c, double o[3]) const { ld3(p, c, o); }
 };
-struct SrcScale {  // p / s   (the power method's tmpOut /= norm)
-  const double *p;
-  double s;
-  __device__ __forceinline__ void operator()(int c, double o[3]) const {
-    ld3(p, c, o);
-    o[0] /= s;
-    o[1] /= s;
-    o[2] /= s;
-  }
-};
 struct SrcPNew {  // z - beta p   (CGStep's p = z - beta*p)
   const double *z, *p;
   double beta;
@@ -95,21 +117,28 @@ template <typename VT, typename Src>
 __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
                                          const Src &src, double out[3]) {
   const int s = v >> 5, lane = v & 31;
-  const int j0 = __ldg(A.slice_off + s), j1 = __ldg(A.slice_off + s + 1);
+  const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
   VT a0 = 0, a1 = 0, a2 = 0;
-#pragma unroll 2
-  for (int j = j0; j < j1; ++j) {
-    const int c = __ldg(A.cols + (size_t)j * kSlice + lane);
-    const VT *q = vals + (size_t)j * (9 * kSlice) + lane;
-    const VT m0 = __ldg(q), m1 = __ldg(q + 32), m2 = __ldg(q + 64);
-    const VT m3 = __ldg(q + 96), m4 = __ldg(q + 128), m5 = __ldg(q + 160);
-    const VT m6 = __ldg(q + 192), m7 = __ldg(q + 224), m8 = __ldg(q + 256);
-    double xv[3];
-    src(c, xv);
-    const VT x0 = (VT)xv[0], x1 = (VT)xv[1], x2 = (VT)xv[2];
-    a0 = fma(m0, x0, a0); a0 = fma(m1, x1, a0); a0 = fma(m2, x2, a0);
-    a1 = fma(m3, x0, a1); a1 = fma(m4, x1, a1); a1 = fma(m5, x2, a1);
-    a2 = fma(m6, x0, a2); a2 = fma(m7, x1, a2); a2 = fma(m8, x2, a2);
+  // Columns of 8 slots are fetched together so that the neighbour gathers
+  // and block loads of those slots are all in flight at once.
+  for (int jb = j0; jb < j1; jb += 8) {
+    int c[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) c[u] = (jb + u < j1) ? ldro(A.cols + (size_t)(jb + u) * kSlice + lane) : -1;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (c[u] < 0) break;
+      const VT *q = vals + (size_t)(jb + u) * (9 * kSlice) + lane;
+      const VT m0 = ldro(q), m1 = ldro(q + 32), m2 = ldro(q + 64);
+      const VT m3 = ldro(q + 96), m4 = ldro(q + 128), m5 = ldro(q + 160);
+      const VT m6 = ldro(q + 192), m7 = ldro(q + 224), m8 = ldro(q + 256);
+      double xv[3];
+      src(c[u], xv);
+      const VT x0 = (VT)xv[0], x1 = (VT)xv[1], x2 = (VT)xv[2];
+      a0 = fma(m0, x0, a0); a0 = fma(m1, x1, a0); a0 = fma(m2, x2, a0);
+      a1 = fma(m3, x0, a1); a1 = fma(m4, x1, a1); a1 = fma(m5, x2, a1);
+      a2 = fma(m6, x0, a2); a2 = fma(m7, x1, a2); a2 = fma(m8, x2, a2);
+    }
   }
   out[0] = (double)a0;
   out[1] = (double)a1;
@@ -121,23 +150,29 @@ template <typename S1, typename S2>
 __device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &s1, const S2 &s2,
                                           double o1[3], double o2[3]) {
   const int s = v >> 5, lane = v & 31;
-  const int j0 = __ldg(A.slice_off + s), j1 = __ldg(A.slice_off + s + 1);
+  const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
   double a0 = 0, a1 = 0, a2 = 0, b0 = 0, b1 = 0, b2 = 0;
-  for (int j = j0; j < j1; ++j) {
-    const int c = __ldg(A.cols + (size_t)j * kSlice + lane);
-    const double *q = A.v64 + (size_t)j * (9 * kSlice) + lane;
-    double m[9];
+  for (int jb = j0; jb < j1; jb += 4) {
+    int c[4];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) m[e] = __ldg(q + 32 * e);
-    double x[3], y[3];
-    s1(c, x);
-    s2(c, y);
-    a0 = fma(m[0], x[0], a0); a0 = fma(m[1], x[1], a0); a0 = fma(m[2], x[2], a0);
-    a1 = fma(m[3], x[0], a1); a1 = fma(m[4], x[1], a1); a1 = fma(m[5], x[2], a1);
-    a2 = fma(m[6], x[0], a2); a2 = fma(m[7], x[1], a2); a2 = fma(m[8], x[2], a2);
-    b0 = fma(m[0], y[0], b0); b0 = fma(m[1], y[1], b0); b0 = fma(m[2], y[2], b0);
-    b1 = fma(m[3], y[0], b1); b1 = fma(m[4], y[1], b1); b1 = fma(m[5], y[2], b1);
-    b2 = fma(m[6], y[0], b2); b2 = fma(m[7], y[1], b2); b2 = fma(m[8], y[2], b2);
+    for (int u = 0; u < 4; ++u) c[u] = (jb + u < j1) ? ldro(A.cols + (size_t)(jb + u) * kSlice + lane) : -1;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (c[u] < 0) break;
+      const double *q = A.v64 + (size_t)(jb + u) * (9 * kSlice) + lane;
+      double m[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) m[e] = ldro(q + 32 * e);
+      double x[3], y[3];
+      s1(c[u], x);
+      s2(c[u], y);
+      a0 = fma(m[0], x[0], a0); a0 = fma(m[1], x[1], a0); a0 = fma(m[2], x[2], a0);
+      a1 = fma(m[3], x[0], a1); a1 = fma(m[4], x[1], a1); a1 = fma(m[5], x[2], a1);
+      a2 = fma(m[6], x[0], a2); a2 = fma(m[7], x[1], a2); a2 = fma(m[8], x[2], a2);
+      b0 = fma(m[0], y[0], b0); b0 = fma(m[1], y[1], b0); b0 = fma(m[2], y[2], b0);
+      b1 = fma(m[3], y[0], b1); b1 = fma(m[4], y[1], b1); b1 = fma(m[5], y[2], b1);
+      b2 = fma(m[6], y[0], b2); b2 = fma(m[7], y[1], b2); b2 = fma(m[8], y[2], b2);
+    }
   }
   o1[0] = a0; o1[1] = a1; o1[2] = a2;
   o2[0] = b0; o2[1] = b1; o2[2] = b2;
@@ -153,28 +188,28 @@ __device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int v, co
 // --------------------------------------------------- vertex constraints --
 struct VCons {
   int k, base;
-  double n[kMaxPlanes][3], c[kMaxPlanes], nn[kMaxPlanes], indn[kMaxPlanes];
+  double n[kMaxPlanes][3], c[kMaxPlanes], inn[kMaxPlanes], indn[kMaxPlanes];
   double lo[3], hi[3];
 };
 
 __device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
   if (D.kind >= KIND_DECOUPLED) {
-    const int b = __ldg(D.plane_ptr + v), e = __ldg(D.plane_ptr + v + 1);
+    const int b = ldro(D.plane_ptr + v), e = ldro(D.plane_ptr + v + 1);
     C.base = b;
     C.k = e - b;
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
       if (j < C.k) {
         const double *q = D.planes + 4 * (size_t)(b + j);
-        C.n[j][0] = __ldg(q);
-        C.n[j][1] = __ldg(q + 1);
-        C.n[j][2] = __ldg(q + 2);
-        C.c[j] = __ldg(q + 3);
-        C.nn[j] = __ldg(D.pl_nn + b + j);
-        C.indn[j] = __ldg(D.pl_indn + b + j);
+        C.n[j][0] = ldro(q);
+        C.n[j][1] = ldro(q + 1);
+        C.n[j][2] = ldro(q + 2);
+        C.c[j] = ldro(q + 3);
+        C.inn[j] = ldro(D.pl_nn + b + j);
+        C.indn[j] = ldro(D.pl_indn + b + j);
       } else {
         C.n[j][0] = C.n[j][1] = C.n[j][2] = C.c[j] = 0.0;
-        C.nn[j] = 1.0;
+        C.inn[j] = 1.0;
         C.indn[j] = 0.0;
       }
     }
@@ -183,8 +218,8 @@ __device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
     C.k = 3;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      C.lo[d] = __ldg(D.L + 3 * (size_t)v + d);
-      C.hi[d] = (D.kind == KIND_BOX) ? __ldg(D.U + 3 * (size_t)v + d) : DBL_MAX;
+      C.lo[d] = ldro(D.L + 3 * (size_t)v + d);
+      C.hi[d] = (D.kind == KIND_BOX) ? ldro(D.U + 3 * (size_t)v + d) : DBL_MAX;
     }
   }
 }
@@ -194,7 +229,7 @@ __device__ __forceinline__ int load_face(const InstDesc &D, const VCons &C) {
   int f = 0;
 #pragma unroll
   for (int j = 0; j < 3; ++j)
-    if (j < C.k) f |= (int)__ldcg(D.face + C.base + j) << (2 * j);
+    if (j < C.k) f |= (int)D.face[C.base + j] << (2 * j);
   return f;
 }
 __device__ __forceinline__ int fcode(int f, int j) { return (f >> (2 * j)) & 3; }
@@ -330,13 +365,18 @@ __device__ void project_v(const InstDesc &D, const VCons &C, const double x[3], 
     double lam[kMaxPlanes];
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
-      lam[j] = (j < C.k) ? fmax((C.c[j] - dot3(C.n[j], x)) / C.nn[j], 0.0) : 0.0;
+      lam[j] = (j < C.k) ? fmax((C.c[j] - dot3(C.n[j], x)) * C.inn[j], 0.0) : 0.0;
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k)
         for (int d = 0; d < 3; ++d) y[d] += C.n[j][d] * lam[j];
   } else if (D.kind == KIND_PLANES) {
     if (C.k == 0) return;
+    if (C.k == 1) {  // one constraint: the QP's solution is max(q, 0) / |n|^2
+      const double l = fmax((C.c[0] - dot3(C.n[0], x)) * C.inn[0], 0.0);
+      for (int d = 0; d < 3; ++d) y[d] += C.n[0][d] * l;
+      return;
+    }
     double G[3][3], q[3], lam[3];
     gram(C, G);
 #pragma unroll
@@ -362,7 +402,7 @@ __device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3
     double lam[kMaxPlanes];
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
-      lam[j] = (j < C.k && fcode(f, j)) ? -dot3(C.n[j], g) / C.nn[j] : 0.0;
+      lam[j] = (j < C.k && fcode(f, j)) ? -dot3(C.n[j], g) * C.inn[j] : 0.0;
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k)
@@ -373,6 +413,12 @@ __device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k && fcode(f, j)) act |= 1 << j;
     if (!act) return;
+    if (__popc(act) == 1) {
+      const int j = __ffs(act) - 1;
+      const double l = -dot3(C.n[j], g) * C.inn[j];
+      for (int d = 0; d < 3; ++d) phi[d] += C.n[j][d] * l;
+      return;
+    }
     double G[3][3], q[3], lam[3];
     gram(C, G);
 #pragma unroll
@@ -399,7 +445,7 @@ __device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
       double l = (j < C.k) ? dot3(C.n[j], beta) : 0.0;
-      if (j < C.k && fcode(f, j)) l = fmax(0.0, l / C.nn[j]);
+      if (j < C.k && fcode(f, j)) l = fmax(0.0, l * C.inn[j]);
       lam[j] = l;  // rows off the face keep (J beta)_i, as the reference does
     }
 #pragma unroll
@@ -414,6 +460,12 @@ __device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k && fcode(f, j)) act |= 1 << j;
     if (!act) return;
+    if (__popc(act) == 1) {
+      const int j = __ffs(act) - 1;
+      const double l = fmax(dot3(C.n[j], beta), 0.0) * C.inn[j];
+      for (int d = 0; d < 3; ++d) beta[d] -= C.n[j][d] * l;
+      return;
+    }
     double G[3][3], q[3], lam[3];
     gram(C, G);
 #pragma unroll
@@ -448,9 +500,9 @@ __device__ void precond_v(const InstDesc &D, const VCons &C, int f, int v, const
     return;
   }
   double di[3];
-  di[0] = __ldg(D.dinv + 3 * (size_t)v);
-  di[1] = __ldg(D.dinv + 3 * (size_t)v + 1);
-  di[2] = __ldg(D.dinv + 3 * (size_t)v + 2);
+  di[0] = ldro(D.dinv + 3 * (size_t)v);
+  di[1] = ldro(D.dinv + 3 * (size_t)v + 1);
+  di[2] = ldro(D.dinv + 3 * (size_t)v + 2);
   if (D.pre == PRE_INFACE) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) z[d] = phi[d] * di[d];
@@ -569,9 +621,9 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
   const double *src = S.pow_src < 0 ? D.ev : B(D, S.pow_src);
   double u[3];
   ld3(src, v, u);
-  u[0] /= S.pow_scale;
-  u[1] /= S.pow_scale;
-  u[2] /= S.pow_scale;
+  u[0] *= S.pow_scale;  // pow_scale holds 1/||w|| (tmpOut /= norm)
+  u[1] *= S.pow_scale;
+  u[2] *= S.pow_scale;
   if (S.phase == PH_POW_LAST || k >= 1) {
     double t[3];
     ld3(B(D, B_T0 + ((k - 1) & 1)), v, t);
@@ -581,7 +633,10 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
   if (S.phase == PH_POW_LAST) return;
   st3(B(D, B_T0 + (k & 1)), v, u);
   double w[3];
-  spmv_any(D, f32, v, SrcScale{src, S.pow_scale}, w);
+  spmv_any(D, f32, v, SrcV{src}, w);  // A (src / ||w||) = (A src) / ||w||
+  w[0] *= S.pow_scale;
+  w[1] *= S.pow_scale;
+  w[2] *= S.pow_scale;
   st3(B(D, (k & 1) ? B_W1 : B_W), v, w);
   part[1] += dot3(w, w);
 }
@@ -606,8 +661,8 @@ __device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int
   double x[3], ax[3];
   ld3(B(D, B_X0 + S.xc), v, x);
   spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
-  const double g[3] = {ax[0] - __ldg(D.b + 3 * (size_t)v), ax[1] - __ldg(D.b + 3 * (size_t)v + 1),
-                       ax[2] - __ldg(D.b + 3 * (size_t)v + 2)};
+  const double g[3] = {ax[0] - ldro(D.b + 3 * (size_t)v), ax[1] - ldro(D.b + 3 * (size_t)v + 1),
+                       ax[2] - ldro(D.b + 3 * (size_t)v + 2)};
   epilogue_full(D, S, C, v, x, g, part);
 }
 
@@ -624,7 +679,7 @@ __device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, 
       spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
       double e[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) e[d] = (ax[d] - __ldg(D.b + 3 * (size_t)v + d)) - g[d];
+      for (int d = 0; d < 3; ++d) e[d] = (ax[d] - ldro(D.b + 3 * (size_t)v + d)) - g[d];
       st3(B(D, B_E), v, e);
       part[2] += dot3(p, e);
     }
@@ -729,8 +784,8 @@ __device__ __noinline__ void row_ru(const InstDesc &D, const InstState &S, int v
   ld3(B(D, B_X0 + S.xc), v, x);
   ld3(B(D, B_AP), v, ap);
   spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
-  const double g[3] = {ax[0] - __ldg(D.b + 3 * (size_t)v), ax[1] - __ldg(D.b + 3 * (size_t)v + 1),
-                       ax[2] - __ldg(D.b + 3 * (size_t)v + 2)};
+  const double g[3] = {ax[0] - ldro(D.b + 3 * (size_t)v), ax[1] - ldro(D.b + 3 * (size_t)v + 1),
+                       ax[2] - ldro(D.b + 3 * (size_t)v + 2)};
   double phi[3], z[3], beta[3];
   phi_v(D, C, f, g, phi);
   precond_v(D, C, f, v, g, phi, z);
@@ -761,9 +816,9 @@ __device__ __noinline__ void row_exp(const InstDesc &D, const InstState &S, int 
     double y[3], ay[3];
     ld3(yb, v, y);
     spmv_row<double>(D.A, D.A.v64, v, SrcV{yb}, ay);
-    const double g[3] = {ay[0] - __ldg(D.b + 3 * (size_t)v),
-                         ay[1] - __ldg(D.b + 3 * (size_t)v + 1),
-                         ay[2] - __ldg(D.b + 3 * (size_t)v + 2)};
+    const double g[3] = {ay[0] - ldro(D.b + 3 * (size_t)v),
+                         ay[1] - ldro(D.b + 3 * (size_t)v + 1),
+                         ay[2] - ldro(D.b + 3 * (size_t)v + 2)};
     st3(B(D, B_G0 + S.gc), v, g);
     int f;
     decide_face(D, C, y, f);
@@ -812,7 +867,7 @@ __device__ __noinline__ void row_prop(const InstDesc &D, const InstState &S, int
       double ax[3];
       spmv2_row(D.A, v, SrcV{B(D, B_X0 + S.xc)}, SrcV{db}, ax, ad);
 #pragma unroll
-      for (int d = 0; d < 3; ++d) g[d] = ax[d] - __ldg(D.b + 3 * (size_t)v + d);
+      for (int d = 0; d < 3; ++d) g[d] = ax[d] - ldro(D.b + 3 * (size_t)v + d);
       st3(B(D, B_G0 + S.gc), v, g);
     } else {
       ld3(B(D, B_G0 + S.gc), v, g);
@@ -1012,7 +1067,7 @@ __device__ void advance(const InstDesc &D, InstState &S, const double *s) {
     case PH_POW_RAND:
       S.pow_k = 0;
       S.pow_src = B_W1;
-      S.pow_scale = sqrt(s[0]);  // tmp.normalize()
+      S.pow_scale = 1.0 / sqrt(s[0]);  // tmp.normalize()
       S.phase = PH_POW;
       break;
     case PH_POW: {
@@ -1036,7 +1091,7 @@ __device__ void advance(const InstDesc &D, InstState &S, const double *s) {
         break;
       }
       S.pow_nrm_prev = nrm;
-      S.pow_scale = nrm;
+      S.pow_scale = 1.0 / nrm;
       S.pow_src = (k & 1) ? B_W1 : B_W;
       if (k == 1000) {
         S.pow_k = 1001;
@@ -1219,17 +1274,32 @@ __device__ __forceinline__ double warp_min(double v) {
   return v;
 }
 
-// Block-reduce part[kPart] in a fixed order; thread k < kPart gets slot k.
-__device__ double block_reduce(double *part, double (*red)[kThreads / 32]) {
+// Partial sums each phase produces (slot kMinSlot only for PH_PL_SPMV).
+__device__ __forceinline__ int nslots(int phase) {
+  switch (phase) {
+    case PH_POW_RAND: case PH_POW_LAST: case PH_CG_DAD: case PH_EXP_B: return 1;
+    case PH_POW: case PH_PROP_A: case PH_PL_PROP_A: case PH_PL_SPMV: return 2;
+    case PH_CG_ENTRY: case PH_CG_SPMV: return 3;
+    case PH_INIT: case PH_EXP_C: case PH_PL_EXP_B: case PH_RU: return 5;
+    case PH_PROP_B: case PH_PL_CG: return 6;
+    case PH_CG_YF: return 8;
+    default: return 0;
+  }
+}
+
+// Block-reduce the first `ns` slots of part[] (and the min slot when
+// `with_min`) in a fixed order; thread k gets slot k.
+__device__ double block_reduce(double *part, double (*red)[kThreads / 32], int ns, bool with_min) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < kPart; ++k) {
+    if (k == kMinSlot ? !with_min : k >= ns) continue;
     const double v = (k == kMinSlot) ? warp_min(part[k]) : warp_sum(part[k]);
     if (lane == 0) red[k][warp] = v;
   }
   __syncthreads();
   double r = 0.0;
-  if (threadIdx.x < kPart) {
+  if (threadIdx.x < kPart && (threadIdx.x < ns || (threadIdx.x == kMinSlot && with_min))) {
     const int k = threadIdx.x;
     r = red[k][0];
     for (int w = 1; w < kThreads / 32; ++w) r = (k == kMinSlot) ? fmin(r, red[k][w]) : r + red[k][w];
@@ -1238,34 +1308,34 @@ __device__ double block_reduce(double *part, double (*red)[kThreads / 32]) {
   return r;
 }
 
+// Bounded grid barrier in the style of cooperative groups' grid sync:
+// arrival is an acq_rel atomic, the last CTA publishes the next generation
+// with a release store, the others poll it with acquire loads (bounded by
+// wait_ns and by the error flag), then bar.sync spreads the acquire to the CTA.
 __device__ bool grid_barrier(Ctl *ctl, long long wait_ns, int &active_out) {
   __shared__ int s_ok, s_active;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned int *vgen = &ctl->gen;
     volatile int *verr = &ctl->err;
-    const unsigned int g = *vgen;
-    __threadfence();
-    const unsigned int arrived = atomicAdd(&ctl->count, 1u);
+    const unsigned int g = ld_acquire(&ctl->gen);
+    const unsigned int arrived = atom_add_acq_rel(&ctl->count, 1u);
     int ok = 1;
     if (arrived == gridDim.x - 1) {
       ctl->snap[(g + 1) & 1] = *(volatile int *)&ctl->active;
-      atomicExch(&ctl->count, 0u);
-      __threadfence();
-      atomicAdd(&ctl->gen, 1u);
+      ctl->count = 0u;
+      st_release(&ctl->gen, g + 1);
     } else {
       const long long t0 = gtimer();
-      while (*vgen == g) {
+      while (ld_acquire(&ctl->gen) == g) {
         if (*verr) { ok = 0; break; }
         if (gtimer() - t0 > wait_ns) {
           atomicCAS(&ctl->err, 0, -4);  // MPRGP_TIMEOUT
           ok = 0;
           break;
         }
-        __nanosleep(32);
+        __nanosleep(20);
       }
     }
-    __threadfence();
     s_ok = ok && (*verr == 0);
     s_active = *(volatile int *)&ctl->snap[(g + 1) & 1];
   }
@@ -1278,7 +1348,7 @@ __device__ __forceinline__ int find_instance(const int *prefix, int n, int item)
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(prefix + mid) <= item) lo = mid;
+    if (ldro(prefix + mid) <= item) lo = mid;
     else hi = mid - 1;
   }
   return lo;
@@ -1295,11 +1365,15 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
   for (int ph = 0; ph < args.max_phases; ++ph) {
     for (int item = blockIdx.x; item < args.total_items; item += gridDim.x) {
       const int inst = find_instance(args.item_prefix, args.ninst, item);
-      if (threadIdx.x == 0) {
-        sD = args.desc[inst];
-        const int *src = reinterpret_cast<const int *>(sD.st);
-        int *dst = reinterpret_cast<int *>(&sS);
-        for (int w = 0; w < (int)(sizeof(InstState) / 4); ++w) dst[w] = __ldcg(src + w);
+      {
+        const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
+        int *dstd = reinterpret_cast<int *>(&sD);
+        for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads)
+          dstd[w] = ldro(srcd + w);
+        const int *srcs = reinterpret_cast<const int *>(args.desc[inst].st);
+        int *dsts = reinterpret_cast<int *>(&sS);
+        for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads)
+          dsts[w] = srcs[w];
       }
       __syncthreads();
       if (sS.phase == PH_DONE) {
@@ -1312,31 +1386,30 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
 #pragma unroll
       for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
       if (v < sD.nv) row_op(sD, sS, v, part);
-      const double r = block_reduce(part, red);
-      if (threadIdx.x < kPart) {
+      const int ns = nslots(sS.phase);
+      const bool wmin = sS.phase == PH_PL_SPMV;
+      const double r = block_reduce(part, red, ns, wmin);
+      if (threadIdx.x < ns || (wmin && threadIdx.x == kMinSlot))
         sD.part[(size_t)local * kPart + threadIdx.x] = r;
-        __threadfence();
-      }
       __syncthreads();
       if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned int old = atomicAdd(sD.cnt, 1u);
+        const unsigned int old = atom_add_acq_rel(sD.cnt, 1u);
         s_last = (old == (unsigned int)sD.nitems - 1u);
       }
       __syncthreads();
       if (s_last) {
-        __threadfence();
         double acc[kPart];
 #pragma unroll
         for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
         for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
 #pragma unroll
           for (int k = 0; k < kPart; ++k) {
-            const double x = __ldcg(sD.part + (size_t)it * kPart + k);
+            if (k == kMinSlot ? !wmin : k >= ns) continue;
+            const double x = sD.part[(size_t)it * kPart + k];
             acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
           }
         }
-        const double t = block_reduce(acc, red);
+        const double t = block_reduce(acc, red, ns, wmin);
         if (threadIdx.x < kPart) sums[threadIdx.x] = t;
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1345,7 +1418,6 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
           *sD.st = S;
           *sD.cnt = 0u;
           if (S.phase == PH_DONE) atomicSub(&ctl->active, 1);
-          __threadfence();
         }
       }
       __syncthreads();
@@ -1402,7 +1474,7 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
 }
 
 // Planes (n, p) with n.x + p >= 0 -> rows (n, c = -p) of J x >= c, with
-// diag(J J^T) and 1/diag(J D^-1 J^T) (MPRGPPrecondition.h:81-89).
+// 1/diag(J J^T) and 1/diag(J D^-1 J^T) (MPRGPPrecondition.h:81-89).
 __global__ void planes_setup_kernel(int nv, const int *__restrict__ plane_ptr,
                                     const double *__restrict__ in, double *out, double *nn,
                                     double *indn, const double *__restrict__ dinv) {
@@ -1414,7 +1486,7 @@ __global__ void planes_setup_kernel(int nv, const int *__restrict__ plane_ptr,
     out[4 * (size_t)q + 1] = n1;
     out[4 * (size_t)q + 2] = n2;
     out[4 * (size_t)q + 3] = -in[4 * (size_t)q + 3];
-    nn[q] = n0 * n0 + n1 * n1 + n2 * n2;
+    nn[q] = 1.0 / (n0 * n0 + n1 * n1 + n2 * n2);
     if (dinv) {
       const double t = n0 * n0 * dinv[3 * (size_t)v] + n1 * n1 * dinv[3 * (size_t)v + 1] +
                        n2 * n2 * dinv[3 * (size_t)v + 2];

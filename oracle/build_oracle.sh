@@ -5,7 +5,7 @@
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 mkdir -p "$HERE/_build"
-g++ -std=c++17 -O3 -fPIC -shared -Wall -Wno-unused-function \
+g++ -std=c++17 -O3 -fopenmp -fPIC -shared -Wall -Wno-unused-function \
   "$HERE/oracle_capi.cpp" -o "$HERE/_build/liboracle.so"
 echo "built $HERE/_build/liboracle.so"
 if [ -d "${MPRGP_REFERENCE_ROOT:-/root/reference}" ]; then

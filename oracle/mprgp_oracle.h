@@ -57,9 +57,20 @@ struct ScalarUtil {
 };
 
 // ---------------------------------------------------------------- vectors --
+// Thread count of the optional OpenMP build (the reference's serial path is
+// 1 thread; OMP_PARALLEL_FOR_ is empty in MPRGPUtility.h:64).
+inline int &omp_threads() {
+  static int n = 1;
+  return n;
+}
+
 inline double dot(const Vec &a, const Vec &b) {
   double s = 0.0;
-  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  const long long n = (long long)a.size();
+#ifdef _OPENMP
+#pragma omp parallel for reduction(+ : s) num_threads(omp_threads()) if (omp_threads() > 1)
+#endif
+  for (long long i = 0; i < n; ++i) s += a[i] * b[i];
   return s;
 }
 inline double norm(const Vec &a) { return std::sqrt(dot(a, a)); }
@@ -86,6 +97,9 @@ struct Csr {
   int nonZeros() const { return (int)idx.size(); }
   void multiply(const Vec &x, Vec &y) const {  // y = M x
     y.assign(rows, 0.0);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(omp_threads()) if (omp_threads() > 1)
+#endif
     for (int r = 0; r < rows; ++r) {
       double s = 0.0;
       for (int k = ptr[r]; k < ptr[r + 1]; ++k) s += val[k] * x[idx[k]];

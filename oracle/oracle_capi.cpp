@@ -250,6 +250,18 @@ double oracle_spec_rad(int n, const int *a_ptr, const int *a_idx, const double *
 
 double oracle_seeded_uniform(uint64_t seed, uint64_t i) { return seeded_uniform(seed, i); }
 
+// Threads of the OpenMP build for SpMV and dot products (1 = serial, as the
+// reference).  Returns the count in effect.
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  omp_threads() = n > 0 ? n : 1;
+#else
+  (void)n;
+  omp_threads() = 1;
+#endif
+  return omp_threads();
+}
+
 // Enables (cap > 0) or disables the step trace of the next solves.
 static Trace g_trace_buf;
 void oracle_set_trace(int on) {

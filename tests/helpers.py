@@ -41,6 +41,8 @@ def oracle():
         L.oracle_spec_rad.restype = C.c_double
         L.oracle_spec_rad.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_uint64,
                                       C.POINTER(C.c_int)]
+        L.oracle_set_threads.restype = C.c_int
+        L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_seeded_uniform.restype = C.c_double
         L.oracle_seeded_uniform.argtypes = [C.c_uint64, C.c_uint64]
         _orc = L
