@@ -163,6 +163,25 @@ int mprgp_solve_bsr(mprgp_context *ctx, int nv, int nnzb, const int *row_ptr, co
                     const mprgp_options *opt, double *x, unsigned char *face, double *ev,
                     mprgp_stats *stats);
 
+/* ---- solve without allocating device memory ------------------------------ */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * while they solve (a simulation step recorded into a CUDA graph and
+ * replayed, a real-time loop kept off the allocator, a host under a fixed
+ * GPU memory budget).  Every pointer is a device pointer the caller owns:
+ * A as 3x3-block CSR, b, the per-vertex planes (n, p) with n.x + p >= 0, x
+ * (solved in place) and optionally face (one byte per plane row).  The
+ * solver's working memory lives in one 64 MiB file-scope device array that
+ * every GPU loading the library holds until exit; problems that do not fit
+ * (about 37k vertices in FP64) are rejected with MPRGP_INVALID.  The first
+ * call on a device looks up that array's address (one-time set-up; make it
+ * before any stream capture).  All calls share the array: calls whose GPU
+ * work overlaps race and must be serialized.  Kinds DECOUPLED and PLANES,
+ * monotone algorithm, FP64 or MIXED; no stored power vector (use_ev = 0). */
+int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *row_ptr, const int *cols,
+                        const double *vals, const double *b, const int *plane_ptr,
+                        const double *planes, const mprgp_options *opt, double *x,
+                        unsigned char *face, mprgp_stats *stats);
+
 /* ---- batched: many instances advance in one persistent launch ----------- */
 int mprgp_solve_batch(mprgp_context *ctx, int count, mprgp_problem *const *probs,
                       const mprgp_options *opts, mprgp_stats *stats);

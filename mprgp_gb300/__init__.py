@@ -96,6 +96,8 @@ def _sig(lib):
       C.POINTER(Options), _P, _P, _P, C.POINTER(Stats))
     s("mprgp_solve_batch", C.c_int, _P, C.c_int, C.POINTER(_P), C.POINTER(Options),
       C.POINTER(Stats))
+    s("mprgp_solve_noalloc", C.c_int, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
+      C.POINTER(Options), _P, _P, C.POINTER(Stats))
     s("mprgp_beam_default", None, C.POINTER(BeamParams))
     s("mprgp_beam_sizes", C.c_int, C.POINTER(BeamParams), _IP, _IP, _IP)
     s("mprgp_beam_build", C.c_int, C.POINTER(BeamParams), _P, _P, _P, _P, _P, _P, _P)
@@ -343,6 +345,17 @@ def load_beam(ctx: Context, qp: BeamQP, precisions=1) -> Problem:
     pr.set_planes(qp.plane_ptr, qp.planes)
     pr.set_x(qp.x0)
     return pr
+
+
+def solve_noalloc(stream: int, nv: int, nnzb: int, row_ptr: int, cols: int, vals: int, b: int,
+                  plane_ptr: int, planes: int, opt: Options, x: int, face: int = 0):
+    """mprgp_solve_noalloc with raw device pointers; returns (code, Stats)."""
+    st = Stats()
+    rc = lib().mprgp_solve_noalloc(C.c_void_p(stream), nv, nnzb, C.c_void_p(row_ptr),
+                                   C.c_void_p(cols), C.c_void_p(vals), C.c_void_p(b),
+                                   C.c_void_p(plane_ptr), C.c_void_p(planes), C.byref(opt),
+                                   C.c_void_p(x), C.c_void_p(face or None), C.byref(st))
+    return _check(rc, "solve_noalloc"), st
 
 
 # ---------------------------------------------------------- conversions --

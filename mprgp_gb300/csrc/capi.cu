@@ -325,6 +325,11 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
 
 }  // namespace
 
+namespace mprgp {
+// Lets other translation units of the library report through mprgp_last_error().
+void set_last_error(const char *what) { g_last_error = what; }
+}  // namespace mprgp
+
 extern "C" {
 
 int mprgp_version(void) { return 10000; }
