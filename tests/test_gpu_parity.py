@@ -209,3 +209,32 @@ def test_batch_equals_single(ctx):
         assert np.array_equal(xb, xs)          # deterministic reductions
         assert st.iterations == ss.iterations
         pr.close()
+
+
+GOLDEN = sorted(__import__("glob").glob(__import__("os").path.join(
+    __import__("os").path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[p.rsplit("/", 1)[-1][:-4] for p in GOLDEN])
+def test_gpu_matches_golden(ctx, path):
+    """GPU solutions against the QuadProg++ solutions stored in the fixtures
+    (the reference's own dense QP solver, run where the reference is present)."""
+    d = dict(np.load(path))
+    qp = M.BeamQP(int(d["nv"]), d["row_ptr"], d["cols"], d["vals"], d["b"], d["x0"],
+                  d["plane_ptr"], d["planes"], {})
+    tol = 1e-10 * np.linalg.norm(qp.b)
+    xr = d["x_qp"]
+    if "L" in d:
+        L, U = d["L"], d["U"]
+        opt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_BOX, seed=SEED)
+        x, face, st = ctx.solve_bsr(qp, opt, np.clip(qp.x0, L, U), L=L, U=U)
+        act = (np.abs(x - L) < 1e-9) | (np.abs(x - U) < 1e-9)
+        act_r = (np.abs(xr - L) < 1e-9) | (np.abs(xr - U) < 1e-9)
+    else:
+        A, b, J, c = H.qp_from_beam(qp)
+        x, face, st = gpu_solve(ctx, qp, M.KIND_PLANES, tol)
+        act = H.decide_face_planes(J, c, x)
+        act_r = H.decide_face_planes(J, c, xr)
+    assert st.code == 0
+    assert rel(x, xr) <= 1e-8
+    assert np.array_equal(act, act_r)
