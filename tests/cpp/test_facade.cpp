@@ -1,0 +1,101 @@
+// Drop-in test of the C++ façade: the reference's own unit tests
+// (test_case/MPRGPTest.cpp) written against include/mprgp/MPRGPSolver.h,
+// plus the reference's binary QP file round trip (MPRGPUtility.h:407-485)
+// and the file-form solve (MPRGPSolver.h:576-589).  Prints one line per
+// check; exits non-zero on failure.
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include "mprgp/MPRGPSolver.h"
+
+using namespace MATH;
+
+static int failures = 0;
+#define CHECK(cond)                                                  \
+  do {                                                               \
+    if (!(cond)) {                                                   \
+      std::printf("FAIL %s:%d %s\n", __FILE__, __LINE__, #cond);     \
+      ++failures;                                                    \
+    }                                                                \
+  } while (0)
+
+static SparseMatrix<double> from_dense(const std::vector<double> &M, int r, int c) {
+  std::vector<Triplet<double>> t;
+  for (int i = 0; i < r; ++i)
+    for (int j = 0; j < c; ++j)
+      if (M[i * c + j] != 0.0) t.emplace_back(i, j, M[i * c + j]);
+  SparseMatrix<double> S(r, c);
+  S.setFromTriplets(t.begin(), t.end());
+  return S;
+}
+
+int main() {
+  std::mt19937 gen(7);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  // test_solver (MPRGPTest.cpp:70-98): random SPD 5x5, J = I.
+  const int n = 5;
+  std::vector<double> Md(n * n), MtM(n * n, 0.0), I(n * n, 0.0);
+  for (int i = 0; i < n * n; ++i) Md[i] = U(gen) + ((i % (n + 1)) == 0 ? 3.0 : 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      for (int k = 0; k < n; ++k) MtM[i * n + j] += Md[k * n + i] * Md[k * n + j];
+  for (int i = 0; i < n; ++i) I[i * n + i] = 1.0;
+  const SparseMatrix<double> A = from_dense(MtM, n, n), J = from_dense(I, n, n);
+  Vec<double> B(n), c(n), x(n);
+  for (int i = 0; i < n; ++i) { B[i] = U(gen); c[i] = U(gen); x[i] = U(gen); }
+  typedef FixedSparseMatrix<double> MAT;
+  MAT FA(A);
+  {
+    Vec<double> y = x;
+    const int rc = MPRGPGeneralCon<double>::solve<MAT, true>(FA, B, J, c, y, 1e-10, 1000);
+    std::printf("general: code %d\n", rc);
+    CHECK(rc == 0);
+    for (int i = 0; i < n; ++i) CHECK(y[i] >= c[i] - 1e-9);
+  }
+  {
+    Vec<double> y = x;
+    const int rc = MPRGPDecoupledCon<double>::solve<MAT, true>(FA, B, J, c, y, 1e-10, 1000);
+    std::printf("decoupled: code %d\n", rc);
+    CHECK(rc == 0);
+    for (int i = 0; i < n; ++i) CHECK(y[i] >= c[i] - 1e-9);
+  }
+  {  // lower bound and box façades on the same system
+    Vec<double> y = x, L = c, H(n, 0.7);
+    for (int i = 0; i < n; ++i) y[i] = std::max(y[i], L[i]);
+    CHECK(MPRGPLowerBound<double>::solve(FA, B, L, y, 1e-10, 1000) == 0);
+    Vec<double> z(n);
+    for (int i = 0; i < n; ++i) z[i] = std::min(std::max(x[i], L[i]), std::max(L[i], H[i]));
+    for (int i = 0; i < n; ++i) H[i] = std::max(L[i], H[i]);
+    CHECK(MPRGPBoxBound<double>::solve(FA, B, L, H, z, 1e-10, 1000) == 0);
+    for (int i = 0; i < n; ++i) CHECK(z[i] >= L[i] - 1e-9 && z[i] <= H[i] + 1e-9);
+  }
+  {  // generic classes with projector objects
+    Vec<double> JJt(n, 1.0), y = x;
+    DecoupledConProjector<double> proj(J, JJt, c);
+    proj.project(x, y);
+    DiagonalDecouplePreconSolver<double, MAT> pre(FA, proj.getFace(), J);
+    MPRGPMonotonic<double, MAT, DecoupledConProjector<double>,
+                   DiagonalDecouplePreconSolver<double, MAT>>
+        solver(FA, B, pre, proj, 1000, 1e-10);
+    CHECK(solver.solve(y) == 0);
+    CHECK(solver.residualOut() <= 1e-10);
+    std::printf("monotone decoupled: iterations %zu active %d\n", solver.iterationsOut(),
+                COUNT_CONSTRAINTS(proj.getFace()));
+  }
+  {  // QP file round trip and the file-form solve (MPRGPSolver.h:576-589)
+    const std::string path = "facade_qp.b";
+    CHECK(writeQP(A, B, J, c, x, path));
+    SparseMatrix<double> A2, J2;
+    Vec<double> B2, c2, x2;
+    CHECK(loadQP(A2, B2, J2, c2, x2, path));
+    CHECK(A2.nonZeros() == A.nonZeros() && J2.rows() == J.rows() && x2 == x && c2 == c);
+    Vec<double> y;
+    const int rc = MPRGPDecoupledCon<double>::solve<true>(path, y, 1e-10, 1000);
+    std::printf("file-form solve: code %d\n", rc);
+    CHECK(rc == 0 && (int)y.size() == n);
+    std::remove(path.c_str());
+  }
+  std::printf("%s (%d failures)\n", failures ? "FAILED" : "OK", failures);
+  return failures ? 1 : 0;
+}
