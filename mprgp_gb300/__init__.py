@@ -75,6 +75,7 @@ def _sig(lib):
     s("mprgp_context_stream", _P, _P)
     s("mprgp_context_sync", C.c_int, _P)
     s("mprgp_context_info", C.c_int, _P, _IP, _IP)
+    s("mprgp_context_set_tuning", C.c_int, _P, C.c_int, C.c_int)
     s("mprgp_problem_create", C.c_int, _P, C.c_int, C.POINTER(_P))
     s("mprgp_problem_destroy", C.c_int, _P)
     s("mprgp_problem_set_matrix", C.c_int, _P, C.c_int, _P, _P, _P, C.c_int, C.c_int)
@@ -210,6 +211,9 @@ class Context:
 
     def sync(self):
         _check(lib().mprgp_context_sync(self.h), "sync")
+
+    def set_tuning(self, stage: int = 0, ctas_per_sm: int = 0):
+        _check(lib().mprgp_context_set_tuning(self.h, stage, ctas_per_sm), "set_tuning")
 
     def close(self):
         if self.h:

@@ -21,7 +21,7 @@
 
 namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
-cudaError_t engine_max_blocks_per_sm(int *n);
+cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,
                         double *dinv, cudaStream_t st);
@@ -37,7 +37,9 @@ struct mprgp_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   Ctl *ctl = nullptr;
-  int nsm = 0, bps = 0;
+  int nsm = 0, bps = 0, bps_stage = 0;
+  int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
+  int ctas_per_sm = 0;   // persistent CTAs per SM (0 = all resident)
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   mprgp_problem *scratch = nullptr;  // reused by mprgp_solve_bsr
   // per-launch arrays (grown on demand)
@@ -62,6 +64,7 @@ struct mprgp_problem {
   unsigned char *face = nullptr;
   int face_len = 0;
   double *vec = nullptr, *ev = nullptr, *part = nullptr;
+  float *vec32 = nullptr;
   unsigned int *cnt = nullptr;
   InstState *st = nullptr;
   double *trace = nullptr;
@@ -112,7 +115,7 @@ void free_problem_arrays(mprgp_problem *p) {
   dfree(p->slice_off); dfree(p->cols); dfree(p->v64); dfree(p->v32);
   dfree(p->dinv); dfree(p->b); dfree(p->plane_ptr); dfree(p->planes_raw);
   dfree(p->planes); dfree(p->pl_nn); dfree(p->pl_indn); dfree(p->L); dfree(p->U);
-  dfree(p->face); dfree(p->vec); dfree(p->ev); dfree(p->part); dfree(p->cnt); dfree(p->st);
+  dfree(p->face); dfree(p->vec); dfree(p->vec32); dfree(p->ev); dfree(p->part); dfree(p->cnt); dfree(p->st);
   dfree(p->trace); dfree(p->stage_ptr); dfree(p->stage_cols); dfree(p->stage_vals);
 }
 
@@ -197,6 +200,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->face = p->face;
   const size_t n = 3 * (size_t)p->nv;
   for (int i = 0; i < kNumBuf; ++i) d->buf[i] = p->vec + (size_t)i * n;
+  for (int i = 0; i < kNumBuf32; ++i) d->buf32[i] = p->vec32 + (size_t)i * n;
   d->ev = p->ev;
   d->part = p->part;
   d->cnt = p->cnt;
@@ -295,8 +299,12 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   args.max_phases = (int)std::min<long long>(phase_bound, INT_MAX);
   args.wait_ns = (long long)(wait_s * 1e9);
   args.total_ns = (long long)(std::max(60.0, 20.0 * wait_s) * 1e9);
+  const bool stage = c->stage && c->bps_stage > 0;
+  args.stage_bytes = stage ? kStageBytes : 0;
   args.ctl = c->ctl;
-  const int grid = std::max(1, std::min(prefix[n], c->nsm * c->bps));
+  int per_sm = stage ? c->bps_stage : c->bps;
+  if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
+  const int grid = std::max(1, std::min(prefix[n], c->nsm * per_sm));
   CK(cudaEventRecord(c->e0, s));
   CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(c->e1, s));
@@ -387,7 +395,8 @@ int mprgp_context_create(int device, mprgp_context **out) {
   auto *c = new mprgp_context();
   c->device = device;
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
-  CK(engine_max_blocks_per_sm(&c->bps));
+  CK(engine_max_blocks_per_sm(&c->bps, 0));
+  CK(engine_max_blocks_per_sm(&c->bps_stage, kStageBytes));
   if (c->bps < 1) {
     delete c;
     return fail(MPRGP_NO_DEVICE, "engine kernel cannot be resident");
@@ -424,6 +433,13 @@ int mprgp_context_sync(mprgp_context *c) {
   return MPRGP_OK;
 }
 
+int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
+  if (!c || stage < 0 || stage > 1 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  c->stage = stage;
+  c->ctas_per_sm = ctas_per_sm;
+  return MPRGP_OK;
+}
+
 int mprgp_context_info(mprgp_context *c, int *nsm, int *blocks_per_sm) {
   if (!c) return fail(MPRGP_INVALID, "ctx");
   if (nsm) *nsm = c->nsm;
@@ -438,7 +454,7 @@ size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {
   if (precisions & 1) by += slots * kSlice * 9 * 8;
   if (precisions & 2) by += slots * kSlice * 9 * 4;
   const size_t n = 3 * (size_t)nv;
-  by += n * 8 * (kNumBuf + 3);  // vectors, dinv, b, ev
+  by += n * 8 * (kNumBuf + 3) + n * 4 * kNumBuf32;  // vectors, dinv, b, ev, FP32 shadows
   by += (size_t)nplanes * (8 * 4 * 2 + 8 * 2 + 1) + (size_t)(nv + 1) * 4 + n * 16 + n;
   by += (size_t)nitems_of(nv) * kPart * 8 + sizeof(InstState) + 64;
   return by;
@@ -454,7 +470,8 @@ int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
   p->nslices = (nv + kSlice - 1) / kSlice;
   const size_t n = 3 * (size_t)nv;
   int rc = 0;
-  if ((rc = dalloc(&p->vec, n * kNumBuf)) || (rc = dalloc(&p->ev, n)) ||
+  if ((rc = dalloc(&p->vec, n * kNumBuf)) || (rc = dalloc(&p->vec32, n * kNumBuf32)) ||
+      (rc = dalloc(&p->ev, n)) ||
       (rc = dalloc(&p->b, n)) || (rc = dalloc(&p->dinv, n)) ||
       (rc = dalloc(&p->part, (size_t)nitems_of(nv) * kPart)) || (rc = dalloc(&p->cnt, 1)) ||
       (rc = dalloc(&p->st, 1)) || (rc = dalloc(&p->slice_off, p->nslices + 1))) {

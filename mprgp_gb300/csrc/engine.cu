@@ -69,6 +69,52 @@ __device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int *p, unsign
 __device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
+
+// ------------------------------------------------ shared-memory staging --
+// For FP32 matrix passes an item's slice of A -- block columns and values of
+// its 8 SELL slices, contiguous in global memory -- is brought into shared
+// memory by one cp.async.bulk per array, completed on an mbarrier.  The
+// loads of A then cost no registers and arrive as one burst per item.
+extern __shared__ __align__(128) unsigned char g_stage[];
+__shared__ int g_staged;             // 1 while the current item's A is staged
+__shared__ int g_stage_first;        // first staged slot
+__shared__ unsigned int g_stage_voff;  // byte offset of the values in g_stage
+__shared__ __align__(8) unsigned long long g_stage_bar;
+
+__device__ __forceinline__ unsigned int smem_u32(const void *p) {
+  return static_cast<unsigned int>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" : : "r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" : : : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned int bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               : : "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned int bytes,
+                                         unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      : : "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned int parity) {
+  unsigned int ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+// Bounded wait on the staging barrier; false after `limit_ns`.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned int parity,
+                                                  long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = gtimer();
+  while (!mbar_try_wait(bar, parity))
+    if (gtimer() - t0 > limit_ns) return false;
+  return true;
+}
 __device__ __forceinline__ void st3(double *b, int v, const double o[3]) {
   double *q = b + 3 * (size_t)v;
   q[0] = o[0];
@@ -113,6 +159,43 @@ struct SrcPNew {  // z - beta p   (CGStep's p = z - beta*p)
   }
 };
 
+// FP32 sources for the mixed form: the FP32 shadow of a vector, or the CG
+// direction z - beta p formed from the shadows in FP32.
+struct SrcF {
+  const float *p;
+  __device__ __forceinline__ void operator()(int c, float o[3]) const {
+    const float *q = p + 3 * (size_t)c;
+    o[0] = q[0];
+    o[1] = q[1];
+    o[2] = q[2];
+  }
+};
+struct SrcPNewF {
+  const float *z, *p;
+  float beta;
+  __device__ __forceinline__ void operator()(int c, float o[3]) const {
+    const float *zq = z + 3 * (size_t)c, *pq = p + 3 * (size_t)c;
+    o[0] = fmaf(-beta, pq[0], zq[0]);
+    o[1] = fmaf(-beta, pq[1], zq[1]);
+    o[2] = fmaf(-beta, pq[2], zq[2]);
+  }
+};
+struct SrcVtoF {  // FP64 vector read by an FP32 pass (standalone y = A32 x)
+  const double *p;
+  __device__ __forceinline__ void operator()(int c, float o[3]) const {
+    const double *q = p + 3 * (size_t)c;
+    o[0] = (float)q[0];
+    o[1] = (float)q[1];
+    o[2] = (float)q[2];
+  }
+};
+__device__ __forceinline__ void st3f(float *b, int v, const double o[3]) {
+  float *q = b + 3 * (size_t)v;
+  q[0] = (float)o[0];
+  q[1] = (float)o[1];
+  q[2] = (float)o[2];
+}
+
 template <typename VT, typename Src>
 __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
                                          const Src &src, double out[3]) {
@@ -132,9 +215,9 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
       const VT m0 = ldro(q), m1 = ldro(q + 32), m2 = ldro(q + 64);
       const VT m3 = ldro(q + 96), m4 = ldro(q + 128), m5 = ldro(q + 160);
       const VT m6 = ldro(q + 192), m7 = ldro(q + 224), m8 = ldro(q + 256);
-      double xv[3];
+      VT xv[3];
       src(c[u], xv);
-      const VT x0 = (VT)xv[0], x1 = (VT)xv[1], x2 = (VT)xv[2];
+      const VT x0 = xv[0], x1 = xv[1], x2 = xv[2];
       a0 = fma(m0, x0, a0); a0 = fma(m1, x1, a0); a0 = fma(m2, x2, a0);
       a1 = fma(m3, x0, a1); a1 = fma(m4, x1, a1); a1 = fma(m5, x2, a1);
       a2 = fma(m6, x0, a2); a2 = fma(m7, x1, a2); a2 = fma(m8, x2, a2);
@@ -178,11 +261,47 @@ __device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &
   o2[0] = b0; o2[1] = b1; o2[2] = b2;
 }
 
-template <typename Src>
-__device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int v, const Src &src,
-                                         double out[3]) {
-  if (fp32) spmv_row<float>(D.A, D.A.v32, v, src, out);
-  else spmv_row<double>(D.A, D.A.v64, v, src, out);
+// Same product with this item's block columns and values read from the
+// shared-memory stage.
+template <typename VT, typename Src>
+__device__ __forceinline__ void spmv_row_staged(const SellMatrix &A, int v, const Src &src,
+                                                double out[3]) {
+  const int s = v >> 5, lane = v & 31;
+  const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
+  const int base = g_stage_first;
+  const int *cs = reinterpret_cast<const int *>(g_stage);
+  const VT *vs = reinterpret_cast<const VT *>(g_stage + g_stage_voff);
+  VT a0 = 0, a1 = 0, a2 = 0;
+  for (int jb = j0; jb < j1; jb += 8) {
+    int c[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) c[u] = (jb + u < j1) ? cs[(jb + u - base) * kSlice + lane] : -1;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      if (c[u] < 0) break;
+      VT xv[3];
+      src(c[u], xv);
+      const VT *q = vs + (size_t)(jb + u - base) * (9 * kSlice) + lane;
+      const VT x0 = xv[0], x1 = xv[1], x2 = xv[2];
+      a0 = fma(q[0], x0, a0); a0 = fma(q[32], x1, a0); a0 = fma(q[64], x2, a0);
+      a1 = fma(q[96], x0, a1); a1 = fma(q[128], x1, a1); a1 = fma(q[160], x2, a1);
+      a2 = fma(q[192], x0, a2); a2 = fma(q[224], x1, a2); a2 = fma(q[256], x2, a2);
+    }
+  }
+  out[0] = (double)a0;
+  out[1] = (double)a1;
+  out[2] = (double)a2;
+}
+
+template <typename Src64, typename Src32>
+__device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int v, const Src64 &src64,
+                                         const Src32 &src32, double out[3]) {
+  if (fp32) {
+    if (g_staged) spmv_row_staged<float>(D.A, v, src32, out);
+    else spmv_row<float>(D.A, D.A.v32, v, src32, out);
+  } else {
+    spmv_row<double>(D.A, D.A.v64, v, src64, out);
+  }
 }
 
 // --------------------------------------------------- vertex constraints --
@@ -596,6 +715,10 @@ __device__ void epilogue_full(const InstDesc &D, const InstState &S, const VCons
   st3(B(D, B_G0 + S.gc), v, g);
   st3(B(D, B_Z0 + S.zc), v, z);
   st3(B(D, B_P0 + S.pc), v, z);
+  if (D.prec == PREC_MIXED) {
+    st3f(D.buf32[F_Z0 + S.zc], v, z);
+    st3f(D.buf32[F_P0 + S.pc], v, z);
+  }
   st3(B(D, B_BT0 + S.bc), v, beta);
   const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
   part[0] += dot3(gp, gp);
@@ -614,6 +737,7 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
 #pragma unroll
     for (int d = 0; d < 3; ++d) t[d] = seeded_uniform(D.seed, 3ull * v + d);
     st3(B(D, B_W1), v, t);
+    if (f32) st3f(D.buf32[F_W1], v, t);
     part[0] += dot3(t, t);
     return;
   }
@@ -633,11 +757,16 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
   if (S.phase == PH_POW_LAST) return;
   st3(B(D, B_T0 + (k & 1)), v, u);
   double w[3];
-  spmv_any(D, f32, v, SrcV{src}, w);  // A (src / ||w||) = (A src) / ||w||
+  // A (src / ||w||) = (A src) / ||w||; the FP32 pass reads src's FP32 shadow
+  // (the stored start vector ev has none and takes the FP64 pass).
+  const bool f32src = f32 && S.pow_src >= 0;
+  spmv_any(D, f32src, v, SrcV{src},
+           SrcF{f32src ? D.buf32[S.pow_src == B_W ? F_W0 : F_W1] : nullptr}, w);
   w[0] *= S.pow_scale;
   w[1] *= S.pow_scale;
   w[2] *= S.pow_scale;
   st3(B(D, (k & 1) ? B_W1 : B_W), v, w);
+  if (f32) st3f(D.buf32[(k & 1) ? F_W1 : F_W0], v, w);
   part[1] += dot3(w, w);
 }
 
@@ -683,7 +812,8 @@ __device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, 
       st3(B(D, B_E), v, e);
       part[2] += dot3(p, e);
     }
-    spmv_any(D, f32 && S.phase != PH_PL_SPMV, v, SrcV{pp}, ap);
+    spmv_any(D, f32 && S.phase != PH_PL_SPMV, v, SrcV{pp},
+             SrcF{f32 ? D.buf32[F_P0 + S.pc] : nullptr}, ap);
   } else {
     const double *zz = B(D, B_Z0 + S.zc), *po = B(D, B_P0 + S.pc);
     double z[3];
@@ -692,7 +822,11 @@ __device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, 
 #pragma unroll
     for (int d = 0; d < 3; ++d) p[d] = z[d] - S.beta_cg * p[d];
     st3(B(D, B_P0 + (S.pc ^ 1)), v, p);
-    spmv_any(D, f32 && S.phase != PH_PL_SPMV, v, SrcPNew{zz, po, S.beta_cg}, ap);
+    const bool f32p = f32 && S.phase != PH_PL_SPMV;
+    if (f32p) st3f(D.buf32[F_P0 + (S.pc ^ 1)], v, p);
+    spmv_any(D, f32p, v, SrcPNew{zz, po, S.beta_cg},
+             SrcPNewF{f32p ? D.buf32[F_Z0 + S.zc] : nullptr,
+                      f32p ? D.buf32[F_P0 + S.pc] : nullptr, (float)S.beta_cg}, ap);
     if (S.e_nz && S.phase == PH_CG_SPMV) {
       double e[3];
       ld3(B(D, B_E), v, e);
@@ -753,6 +887,7 @@ __device__ __noinline__ void row_cg_yf(const InstDesc &D, const InstState &S, in
   precond_v(D, C, f, v, gy, phi, z);
   beta_v(D, C, f, gy, phi, beta);
   st3(B(D, B_Z0 + (S.zc ^ 1)), v, z);
+  if (D.prec == PREC_MIXED) st3f(D.buf32[F_Z0 + (S.zc ^ 1)], v, z);
   st3(B(D, B_BT0 + (S.bc ^ 1)), v, beta);
   const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
   part[3] += dot3(z, ap);
@@ -792,6 +927,7 @@ __device__ __noinline__ void row_ru(const InstDesc &D, const InstState &S, int v
   beta_v(D, C, f, g, phi, beta);
   st3(B(D, B_G0 + S.gc), v, g);
   st3(B(D, B_Z0 + S.zc), v, z);
+  st3f(D.buf32[F_Z0 + S.zc], v, z);  // residual replacement runs in the mixed form only
   st3(B(D, B_BT0 + S.bc), v, beta);
   const double gp[3] = {phi[0] + beta[0], phi[1] + beta[1], phi[2] + beta[2]};
   part[0] += dot3(gp, gp);
@@ -1362,10 +1498,19 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
   __shared__ int s_last;
   Ctl *ctl = args.ctl;
   const long long t_start = gtimer();
+  __shared__ int s_cache_inst, s_cache_ph;  // instance/phase of the sD, sS copies
+  if (threadIdx.x == 0) {
+    mbar_init(&g_stage_bar);
+    g_staged = 0;
+    s_cache_inst = -1;
+    s_cache_ph = -1;
+  }
+  __syncthreads();
+  unsigned int stage_parity = 0;
   for (int ph = 0; ph < args.max_phases; ++ph) {
     for (int item = blockIdx.x; item < args.total_items; item += gridDim.x) {
       const int inst = find_instance(args.item_prefix, args.ninst, item);
-      {
+      if (inst != s_cache_inst || ph != s_cache_ph) {
         const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
         int *dstd = reinterpret_cast<int *>(&sD);
         for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads)
@@ -1374,6 +1519,11 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
         int *dsts = reinterpret_cast<int *>(&sS);
         for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads)
           dsts[w] = srcs[w];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          s_cache_inst = inst;
+          s_cache_ph = ph;
+        }
       }
       __syncthreads();
       if (sS.phase == PH_DONE) {
@@ -1382,6 +1532,41 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
       }
       const int local = item - sD.item_begin;
       const int v = local * kThreads + threadIdx.x;
+      // Stage A for the FP32 matrix passes when the item's slice fits.
+      const bool fp32_pass = sD.prec == PREC_MIXED &&
+                             (sS.phase == PH_POW || sS.phase == PH_CG_SPMV ||
+                              (sS.phase == PH_CG_ENTRY && sS.g_cons));
+      if (fp32_pass && args.stage_bytes > 0) {
+        if (threadIdx.x == 0) {
+          const int s0 = local * (kThreads / kSlice);
+          const int s1 = min(s0 + kThreads / kSlice, sD.A.nslices);
+          const int f = ldro(sD.A.slice_off + s0), l = ldro(sD.A.slice_off + s1);
+          const unsigned int cb = (unsigned int)(l - f) * kSlice * 4u;
+          const unsigned int vb = (unsigned int)(l - f) * kSlice * 9u * 4u;
+          if (cb + vb <= (unsigned int)args.stage_bytes && l > f) {
+            g_staged = 1;
+            g_stage_first = f;
+            g_stage_voff = cb;
+            asm volatile("fence.proxy.async.shared::cta;" : : : "memory");
+            mbar_expect_tx(&g_stage_bar, cb + vb);
+            bulk_g2s(g_stage, sD.A.cols + (size_t)f * kSlice, cb, &g_stage_bar);
+            bulk_g2s(g_stage + cb, sD.A.v32 + (size_t)f * kSlice * 9, vb, &g_stage_bar);
+          } else {
+            g_staged = 0;
+          }
+        }
+        __syncthreads();
+        if (g_staged) {
+          if (!mbar_wait_bounded(&g_stage_bar, stage_parity, args.wait_ns)) {
+            // Record the failure, give the copy a second bounded wait so no
+            // transfer lands after exit, then leave.
+            if (threadIdx.x == 0) atomicCAS(&ctl->err, 0, -4);
+            mbar_wait_bounded(&g_stage_bar, stage_parity, args.wait_ns);
+            return;
+          }
+          stage_parity ^= 1u;
+        }
+      }
       double part[kPart];
 #pragma unroll
       for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
@@ -1421,6 +1606,7 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
         }
       }
       __syncthreads();
+      if (threadIdx.x == 0) g_staged = 0;
     }
     int active;
     if (!grid_barrier(ctl, args.wait_ns, active)) return;
@@ -1503,7 +1689,8 @@ __global__ void __launch_bounds__(256) spmv_kernel(SellMatrix A, const VT *__res
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   double o[3];
-  spmv_row<VT>(A, vals, v, SrcV{x}, o);
+  if constexpr (sizeof(VT) == 4) spmv_row<VT>(A, vals, v, SrcVtoF{x}, o);
+  else spmv_row<VT>(A, vals, v, SrcV{x}, o);
   st3(y, v, o);
 }
 
@@ -1511,10 +1698,14 @@ __global__ void __launch_bounds__(256) spmv_kernel(SellMatrix A, const VT *__res
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream) {
   void *params[] = {(void *)&args};
   return cudaLaunchCooperativeKernel((const void *)engine_kernel, dim3(grid), dim3(kThreads),
-                                     params, 0, stream);
+                                     params, (size_t)args.stage_bytes, stream);
 }
-cudaError_t engine_max_blocks_per_sm(int *n) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, engine_kernel, kThreads, 0);
+// Resident engine CTAs per SM with `stage_bytes` of dynamic shared memory.
+cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
+  cudaError_t e = cudaFuncSetAttribute(engine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kStageBytes);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, engine_kernel, kThreads, stage_bytes);
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,

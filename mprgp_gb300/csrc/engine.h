@@ -19,6 +19,7 @@ constexpr int kSlice = 32;          // SELL slice height (one warp)
 constexpr int kPart = 10;           // partial sums per item (slot kMinSlot is a min)
 constexpr int kMinSlot = 9;
 constexpr int kMaxPlanes = 3;       // plane constraints per vertex
+constexpr int kStageBytes = 192 * 1024;  // shared-memory stage of one item's FP32 A
 
 enum Kind : int { KIND_LOWER = 0, KIND_BOX = 1, KIND_DECOUPLED = 2, KIND_PLANES = 3 };
 enum Alg : int { ALG_MONOTONE = 1, ALG_PLAIN = 2 };
@@ -30,6 +31,10 @@ enum Buf : int {
   B_X0 = 0, B_X1, B_G0, B_G1, B_Z0, B_Z1, B_P0, B_P1, B_BT0, B_BT1,
   B_AP, B_W, B_E, B_T0, B_T1, B_W1, kNumBuf
 };
+// FP32 shadows of the vectors the mixed form's FP32 matrix passes read
+// (z, p and the power iterate), each 3*nv floats, written by the phase that
+// produces the FP64 vector.
+enum Buf32 : int { F_Z0 = 0, F_Z1, F_P0, F_P1, F_W0, F_W1, kNumBuf32 };
 
 enum Phase : int {
   PH_DONE = 0,
@@ -95,6 +100,7 @@ struct InstDesc {
   const double *L, *U;        // bounds kinds
   unsigned char *face;        // one per constraint row / per unknown
   double *buf[kNumBuf];
+  float *buf32[kNumBuf32];    // mixed form only
   double *ev;
   double *part;               // nitems * kPart
   unsigned int *cnt;          // items finished in the current phase
@@ -120,6 +126,8 @@ struct EngineArgs {
   int max_phases;          // quantum / hard bound on macro-phases
   long long wait_ns;       // bound on a barrier wait
   long long total_ns;      // bound on the whole launch
+  int stage_bytes;         // dynamic shared memory for staging (0 = off)
+  int pad;
   Ctl *ctl;
 };
 

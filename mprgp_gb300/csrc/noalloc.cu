@@ -38,7 +38,7 @@
 
 namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
-cudaError_t engine_max_blocks_per_sm(int *n);
+cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,
                         double *dinv, cudaStream_t st);
@@ -94,7 +94,7 @@ int setup_device(DeviceSetup **out) {
     NCK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return err(MPRGP_NO_DEVICE, "device lacks cooperative launch");
     NCK(cudaDeviceGetAttribute(&d.nsm, cudaDevAttrMultiProcessorCount, dev));
-    NCK(engine_max_blocks_per_sm(&d.bps));
+    NCK(engine_max_blocks_per_sm(&d.bps, 0));
     if (d.bps < 1) return err(MPRGP_NO_DEVICE, "engine kernel cannot be resident");
     d.base = static_cast<unsigned char *>(ptr);
     d.ready = true;
@@ -194,6 +194,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   const size_t o_nn = c.take<double>(std::max(m, 1)), o_indn = c.take<double>(std::max(m, 1));
   const size_t o_face = c.take<unsigned char>(std::max(m, 1));
   const size_t o_vec = c.take<double>(n * kNumBuf), o_ev = c.take<double>(n);
+  const size_t o_vec32 = mixed ? c.take<float>(n * kNumBuf32) : 0;
   const size_t o_part = c.take<double>((size_t)nitems * kPart);
   if (c.off > kNoAllocScratchBytes) {
     return err(MPRGP_INVALID, "solve_noalloc: problem needs " + std::to_string(c.off >> 20) +
@@ -253,6 +254,8 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   D.pl_indn = d_indn;
   D.face = d_face;
   for (int i = 0; i < kNumBuf; ++i) D.buf[i] = d_vec + (size_t)i * n;
+  for (int i = 0; i < kNumBuf32; ++i)
+    D.buf32[i] = mixed ? reinterpret_cast<float *>(base + o_vec32) + (size_t)i * n : nullptr;
   D.ev = reinterpret_cast<double *>(base + o_ev);
   D.part = reinterpret_cast<double *>(base + o_part);
   D.cnt = d_cnt;
@@ -281,6 +284,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   args.max_phases = (int)std::min<long long>(1100LL + 8LL * ((long long)opt->max_it + 2), INT_MAX);
   args.wait_ns = (long long)(wait_s * 1e9);
   args.total_ns = (long long)(std::max(60.0, 20.0 * wait_s) * 1e9);
+  args.stage_bytes = 0;
   args.ctl = ctl;
   const int grid = std::max(1, std::min(nitems, dev->nsm * dev->bps));
   const auto t0 = std::chrono::steady_clock::now();
