@@ -112,10 +112,11 @@ int mprgp_context_sync(mprgp_context *ctx);
 /* SM count and resident engine CTAs per SM (the persistent grid's shape). */
 int mprgp_context_info(mprgp_context *ctx, int *nsm, int *blocks_per_sm);
 /* Launch shape of later solves on this context (chosen by the autotuner,
- * mprgp_gb300/autotune.py): stage = 1 brings each item's FP32 matrix slice
- * into shared memory with bulk async copies (one CTA per SM), 0 reads it
- * from global memory (two CTAs per SM); ctas_per_sm caps the persistent
- * grid (0 = every resident CTA). */
+ * mprgp_gb300/autotune.py): bit 0 of stage = 1 brings each item's FP32
+ * matrix slice into shared memory with bulk async copies (one CTA per SM),
+ * 0 reads it from global memory; bit 1 of stage = 1 runs the power method in
+ * the persistent engine instead of the dedicated power kernel; ctas_per_sm
+ * caps the persistent grid (0 = every resident CTA). */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
 
 /* ---- problem: one QP instance resident in device memory ----------------- */

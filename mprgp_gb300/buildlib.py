@@ -35,6 +35,7 @@ def _compile(src: str, ptxas_verbose: bool) -> str:
            "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
     if src.endswith(".cu"):
         cmd += ARCH + ["-lineinfo"]
+        cmd += os.environ.get("MPRGP_NVCC_FLAGS", "").split()
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
     else:

@@ -21,6 +21,7 @@
 
 namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
+cudaError_t launch_power(const EngineArgs &args, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,
@@ -39,6 +40,7 @@ struct mprgp_context {
   Ctl *ctl = nullptr;
   int nsm = 0, bps = 0, bps_stage = 0;
   int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
+  int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
   int ctas_per_sm = 0;   // persistent CTAs per SM (0 = all resident)
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   mprgp_problem *scratch = nullptr;  // reused by mprgp_solve_bsr
@@ -211,9 +213,8 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   s->xc = p->xc;
   s->code = -1;
   s->ev_valid = (o->use_ev && p->ev_valid) ? 1 : 0;
-  if (o->project_x0) {
-    s->phase = PH_PROJ0;
-  } else if (s->ev_valid) {
+  d->project_x0 = o->project_x0 ? 1 : 0;
+  if (s->ev_valid) {
     s->phase = PH_POW;
     s->pow_src = -1;
     s->pow_scale = 1.0;
@@ -306,6 +307,11 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
   const int grid = std::max(1, std::min(prefix[n], c->nsm * per_sm));
   CK(cudaEventRecord(c->e0, s));
+  // The power method first, as ordinary launches (at most 1003 phases: the
+  // seeded start, 1001 iterations, the last difference); then the engine.
+  if (c->power_kernel) {
+    for (int k = 0; k < 1003; ++k) CK(launch_power(args, s));
+  }
   CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(c->e1, s));
   CK(cudaStreamSynchronize(s));
@@ -434,7 +440,9 @@ int mprgp_context_sync(mprgp_context *c) {
 }
 
 int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
-  if (!c || stage < 0 || stage > 1 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  if (!c || stage < 0 || stage > 3 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  c->power_kernel = (stage & 2) ? 0 : 1;
+  stage &= 1;
   c->stage = stage;
   c->ctas_per_sm = ctas_per_sm;
   return MPRGP_OK;

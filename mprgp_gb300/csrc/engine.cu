@@ -23,6 +23,11 @@ namespace mprgp {
 
 constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:9)
 
+// Resident CTAs per SM the engine is compiled for (register budget).
+#ifndef MPRGP_ENGINE_MIN_BLOCKS
+#define MPRGP_ENGINE_MIN_BLOCKS 4
+#endif
+
 // ------------------------------------------------------------ primitives --
 __device__ __forceinline__ long long gtimer() {
   long long t;
@@ -1185,21 +1190,11 @@ __device__ void cg_decide(const InstDesc &D, InstState &S, double dfy, double co
   else S.phase = PH_PROP_A;
 }
 
-__device__ void advance(const InstDesc &D, InstState &S, const double *s) {
-  S.phases++;
-  const int phase_in = S.phase;
+// Transitions of the power method (specRad, MPRGPSolver.h:42-79), shared by
+// the persistent engine and the dedicated power kernel.
+__device__ void advance_power(const InstDesc &D, InstState &S, const double *s) {
   const double eps = D.tol;  // specRad(A, ev, tol): eps = tol (MPRGPSolver.h:28)
   switch (S.phase) {
-    case PH_PROJ0:
-      if (S.ev_valid) {  // start from the stored vector, as given (not normalised)
-        S.pow_k = 0;
-        S.pow_src = -1;
-        S.pow_scale = 1.0;
-        S.phase = PH_POW;
-      } else {
-        S.phase = PH_POW_RAND;
-      }
-      break;
     case PH_POW_RAND:
       S.pow_k = 0;
       S.pow_src = B_W1;
@@ -1246,6 +1241,26 @@ __device__ void advance(const InstDesc &D, InstState &S, const double *s) {
       } else {
         S.power_iters = 1001;
       }
+      S.phase = PH_INIT;
+      break;
+    default:
+      break;
+  }
+  if (S.phase == PH_INIT) {  // leaving the power method
+    S.alpha_bar = 2.0 / S.spec_rad;  // MPRGPSolver.h:28
+    if (D.project_x0) S.phase = PH_PROJ0;
+  }
+}
+
+__device__ void advance(const InstDesc &D, InstState &S, const double *s) {
+  S.phases++;
+  switch (S.phase) {
+    case PH_POW_RAND:
+    case PH_POW:
+    case PH_POW_LAST:
+      advance_power(D, S, s);
+      break;
+    case PH_PROJ0:
       S.phase = PH_INIT;
       break;
     case PH_INIT:
@@ -1387,7 +1402,6 @@ __device__ void advance(const InstDesc &D, InstState &S, const double *s) {
       S.phase = PH_DONE;
       break;
   }
-  if (S.phase == PH_INIT && phase_in != PH_INIT) S.alpha_bar = 2.0 / S.spec_rad;  // :28
   // A NaN step length in a proportioning or plain step means the iteration
   // broke down (p^T A p or D^T A D was 0); the monotone CG step tolerates it
   // the way the reference does (its comparisons fail and it expands).
@@ -1490,7 +1504,7 @@ __device__ __forceinline__ int find_instance(const int *prefix, int n, int item)
   return lo;
 }
 
-__global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
+__global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kernel(EngineArgs args) {
   __shared__ InstDesc sD;
   __shared__ InstState sS;
   __shared__ double red[kPart][kThreads / 32];
@@ -1618,6 +1632,68 @@ __global__ void __launch_bounds__(kThreads, 2) engine_kernel(EngineArgs args) {
   }
 }
 
+// ------------------------------------------------------- power kernel ----
+// The power-method phases as ordinary launches: one CTA per item, one launch
+// per phase, the launch boundary as the phase barrier, the same per-row work,
+// reductions and transitions as the persistent engine (hence the same
+// results).  Its small register budget keeps every SM full of warps, which
+// the latency-bound SpMV of these phases needs.
+__global__ void __launch_bounds__(kThreads, 6) power_kernel(EngineArgs args) {
+  __shared__ InstDesc sD;
+  __shared__ InstState sS;
+  __shared__ double red[kPart][kThreads / 32];
+  __shared__ double sums[kPart];
+  __shared__ int s_last;
+  const int item = blockIdx.x;
+  const int inst = find_instance(args.item_prefix, args.ninst, item);
+  if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
+  {
+    const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
+    int *dstd = reinterpret_cast<int *>(&sD);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads) dstd[w] = ldro(srcd + w);
+  }
+  __syncthreads();
+  {
+    const int *srcs = reinterpret_cast<const int *>(sD.st);
+    int *dsts = reinterpret_cast<int *>(&sS);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads) dsts[w] = srcs[w];
+  }
+  __syncthreads();
+  const int phase = sS.phase;
+  if (phase != PH_POW_RAND && phase != PH_POW && phase != PH_POW_LAST) return;
+  const int local = item - sD.item_begin;
+  const int v = local * kThreads + threadIdx.x;
+  double part[kPart];
+#pragma unroll
+  for (int k = 0; k < kPart; ++k) part[k] = 0.0;
+  if (v < sD.nv) row_power(sD, sS, v, part);
+  const int ns = nslots(phase);
+  const double r = block_reduce(part, red, ns, false);
+  if (threadIdx.x < ns) sD.part[(size_t)local * kPart + threadIdx.x] = r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int old = atom_add_acq_rel(sD.cnt, 1u);
+    s_last = (old == (unsigned int)sD.nitems - 1u);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  double acc[kPart];
+#pragma unroll
+  for (int k = 0; k < kPart; ++k) acc[k] = 0.0;
+  for (int it = threadIdx.x; it < sD.nitems; it += kThreads)
+    for (int k = 0; k < ns; ++k) acc[k] += sD.part[(size_t)it * kPart + k];
+  const double t = block_reduce(acc, red, ns, false);
+  if (threadIdx.x < ns) sums[threadIdx.x] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    InstState S = sS;
+    S.phases++;
+    advance_power(sD, S, sums);
+    *sD.st = S;
+    *sD.cnt = 0u;
+  }
+}
+
 // ------------------------------------------------------ setup kernels -----
 // BSR (row_ptr, cols, 9 values per block, row-major) -> SELL-32, plus
 // D^-1 = 1/diag(A) (getDiagonal, MPRGPUtility.h:503-515).
@@ -1706,6 +1782,10 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
                                        kStageBytes);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, engine_kernel, kThreads, stage_bytes);
+}
+cudaError_t launch_power(const EngineArgs &args, cudaStream_t stream) {
+  power_kernel<<<args.total_items, kThreads, 0, stream>>>(args);
+  return cudaGetLastError();
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,

@@ -36,6 +36,8 @@ enum Buf : int {
 // produces the FP64 vector.
 enum Buf32 : int { F_Z0 = 0, F_Z1, F_P0, F_P1, F_W0, F_W1, kNumBuf32 };
 
+// A solve starts with the power method (independent of x), then projects x
+// if asked (the solve(A,B,J,c,x) overloads), then runs MPRGP.
 enum Phase : int {
   PH_DONE = 0,
   PH_PROJ0,     // x = P(x)
@@ -89,7 +91,7 @@ struct InstDesc {
   SellMatrix A;
   int nv, nitems, item_begin, m;
   int kind, alg, pre, prec;
-  int max_it, pad1;
+  int max_it, project_x0;
   double tol;
   unsigned long long seed;
   const double *b, *dinv;

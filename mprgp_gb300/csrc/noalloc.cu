@@ -263,7 +263,8 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   InstState S;
   std::memset(&S, 0, sizeof(S));
   S.code = -1;
-  S.phase = opt->project_x0 ? PH_PROJ0 : PH_POW_RAND;
+  S.phase = PH_POW_RAND;
+  D.project_x0 = opt->project_x0 ? 1 : 0;
   const int pref[2] = {0, nitems};
   Ctl c0;
   std::memset(&c0, 0, sizeof(c0));
