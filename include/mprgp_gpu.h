@@ -193,6 +193,40 @@ int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *row_ptr, cons
 int mprgp_solve_batch(mprgp_context *ctx, int count, mprgp_problem *const *probs,
                       const mprgp_options *opts, mprgp_stats *stats);
 
+/* ---- serving: continuous batching of QP requests ------------------------- */
+/* No counterpart in the reference API (its FEM driver solves one QP per frame,
+ * MprgpFemSolver.cpp:521-533); this is the serving form of the solver.
+ * A request is a new scene (host BSR A, b, planes, x0 -- copied at submit;
+ * project_x0 applies) or, with row_ptr == NULL, the next timestep of a live
+ * scene: only b is new, and A, the planes, x (the last solution) and the face
+ * stay resident on the device and warm-start the solve.  Each step admits
+ * queued requests into free slots while their device footprint fits the HBM
+ * budget (idle scenes are evicted least-recently-used first), advances all
+ * admitted requests together by one engine quantum and retires the finished
+ * ones.  Results do not depend on the mix: every instance reduces in a fixed
+ * order.  Plane kinds (DECOUPLED, PLANES). */
+typedef struct mprgp_server_config {
+  size_t hbm_budget;  /* device bytes for resident scenes (0 = 80% of free) */
+  int max_slots;      /* requests in flight (0 = 64) */
+  int quantum_phases; /* engine macro-phases per step (0 = 256) */
+  int power_launches; /* power-kernel launches per step (0..1003) */
+  int pad;
+} mprgp_server_config;
+typedef struct mprgp_server mprgp_server;
+int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out);
+int mprgp_server_destroy(mprgp_server *srv);
+int mprgp_server_submit(mprgp_server *srv, int scene, int nv, int nnzb, const int *row_ptr,
+                        const int *cols, const double *vals, const double *b,
+                        const int *plane_ptr, const double *planes, const double *x0,
+                        const mprgp_options *opt, long long *ticket);
+int mprgp_server_step(mprgp_server *srv, int *running, int *queued, int *completed);
+/* state: 0 queued, 1 running, 2 done.  When done, copies x (3 nv), face and
+ * stats, times = {submit, admit, done} in seconds, releases the ticket and
+ * returns the solve's code. */
+int mprgp_server_result(mprgp_server *srv, long long ticket, double *x, unsigned char *face,
+                        mprgp_stats *stats, double *times, int *state);
+int mprgp_server_info(mprgp_server *srv, size_t *budget, size_t *used, int *scenes);
+
 /* ---- beam generator (synthetic implicit-Euler FEM QPs) ------------------- */
 typedef struct mprgp_beam_params {
   int a, b, c;          /* cube counts along x, y (up), z */

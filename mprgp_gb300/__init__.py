@@ -43,6 +43,11 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_slots", C.c_int), ("quantum_phases", C.c_int),
+                ("power_launches", C.c_int), ("pad", C.c_int)]
+
+
 class BeamParams(C.Structure):
     _fields_ = [("a", C.c_int), ("b", C.c_int), ("c", C.c_int), ("edge", C.c_double),
                 ("young", C.c_double), ("poisson", C.c_double), ("rho", C.c_double),
@@ -99,6 +104,13 @@ def _sig(lib):
       C.POINTER(Stats))
     s("mprgp_solve_noalloc", C.c_int, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
       C.POINTER(Options), _P, _P, C.POINTER(Stats))
+    s("mprgp_server_create", C.c_int, _P, C.POINTER(ServerConfig), C.POINTER(_P))
+    s("mprgp_server_destroy", C.c_int, _P)
+    s("mprgp_server_submit", C.c_int, _P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P,
+      C.POINTER(Options), C.POINTER(C.c_longlong))
+    s("mprgp_server_step", C.c_int, _P, _IP, _IP, _IP)
+    s("mprgp_server_result", C.c_int, _P, C.c_longlong, _P, _P, C.POINTER(Stats), _P, _IP)
+    s("mprgp_server_info", C.c_int, _P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), _IP)
     s("mprgp_beam_default", None, C.POINTER(BeamParams))
     s("mprgp_beam_sizes", C.c_int, C.POINTER(BeamParams), _IP, _IP, _IP)
     s("mprgp_beam_build", C.c_int, C.POINTER(BeamParams), _P, _P, _P, _P, _P, _P, _P)
@@ -349,6 +361,70 @@ def load_beam(ctx: Context, qp: BeamQP, precisions=1) -> Problem:
     pr.set_planes(qp.plane_ptr, qp.planes)
     pr.set_x(qp.x0)
     return pr
+
+
+class Server:
+    """Continuous-batching QP server (mprgp_server_*)."""
+
+    def __init__(self, ctx: Context, hbm_budget=0, max_slots=0, quantum_phases=0,
+                 power_launches=256):
+        self.ctx = ctx
+        cfg = ServerConfig(hbm_budget, max_slots, quantum_phases, power_launches, 0)
+        self.h = C.c_void_p()
+        _check(lib().mprgp_server_create(ctx.h, C.byref(cfg), C.byref(self.h)), "server_create")
+        self.nv = {}
+
+    def close(self):
+        if self.h:
+            lib().mprgp_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, scene: int, qp: BeamQP, opt: Options, b=None, followup=False) -> int:
+        t = C.c_longlong()
+        rhs = np.ascontiguousarray(qp.b if b is None else b, np.float64)
+        if followup:
+            _check(lib().mprgp_server_submit(self.h, scene, qp.nv, 0, None, None, None, _ptr(rhs),
+                                             None, None, None, C.byref(opt), C.byref(t)),
+                   "server_submit")
+        else:
+            _check(lib().mprgp_server_submit(self.h, scene, qp.nv, qp.nnzb, _ptr(qp.row_ptr),
+                                             _ptr(qp.cols), _ptr(qp.vals), _ptr(rhs),
+                                             _ptr(qp.plane_ptr), _ptr(qp.planes), _ptr(qp.x0),
+                                             C.byref(opt), C.byref(t)), "server_submit")
+        self.nv[t.value] = (qp.nv, len(qp.planes))
+        return t.value
+
+    def step(self):
+        r, q, c = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().mprgp_server_step(self.h, C.byref(r), C.byref(q), C.byref(c)), "server_step")
+        return r.value, q.value, c.value
+
+    def result(self, ticket: int):
+        """(state, x, face, stats, times) -- x etc. are None until state == 2."""
+        nv, m = self.nv[ticket]
+        x = np.zeros(3 * nv)
+        face = np.zeros(max(m, 1), np.uint8)
+        st = Stats()
+        times = np.zeros(3)
+        state = C.c_int()
+        rc = lib().mprgp_server_result(self.h, ticket, _ptr(x), _ptr(face), C.byref(st),
+                                       _ptr(times), C.byref(state))
+        if state.value != 2:
+            return state.value, None, None, None, None
+        _check(rc, "server_result")
+        del self.nv[ticket]
+        return 2, x, face[:m], st, times
+
+    def info(self):
+        b, u, n = C.c_size_t(), C.c_size_t(), C.c_int()
+        _check(lib().mprgp_server_info(self.h, C.byref(b), C.byref(u), C.byref(n)), "server_info")
+        return b.value, u.value, n.value
 
 
 def solve_noalloc(stream: int, nv: int, nnzb: int, row_ptr: int, cols: int, vals: int, b: int,

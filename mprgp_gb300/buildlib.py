@@ -1,6 +1,7 @@
 """Builds libmprgp_gb300.so in-tree with nvcc for sm_103a.
 
-Four translation units (engine.cu, capi.cu, noalloc.cu, beam.cpp) are compiled in
+Five translation units (engine.cu, capi.cu, noalloc.cu, server.cu, beam.cpp) are
+compiled in
 parallel and linked into mprgp_gb300/_build/libmprgp_gb300.so.  The same
 recipe runs on the x86_64 build host and the aarch64 GPU host: no
 architecture-specific host flags.
@@ -19,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmprgp_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "beam.cpp"]
+SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "server.cu", "beam.cpp"]
 
 
 def nvcc() -> str:

@@ -257,9 +257,18 @@ int ensure_launch_arrays(mprgp_context *c, int ninst) {
   return MPRGP_OK;
 }
 
-// Launches the engine over `n` prepared instances until all are done.
-int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
-               mprgp_stats *stats) {
+}  // namespace
+
+namespace mprgp {
+
+// One engine run over `n` problems.  Instances with fresh[i] != 0 start a
+// solve (their initial state is uploaded); the others resume from the state
+// left in device memory by the previous run.  The run advances everything by
+// at most `quantum` engine macro-phases (0: until all are done) after up to
+// `power_launches` launches of the power kernel.  done[i] reports instances
+// that finished (or failed); stats are filled for every instance.
+int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
+               const int *fresh, int quantum, int power_launches, mprgp_stats *stats, int *done) {
   int rc = ensure_launch_arrays(c, n);
   if (rc) return rc;
   std::vector<InstDesc> desc(n);
@@ -282,6 +291,7 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   if (wait_s <= 0.0) wait_s = 5.0;
   cudaStream_t s = c->stream;
   for (int i = 0; i < n; ++i) {
+    if (!fresh[i]) continue;
     CK(cudaMemcpyAsync(probs[i]->st, &st[i], sizeof(InstState), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(probs[i]->cnt, 0, sizeof(unsigned int), s));
   }
@@ -297,7 +307,9 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   args.item_prefix = c->d_prefix;
   args.ninst = n;
   args.total_items = prefix[n];
-  args.max_phases = (int)std::min<long long>(phase_bound, INT_MAX);
+  long long maxp = phase_bound;
+  if (quantum > 0) maxp = std::min<long long>(maxp, quantum);
+  args.max_phases = (int)std::min<long long>(maxp, INT_MAX);
   args.wait_ns = (long long)(wait_s * 1e9);
   args.total_ns = (long long)(std::max(60.0, 20.0 * wait_s) * 1e9);
   const bool stage = c->stage && c->bps_stage > 0;
@@ -309,9 +321,8 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   CK(cudaEventRecord(c->e0, s));
   // The power method first, as ordinary launches (at most 1003 phases: the
   // seeded start, 1001 iterations, the last difference); then the engine.
-  if (c->power_kernel) {
-    for (int k = 0; k < 1003; ++k) CK(launch_power(args, s));
-  }
+  if (c->power_kernel)
+    for (int k = 0; k < power_launches; ++k) CK(launch_power(args, s));
   CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(c->e1, s));
   CK(cudaStreamSynchronize(s));
@@ -325,16 +336,29 @@ int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   int worst = MPRGP_OK;
   for (int i = 0; i < n; ++i) {
     InstState &x = st[i];
+    const bool finished = x.phase == PH_DONE;
     if (ctl1.err) x.code = ctl1.err;
-    else if (x.phase != PH_DONE) x.code = MPRGP_TIMEOUT;
+    else if (!finished && quantum <= 0) x.code = MPRGP_TIMEOUT;
     probs[i]->xc = x.xc;
     probs[i]->trace_n = x.trace_n;
-    if (x.ev_upd && x.code > MPRGP_BREAKDOWN) probs[i]->ev_valid = 1;
+    if (finished && x.ev_upd && x.code > MPRGP_BREAKDOWN) probs[i]->ev_valid = 1;
     fill_stats(x, ms, stats ? &stats[i] : nullptr);
-    if (x.code < worst) worst = x.code;
+    if (done) done[i] = finished || ctl1.err || (!finished && quantum <= 0);
+    if ((finished || quantum <= 0) && x.code < worst) worst = x.code;
   }
   if (ctl1.err) return fail(ctl1.err, "device wait limit reached");
   return worst < MPRGP_NOT_CONVERGED ? worst : MPRGP_OK;
+}
+
+}  // namespace mprgp
+
+namespace {
+
+// Launches the engine over `n` prepared instances until all are done.
+int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
+               mprgp_stats *stats) {
+  std::vector<int> fresh(n, 1);
+  return mprgp::engine_run(c, n, probs, opts, fresh.data(), 0, 1003, stats, nullptr);
 }
 
 }  // namespace

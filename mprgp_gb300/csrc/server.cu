@@ -1,0 +1,320 @@
+// Continuous-batching QP server (the serving form).
+//
+// Requests are either new scenes (host A, b, planes, x0, copied at submit) or
+// follow-up timesteps of a live scene (a new b; A, the planes, x and the face
+// stay resident from the previous solve and warm-start the next one, as the
+// reference's FEM driver re-solves each frame, MprgpFemSolver.cpp:521-533).
+// Each mprgp_server_step admits queued requests into free slots while their
+// device footprint fits the HBM budget (evicting idle scenes, least recently
+// used first), then advances every admitted request by one engine quantum --
+// all of them in the same launches, so their work overlaps on the device --
+// and retires the ones that finished.  A request's result does not depend on
+// what else is in flight: each instance's reductions run in a fixed order.
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mprgp_gpu.h"
+#include "engine.h"
+
+namespace mprgp {
+int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
+               const int *fresh, int quantum, int power_launches, mprgp_stats *stats, int *done);
+void set_last_error(const char *what);
+}  // namespace mprgp
+
+namespace {
+
+struct Request {
+  long long ticket = 0;
+  int scene = 0;
+  bool followup = false;
+  int nv = 0, nnzb = 0;
+  std::vector<int> row_ptr, cols, plane_ptr;
+  std::vector<double> vals, b, planes, x0;
+  mprgp_options opt{};
+  int state = 0;  // 0 queued, 1 running, 2 done
+  int code = 0;
+  std::vector<double> x;
+  std::vector<unsigned char> face;
+  mprgp_stats stats{};
+  double t_submit = 0, t_admit = 0, t_done = 0;
+};
+
+struct Scene {
+  mprgp_problem *prob = nullptr;
+  size_t bytes = 0;
+  long long last_use = 0;
+  bool busy = false;
+  int m = 0;
+};
+
+double now_s() {
+  using clk = std::chrono::steady_clock;
+  static const clk::time_point t0 = clk::now();
+  return std::chrono::duration<double>(clk::now() - t0).count();
+}
+
+int err(int code, const char *what) {
+  mprgp::set_last_error(what);
+  return code;
+}
+
+}  // namespace
+
+struct mprgp_server {
+  mprgp_context *ctx = nullptr;
+  size_t budget = 0, used = 0;
+  int max_slots = 64, quantum = 256, power_launches = 256;
+  long long next_ticket = 1, clock = 0;
+  std::deque<long long> queue;
+  std::map<long long, Request> reqs;
+  std::map<int, Scene> scenes;
+  std::vector<long long> running;
+  std::vector<char> fresh_flag;  // parallel to running
+};
+
+namespace {
+
+void release_scene(mprgp_server *s, std::map<int, Scene>::iterator it) {
+  mprgp_problem_destroy(it->second.prob);
+  s->used -= it->second.bytes;
+  s->scenes.erase(it);
+}
+
+// Frees idle scenes, least recently used first, until `need` bytes fit.
+bool make_room(mprgp_server *s, size_t need) {
+  while (s->used + need > s->budget) {
+    auto victim = s->scenes.end();
+    for (auto it = s->scenes.begin(); it != s->scenes.end(); ++it)
+      if (!it->second.busy && (victim == s->scenes.end() ||
+                               it->second.last_use < victim->second.last_use))
+        victim = it;
+    if (victim == s->scenes.end()) return false;
+    release_scene(s, victim);
+  }
+  return true;
+}
+
+int admit(mprgp_server *s, Request &r) {
+  if (r.followup) {
+    auto it = s->scenes.find(r.scene);
+    Scene &sc = it->second;
+    int rc = mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
+    if (rc) return rc;
+    sc.busy = true;
+    sc.last_use = ++s->clock;
+    return MPRGP_OK;
+  }
+  const int prec = r.opt.precision == MPRGP_PREC_MIXED ? 3 : 1;
+  const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, (int)(r.planes.size() / 4), prec);
+  auto old = s->scenes.find(r.scene);
+  if (old != s->scenes.end() && !old->second.busy) release_scene(s, old);
+  Scene sc;
+  int rc = mprgp_problem_create(s->ctx, r.nv, &sc.prob);
+  if (!rc) rc = mprgp_problem_set_matrix(sc.prob, r.nnzb, r.row_ptr.data(), r.cols.data(),
+                                         r.vals.data(), prec, 0);
+  if (!rc) rc = mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
+  if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.plane_ptr.data(), r.planes.data(), 0);
+  if (!rc) rc = mprgp_problem_set_x(sc.prob, r.x0.data(), 0);
+  if (rc) {
+    if (sc.prob) mprgp_problem_destroy(sc.prob);
+    return rc;
+  }
+  sc.bytes = bytes;
+  sc.busy = true;
+  sc.last_use = ++s->clock;
+  sc.m = (int)(r.planes.size() / 4);
+  s->used += bytes;
+  s->scenes[r.scene] = sc;
+  // host copies are no longer needed
+  std::vector<int>().swap(r.row_ptr);
+  std::vector<int>().swap(r.cols);
+  std::vector<double>().swap(r.vals);
+  return MPRGP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out) {
+  if (!ctx || !out) return err(MPRGP_INVALID, "server_create");
+  auto *s = new mprgp_server();
+  s->ctx = ctx;
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  s->budget = (cfg && cfg->hbm_budget) ? cfg->hbm_budget : (size_t)(0.8 * (double)fr);
+  if (cfg && cfg->max_slots > 0) s->max_slots = cfg->max_slots;
+  if (cfg && cfg->quantum_phases > 0) s->quantum = cfg->quantum_phases;
+  if (cfg && cfg->power_launches >= 0) s->power_launches = std::min(cfg->power_launches, 1003);
+  *out = s;
+  return MPRGP_OK;
+}
+
+int mprgp_server_destroy(mprgp_server *s) {
+  if (!s) return MPRGP_OK;
+  for (auto &kv : s->scenes) mprgp_problem_destroy(kv.second.prob);
+  delete s;
+  return MPRGP_OK;
+}
+
+int mprgp_server_submit(mprgp_server *s, int scene, int nv, int nnzb, const int *row_ptr,
+                        const int *cols, const double *vals, const double *b,
+                        const int *plane_ptr, const double *planes, const double *x0,
+                        const mprgp_options *opt, long long *ticket) {
+  if (!s || !opt || !ticket || nv <= 0 || !b) return err(MPRGP_INVALID, "server_submit");
+  if (opt->kind != MPRGP_KIND_DECOUPLED && opt->kind != MPRGP_KIND_PLANES)
+    return err(MPRGP_INVALID, "server_submit: plane kinds only");
+  Request r;
+  r.ticket = s->next_ticket++;
+  r.scene = scene;
+  r.opt = *opt;
+  r.nv = nv;
+  const size_t n = 3 * (size_t)nv;
+  r.b.assign(b, b + n);
+  if (row_ptr == nullptr) {  // follow-up timestep of a live scene
+    auto it = s->scenes.find(scene);
+    if (it == s->scenes.end()) return err(MPRGP_INVALID, "server_submit: scene not resident");
+    r.followup = true;
+    r.opt.project_x0 = 0;  // x is the scene's last solution (feasible)
+    r.face.assign(std::max(it->second.m, 1), 0);
+  } else {
+    if (!cols || !vals || !plane_ptr || !x0 || nnzb <= 0)
+      return err(MPRGP_INVALID, "server_submit: missing arrays");
+    r.nnzb = nnzb;
+    r.row_ptr.assign(row_ptr, row_ptr + nv + 1);
+    r.cols.assign(cols, cols + nnzb);
+    r.vals.assign(vals, vals + 9 * (size_t)nnzb);
+    r.plane_ptr.assign(plane_ptr, plane_ptr + nv + 1);
+    const int m = plane_ptr[nv];
+    r.planes.assign(planes, planes + 4 * (size_t)m);
+    r.x0.assign(x0, x0 + n);
+    r.face.assign(std::max(m, 1), 0);
+  }
+  r.x.assign(n, 0.0);
+  r.t_submit = now_s();
+  *ticket = r.ticket;
+  s->queue.push_back(r.ticket);
+  s->reqs.emplace(r.ticket, std::move(r));
+  return MPRGP_OK;
+}
+
+int mprgp_server_step(mprgp_server *s, int *running, int *queued, int *completed) {
+  if (!s) return err(MPRGP_INVALID, "server_step");
+  // Admission: FIFO, skipping requests that do not fit yet.
+  for (auto it = s->queue.begin(); it != s->queue.end();) {
+    if ((int)s->running.size() >= s->max_slots) break;
+    Request &r = s->reqs[*it];
+    bool ok = true;
+    if (r.followup) {
+      auto sc = s->scenes.find(r.scene);
+      if (sc == s->scenes.end()) {  // evicted meanwhile: cannot warm start
+        r.state = 2;
+        r.code = MPRGP_INVALID;
+        it = s->queue.erase(it);
+        continue;
+      }
+      ok = !sc->second.busy;
+    } else {
+      const int prec = r.opt.precision == MPRGP_PREC_MIXED ? 3 : 1;
+      const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, (int)(r.planes.size() / 4), prec);
+      auto sc = s->scenes.find(r.scene);
+      ok = (sc == s->scenes.end() || !sc->second.busy) && make_room(s, bytes);
+    }
+    if (!ok) {
+      ++it;
+      continue;
+    }
+    const int rc = admit(s, r);
+    if (rc) {
+      r.state = 2;
+      r.code = rc;
+      it = s->queue.erase(it);
+      continue;
+    }
+    r.state = 1;
+    r.t_admit = now_s();
+    s->running.push_back(r.ticket);
+    s->fresh_flag.push_back(1);
+    it = s->queue.erase(it);
+  }
+  int ncomp = 0;
+  const int n = (int)s->running.size();
+  if (n > 0) {
+    std::vector<mprgp_problem *> probs(n);
+    std::vector<mprgp_options> opts(n);
+    std::vector<int> fresh(n), done(n, 0);
+    std::vector<mprgp_stats> st(n);
+    for (int i = 0; i < n; ++i) {
+      Request &r = s->reqs[s->running[i]];
+      probs[i] = s->scenes[r.scene].prob;
+      opts[i] = r.opt;
+      fresh[i] = s->fresh_flag[i];
+    }
+    const int rc = mprgp::engine_run(s->ctx, n, probs.data(), opts.data(), fresh.data(),
+                                     s->quantum, s->power_launches, st.data(), done.data());
+    if (rc < MPRGP_NOT_CONVERGED) return rc;
+    std::vector<long long> still;
+    std::vector<char> still_fresh;
+    for (int i = 0; i < n; ++i) {
+      Request &r = s->reqs[s->running[i]];
+      if (!done[i]) {
+        still.push_back(r.ticket);
+        still_fresh.push_back(0);
+        continue;
+      }
+      Scene &sc = s->scenes[r.scene];
+      r.stats = st[i];
+      r.code = st[i].code;
+      mprgp_problem_get_x(sc.prob, r.x.data(), 0);
+      if (sc.m > 0) mprgp_problem_get_face(sc.prob, r.face.data());
+      sc.busy = false;
+      r.state = 2;
+      r.t_done = now_s();
+      ++ncomp;
+    }
+    s->running.swap(still);
+    s->fresh_flag.swap(still_fresh);
+  }
+  if (running) *running = (int)s->running.size();
+  if (queued) *queued = (int)s->queue.size();
+  if (completed) *completed = ncomp;
+  return MPRGP_OK;
+}
+
+int mprgp_server_result(mprgp_server *s, long long ticket, double *x, unsigned char *face,
+                        mprgp_stats *stats, double *times, int *state) {
+  if (!s) return err(MPRGP_INVALID, "server_result");
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return err(MPRGP_INVALID, "server_result: unknown ticket");
+  Request &r = it->second;
+  if (state) *state = r.state;
+  if (r.state != 2) return MPRGP_OK;
+  if (x) std::copy(r.x.begin(), r.x.end(), x);
+  if (face) std::copy(r.face.begin(), r.face.end(), face);
+  if (stats) *stats = r.stats;
+  if (times) {
+    times[0] = r.t_submit;
+    times[1] = r.t_admit;
+    times[2] = r.t_done;
+  }
+  const int code = r.code;
+  s->reqs.erase(it);
+  return code;
+}
+
+int mprgp_server_info(mprgp_server *s, size_t *budget, size_t *used, int *scenes) {
+  if (!s) return err(MPRGP_INVALID, "server_info");
+  if (budget) *budget = s->budget;
+  if (used) *used = s->used;
+  if (scenes) *scenes = (int)s->scenes.size();
+  return MPRGP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+"""Serving form: continuous batching (mprgp_server_*).
+
+* every request's result is the same alone (mprgp_solve_bsr) and in the
+  served mix, where requests arrive while others are on the GPU;
+* follow-up timesteps warm-start from the resident scene and converge to the
+  same solution as a cold solve of the same QP;
+* admission respects the HBM budget (scenes are evicted, never overcommitted).
+Tolerance: the stopping test 1e-8 ||b||; x compared to 1e-12 relative
+(in practice bitwise: each instance reduces in a fixed order).
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+import mprgp_gb300 as M
+from mprgp_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+SEED = 0x5EED
+
+
+def opts_for(qp, precision=M.PREC_MIXED, project=1):
+    return M.default_options(tol=1e-8 * np.linalg.norm(qp.b), max_it=20000,
+                             kind=M.KIND_PLANES, project_x0=project, seed=SEED,
+                             precision=precision)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
+def test_same_alone_and_in_the_mix(ctx, precision):
+    dims = [(4, 4, 6), (9, 5, 12), (3, 3, 4), (6, 8, 10), (5, 5, 5), (12, 6, 9)]
+    qps = [M.beam(*d, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=10 + i)
+           for i, (d, e) in enumerate(zip(dims, [0, 2, 1, 2, 0, 1]))]
+    alone = [ctx.solve_bsr(q, opts_for(q, precision), q.x0) for q in qps]
+    srv = M.Server(ctx, quantum_phases=64, power_launches=128, max_slots=4)
+    tickets, done = {}, {}
+    # staggered arrivals: two at a time while earlier ones are in flight
+    pending = list(range(len(qps)))
+    steps = 0
+    while len(done) < len(qps):
+        for _ in range(2):
+            if pending:
+                i = pending.pop(0)
+                tickets[srv.submit(i, qps[i], opts_for(qps[i], precision))] = i
+        srv.step()
+        steps += 1
+        for t, i in list(tickets.items()):
+            state, x, face, st, times = srv.result(t)
+            if state == 2:
+                assert st.code == 0
+                done[i] = (x, face, st)
+                del tickets[t]
+        assert steps < 10000
+    for i, (xa, fa, sa) in enumerate(alone):
+        xs, fs, ss = done[i]
+        assert rel(xs, xa) <= 1e-12, i
+        assert np.array_equal(fs, fa)
+        assert ss.iterations == sa.iterations
+    srv.close()
+
+
+def test_followup_warm_start(ctx):
+    qp = M.beam(6, 5, 10, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=3)
+    srv = M.Server(ctx, quantum_phases=128, power_launches=256)
+    t = srv.submit(0, qp, opts_for(qp))
+    while True:
+        srv.step()
+        state, x1, face1, st1, _ = srv.result(t)
+        if state == 2:
+            break
+    assert st1.code == 0
+    # next timestep: a new right-hand side, x warm-starts from x1 on the device
+    m = np.repeat(W.lumped_mass(qp), 3)
+    b2 = qp.b + m * (x1 - qp.x0)
+    t2 = srv.submit(0, qp, opts_for(qp, project=0), b=b2, followup=True)
+    while True:
+        srv.step()
+        state, x2, face2, st2, _ = srv.result(t2)
+        if state == 2:
+            break
+    assert st2.code == 0
+    # cold solve of the same next-step QP from the same start point
+    qp2 = M.BeamQP(qp.nv, qp.row_ptr, qp.cols, qp.vals, b2, x1, qp.plane_ptr, qp.planes,
+                   qp.params)
+    xc, fc, sc = ctx.solve_bsr(qp2, opts_for(qp2, project=0), x1)
+    assert sc.code == 0
+    A, b, J, c = H.qp_from_beam(qp2)
+    assert rel(x2, xc) <= 1e-12
+    assert np.array_equal(H.decide_face_planes(J, c, x2), H.decide_face_planes(J, c, xc))
+    srv.close()
+
+
+def test_admission_by_hbm_budget(ctx):
+    qps = [M.beam(8, 8, 16, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=s)
+           for s in range(4)]
+    one = M.lib().mprgp_problem_bytes(qps[0].nv, qps[0].nnzb, len(qps[0].planes), 3)
+    srv = M.Server(ctx, hbm_budget=int(2.5 * one), quantum_phases=64, power_launches=64)
+    tickets = [srv.submit(i, q, opts_for(q)) for i, q in enumerate(qps)]
+    max_running, finished = 0, 0
+    for _ in range(100000):
+        running, queued, completed = srv.step()
+        budget, used, scenes = srv.info()
+        assert used <= budget and scenes <= 2
+        max_running = max(max_running, running)
+        for t in list(tickets):
+            state, x, face, st, _ = srv.result(t)
+            if state == 2:
+                assert st.code == 0
+                tickets.remove(t)
+                finished += 1
+        if finished == len(qps):
+            break
+    assert finished == len(qps) and max_running <= 2
+    srv.close()
