@@ -49,8 +49,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c1", choices=sorted(WORKLOADS) + ["c2"])
-    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--config", default="c4", choices=sorted(WORKLOADS) + ["c2", "c4"])
+    ap.add_argument("--form", default=None, choices=["plain", "mixed"],
+                    help="plain FP64 or mixed precision (default: mixed for c2/c4, plain else)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -215,6 +216,7 @@ def run_gb300(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     times, stats = [], []
+    launches0, _ = ctx.counters()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -223,6 +225,7 @@ def run_gb300(args):
             stats.append(st)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+    launches = ctx.counters()[0] - launches0
     if world > 1:
         torch.distributed.barrier()
     total_ms = sum(times)
@@ -264,7 +267,7 @@ def run_gb300(args):
                      "traffic": traffic,
                      "bytes_per_launch": alg_bytes, "launch_ms": round(dev_ms, 4),
                      "bytes_rule": "per matrix pass: nnzb*(9*s_A+4) + (nv+1)*4 + n*8 + n*8"},
-        "gpu_launches": args.steps,
+        "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "wall_s_timed": round(wall, 3),
     }
@@ -457,12 +460,265 @@ def run_batch(args):
         print(json.dumps(line))
 
 
+SERVE_COUNT = 128          # requests per window (one step)
+SERVE_SEED = 7
+SERVE_RATE = 5000.0        # headline arrival rate, req/s (saturates the server)
+SERVE_SWEEP = (100.0, 1000.0, 5000.0)
+SERVE_CPU_SAMPLE = 32      # new-scene requests per reference-arm step
+
+
+def serve_desc(win):
+    nvs = [r.qp.nv for r in win.reqs if not r.followup]
+    nf = sum(r.followup for r in win.reqs)
+    return (f"serving stream window of {len(win.reqs)} requests, Poisson arrivals: {len(nvs)} new "
+            f"beams log-uniform 4x4x4..32x32x64 cubes ({min(nvs)}..{max(nvs)} vertices, "
+            f"{3 * sum(nvs)} DOF total; floor + 0-2 walls, 1-3 planes per vertex; "
+            f"v0 ~ N(0, 0.2^2)) and {nf} follow-up timesteps of live scenes (warm start, "
+            f"A/x/active set resident); tol 1e-8*||b|| each")
+
+
+def serve_sample(win, count):
+    """The first `count` new-scene requests of the window (CPU sample)."""
+    return [r.qp for r in win.reqs if not r.followup][:count]
+
+
+def cpu_solve_many(qps, threads):
+    """Solves independent QPs on `threads` host threads with the CPU
+    restatement of the reference (one single-threaded solve per thread)."""
+    from concurrent.futures import ThreadPoolExecutor
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers as H
+    H.oracle().oracle_set_threads(1)
+    prepared = [H.qp_from_beam(q) + (q.x0,) for q in qps]
+
+    def one(args):
+        A, b, J, c, x0 = args
+        tol = REL_TOL * float(np.linalg.norm(b))
+        x, face, st, _ = H.oracle_solve("general", A, b, x0, J, c, tol=tol, max_it=20000,
+                                        seed=SEED)
+        return st
+
+    t = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        sts = list(ex.map(one, prepared))
+    return time.perf_counter() - t, sts
+
+
+def run_serve(args):
+    """configs c4: a window of the serving stream through the continuous-
+    batching server (mixed form by default), against the plain FP64 GPU solve
+    one request at a time on the same stream."""
+    import torch
+    import mprgp_gb300 as M
+    from mprgp_gb300 import workloads as W
+    from mprgp_gb300.stream import StreamPlayer
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    M.build()
+    win = W.serving_window(SERVE_COUNT, SERVE_SEED)
+    ctx = M.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def flush():
+        flush_buf.fill_(1.0)
+
+    mixed = args.form != "plain"
+    prec = M.PREC_MIXED if mixed else M.PREC_FP64
+    pl = StreamPlayer(ctx, win, rel_tol=REL_TOL, seed=SEED)
+    served = dict(max_slots=128, quantum=256, power_launches=256)
+    plain = dict(max_slots=1, quantum=-1, power_launches=1003)
+
+    def check(res, what):
+        bad = [(i, c) for i, c in enumerate(res.codes) if c != 0]
+        if bad:
+            raise RuntimeError(f"{what}: {len(bad)} requests did not converge: {bad[:4]}")
+        return res
+
+    # warm-up 1 records the follow-up right-hand sides (host-copy submission)
+    check(pl.play(SERVE_RATE, prec, mode="host", **served), "record")
+    pl.stage()
+    for _ in range(max(0, args.warmup - 1)):
+        check(pl.play(SERVE_RATE, prec, "device", flush=flush, stream=stream, **served), "warm-up")
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    timed = []
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            timed.append(check(pl.play(SERVE_RATE, prec, "device", flush=flush, stream=stream,
+                                       keep_x=(k == 0), **served), "served"))
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    total_ms = sum(r.event_ms for r in timed)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    n_req = len(win.reqs)
+    value = world * n_req * args.steps / (total_ms / 1e3)
+    lat = np.concatenate([r.latency_s for r in timed]) * 1e3
+    # plain FP64, one request at a time, same stream and arrivals
+    base = check(pl.play(SERVE_RATE, M.PREC_FP64, "device", flush=flush, stream=stream,
+                         keep_x=True, **plain), "plain FP64")
+    # error of every served result against the plain FP64 GPU solve of the same QP
+    errs, same_face = [], 0
+    for i in range(n_req):
+        xs, xp = timed[0].xs[i], base.xs[i]
+        errs.append(float(np.linalg.norm(xs - xp) / max(np.linalg.norm(xp), 1e-300)))
+        same_face += int(np.array_equal(timed[0].faces[i], base.faces[i]))
+    # arrival-rate sweep (one window each)
+    sweep = []
+    for rate in SERVE_SWEEP:
+        a = check(pl.play(rate, prec, "device", flush=flush, stream=stream, **served), "sweep")
+        b = check(pl.play(rate, M.PREC_FP64, "device", flush=flush, stream=stream, **plain),
+                  "sweep plain")
+        sweep.append({"rate_hz": rate,
+                      "served": {"solves_per_s": round(a.solves_per_s, 2),
+                                 "p50_ms": round(float(np.percentile(a.latency_s, 50)) * 1e3, 3),
+                                 "p99_ms": round(float(np.percentile(a.latency_s, 99)) * 1e3, 3)},
+                      "plain_fp64": {"solves_per_s": round(b.solves_per_s, 2),
+                                     "p50_ms": round(float(np.percentile(b.latency_s, 50)) * 1e3, 3),
+                                     "p99_ms": round(float(np.percentile(b.latency_s, 99)) * 1e3, 3)}})
+    # roofline of the solver kernels over the timed plays
+    scene = {r.scene: r.qp for r in win.reqs if not r.followup}
+    alg = 0
+    for res in timed:
+        for i, st in enumerate(res.stats):
+            q = scene[win.reqs[i].scene]
+            alg += st.spmv_fp64 * spmv_bytes(q, 8) + st.spmv_fp32 * spmv_bytes(q, 4)
+    solver_ms = sum(r.solver_ms for r in timed)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (solver_ms / 1e3) / 1e9
+    launches = sum(r.launches for r in timed)
+    its = [st.iterations for st in timed[0].stats]
+    line = {
+        "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
+        "value": round(value, 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 A (f32 accumulate) + f64 steps/projection/residual" if mixed else "f64",
+        "data": "synthetic (seeded beam QPs, no dataset)",
+        "config": {"workload": serve_desc(win), "config": "c4",
+                   "form": "served-" + ("mixed" if mixed else "fp64"),
+                   "arrival_rate_hz": SERVE_RATE,
+                   "server": {"slots": served["max_slots"], "quantum_phases": served["quantum"],
+                              "power_loop_per_step": served["power_launches"]},
+                   "inputs": "staged in device memory before the timed region (e2e: pinned host)",
+                   "l2": "flushed before every window (256 MB device write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
+                       "p99": round(float(np.percentile(lat, 99)), 3)},
+        "plain_fp64_one_at_a_time": {
+            "value": round(base.solves_per_s, 3), "unit": "solves/s",
+            "p50_ms": round(float(np.percentile(base.latency_s, 50)) * 1e3, 3),
+            "p99_ms": round(float(np.percentile(base.latency_s, 99)) * 1e3, 3),
+            "speedup_of_value": round(value / world / base.solves_per_s, 2)},
+        "error_vs_fp64": {"max_rel_x": float(max(errs)), "median_rel_x": float(np.median(errs)),
+                          "identical_active_sets": same_face, "of": n_req},
+        "sweep": sweep,
+        "solve": {"iterations_max": int(max(its)), "iterations_mean": round(float(np.mean(its)), 1)},
+        "roofline": {"bound": "hbm", "kernel": "mprgp::engine_kernel + mprgp::power_kernel",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": committed_traffic("c4", "mixed" if mixed else "plain"),
+                     "bytes_per_launch": int(alg / max(1, launches)),
+                     "launch_ms": round(solver_ms / max(1, launches), 5),
+                     "bytes_rule": "per matrix pass: nnzb*(9*s_A+4) + (nv+1)*4 + n*8 + n*8"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if not args.no_e2e:
+        check(pl.play(SERVE_RATE, prec, "pinned", flush=flush, stream=stream, **served), "e2e warm-up")
+        e2e = [check(pl.play(SERVE_RATE, prec, "pinned", flush=flush, stream=stream, **served), "e2e")
+               for _ in range(args.steps)]
+        ems = sum(r.event_ms for r in e2e)
+        elat = np.concatenate([r.latency_s for r in e2e]) * 1e3
+        line["e2e"] = {"value": round(world * n_req * args.steps / (ems / 1e3), 3), "unit": "solves/s",
+                       "h2d_bytes_per_step": int(e2e[0].h2d_bytes),
+                       "d2h_bytes_per_step": int(e2e[0].d2h_bytes),
+                       "p50_ms": round(float(np.percentile(elat, 50)), 3),
+                       "p99_ms": round(float(np.percentile(elat, 99)), 3),
+                       "path": "mprgp_server_submit (C ABI) by reference to pinned host buffers, "
+                               "copied at admission; x and face read back at completion"}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        qs, spent, sts = [], 0.0, []
+        for q in serve_sample(win, SERVE_CPU_SAMPLE):
+            dt, st = cpu_solve_many([q], 1)
+            spent += dt
+            qs.append(q)
+            if spent > 15.0:
+                break
+        line["cpu_baseline"] = {
+            "value": round(len(qs) / spent, 4), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": f"the first {len(qs)} new-scene requests of the window, solved one after "
+                      f"another by the CPU restatement of the reference MPRGP (oracle/), "
+                      f"single-threaded; {spent:.1f} s"}
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_reference_serve(args):
+    """Reference arm of c4: the CPU restatement of the reference MPRGP solving
+    a bounded sample of the stream's requests on every host core (independent
+    requests, one single-threaded solve per core)."""
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    import mprgp_gb300 as M
+    from mprgp_gb300 import workloads as W
+    M.build()
+    win = W.serving_window(SERVE_COUNT, SERVE_SEED)
+    sample = serve_sample(win, SERVE_CPU_SAMPLE)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_solve_many(sample, threads)
+    times, last = [], None
+    for _ in range(args.steps):
+        dt, last = cpu_solve_many(sample, threads)
+        times.append(dt)
+    total = sum(times)
+    v = len(sample) * args.steps / total
+    line = {
+        "impl": "reference",
+        "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
+        "value": round(v, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded beam QPs, no dataset)",
+        "config": {"workload": serve_desc(win), "config": "c4", "form": "reference-cpu"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: the first {len(sample)} new-scene requests of the "
+                                   f"window, solved concurrently on {threads} host threads by the "
+                                   f"CPU restatement of the reference MPRGP (oracle/), one "
+                                   f"single-threaded solve per thread"},
+        "e2e": {"value": round(v, 4), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "solve": {"converged": sum(int(s["code"]) == 0 for s in last), "of": len(last)},
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.form is None:
+        args.form = "mixed" if args.config in ("c2", "c4") else "plain"
     if args.impl == "reference":
-        run_reference(args)
+        if args.config == "c4":
+            run_reference_serve(args)
+        else:
+            run_reference(args)
     elif args.config == "c2":
         run_batch(args)
+    elif args.config == "c4":
+        run_serve(args)
     else:
         run_gb300(args)
 

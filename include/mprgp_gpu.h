@@ -111,12 +111,18 @@ void *mprgp_context_stream(mprgp_context *ctx); /* the cudaStream_t it launches 
 int mprgp_context_sync(mprgp_context *ctx);
 /* SM count and resident engine CTAs per SM (the persistent grid's shape). */
 int mprgp_context_info(mprgp_context *ctx, int *nsm, int *blocks_per_sm);
+/* Counters since the context was created: kernels launched (engine runs,
+ * setup kernels and every iteration of the power-method graph loop) and the
+ * device time of the solver runs (power loop + engine), in milliseconds. */
+int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solver_ms);
 /* Launch shape of later solves on this context (chosen by the autotuner,
  * mprgp_gb300/autotune.py): bit 0 of stage = 1 brings each item's FP32
  * matrix slice into shared memory with bulk async copies (one CTA per SM),
  * 0 reads it from global memory; bit 1 of stage = 1 runs the power method in
- * the persistent engine instead of the dedicated power kernel; ctas_per_sm
- * caps the persistent grid (0 = every resident CTA). */
+ * the persistent engine instead of the dedicated power kernel; bit 2 = 1
+ * issues the power kernel's launches from the host stream instead of a
+ * CUDA-graph WHILE loop; ctas_per_sm caps the persistent grid (0 = every
+ * resident CTA). */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
 
 /* ---- problem: one QP instance resident in device memory ----------------- */
@@ -196,10 +202,15 @@ int mprgp_solve_batch(mprgp_context *ctx, int count, mprgp_problem *const *probs
 /* ---- serving: continuous batching of QP requests ------------------------- */
 /* No counterpart in the reference API (its FEM driver solves one QP per frame,
  * MprgpFemSolver.cpp:521-533); this is the serving form of the solver.
- * A request is a new scene (host BSR A, b, planes, x0 -- copied at submit;
- * project_x0 applies) or, with row_ptr == NULL, the next timestep of a live
- * scene: only b is new, and A, the planes, x (the last solution) and the face
- * stay resident on the device and warm-start the solve.  Each step admits
+ * A request is a new scene (BSR A, b, planes, x0; project_x0 applies) or,
+ * with row_ptr == NULL, the next timestep of a live scene: only b is new, and
+ * A, the planes, x (the last solution) and the face stay resident on the
+ * device and warm-start the solve.  mode 0: the arrays are host memory,
+ * copied at submit (num_planes may be -1: plane_ptr[nv] is used); mode 1:
+ * device memory and mode 2: host memory (pinned memory is copied by DMA),
+ * both read at admission, so the caller keeps them unchanged until the
+ * request has completed; mode 1 needs num_planes = plane_ptr[nv].  Each step
+ * admits
  * queued requests into free slots while their device footprint fits the HBM
  * budget (idle scenes are evicted least-recently-used first), advances all
  * admitted requests together by one engine quantum and retires the finished
@@ -208,8 +219,9 @@ int mprgp_solve_batch(mprgp_context *ctx, int count, mprgp_problem *const *probs
 typedef struct mprgp_server_config {
   size_t hbm_budget;  /* device bytes for resident scenes (0 = 80% of free) */
   int max_slots;      /* requests in flight (0 = 64) */
-  int quantum_phases; /* engine macro-phases per step (0 = 256) */
-  int power_launches; /* power-kernel launches per step (0..1003) */
+  int quantum_phases; /* engine macro-phases per step (0 = 256, < 0 = run
+                         every admitted request to completion in one step) */
+  int power_launches; /* power-method loop iterations per step (0..1003) */
   int pad;
 } mprgp_server_config;
 typedef struct mprgp_server mprgp_server;
@@ -218,8 +230,12 @@ int mprgp_server_destroy(mprgp_server *srv);
 int mprgp_server_submit(mprgp_server *srv, int scene, int nv, int nnzb, const int *row_ptr,
                         const int *cols, const double *vals, const double *b,
                         const int *plane_ptr, const double *planes, const double *x0,
-                        const mprgp_options *opt, long long *ticket);
+                        int num_planes, int mode, const mprgp_options *opt,
+                        long long *ticket);
 int mprgp_server_step(mprgp_server *srv, int *running, int *queued, int *completed);
+/* Tickets that completed since the last poll (at most `capacity`, oldest
+ * first); *count receives how many were written. */
+int mprgp_server_poll(mprgp_server *srv, long long *tickets, int capacity, int *count);
 /* state: 0 queued, 1 running, 2 done.  When done, copies x (3 nv), face and
  * stats, times = {submit, admit, done} in seconds, releases the ticket and
  * returns the solve's code. */

@@ -107,8 +107,10 @@ def _sig(lib):
     s("mprgp_server_create", C.c_int, _P, C.POINTER(ServerConfig), C.POINTER(_P))
     s("mprgp_server_destroy", C.c_int, _P)
     s("mprgp_server_submit", C.c_int, _P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P,
-      C.POINTER(Options), C.POINTER(C.c_longlong))
+      C.c_int, C.c_int, C.POINTER(Options), C.POINTER(C.c_longlong))
     s("mprgp_server_step", C.c_int, _P, _IP, _IP, _IP)
+    s("mprgp_server_poll", C.c_int, _P, C.POINTER(C.c_longlong), C.c_int, _IP)
+    s("mprgp_context_counters", C.c_int, _P, C.POINTER(C.c_longlong), C.POINTER(C.c_double))
     s("mprgp_server_result", C.c_int, _P, C.c_longlong, _P, _P, C.POINTER(Stats), _P, _IP)
     s("mprgp_server_info", C.c_int, _P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), _IP)
     s("mprgp_beam_default", None, C.POINTER(BeamParams))
@@ -152,12 +154,19 @@ def _ptr(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
 
+def _set_fields(struct, kw):
+    names = {f[0] for f in type(struct)._fields_}
+    for k, v in kw.items():
+        if k not in names:
+            raise TypeError(f"{type(struct).__name__} has no field {k!r}")
+        setattr(struct, k, v)
+    return struct
+
+
 def default_options(**kw) -> Options:
     o = Options()
     lib().mprgp_default_options(C.byref(o))
-    for k, v in kw.items():
-        setattr(o, k, v)
-    return o
+    return _set_fields(o, kw)
 
 
 # ----------------------------------------------------------------- beams --
@@ -188,8 +197,7 @@ def beam(a: int, b: int, c: int, **kw) -> BeamQP:
     p = BeamParams()
     L.mprgp_beam_default(C.byref(p))
     p.a, p.b, p.c = a, b, c
-    for k, v in kw.items():
-        setattr(p, k, v)
+    _set_fields(p, kw)
     nv, nnzb, npl = C.c_int(), C.c_int(), C.c_int()
     _check(L.mprgp_beam_sizes(C.byref(p), C.byref(nv), C.byref(nnzb), C.byref(npl)), "beam_sizes")
     nv, nnzb, npl = nv.value, nnzb.value, npl.value
@@ -223,6 +231,12 @@ class Context:
 
     def sync(self):
         _check(lib().mprgp_context_sync(self.h), "sync")
+
+    def counters(self):
+        """(kernels launched, device ms of solver runs) since creation."""
+        n, ms = C.c_longlong(), C.c_double()
+        _check(lib().mprgp_context_counters(self.h, C.byref(n), C.byref(ms)), "context_counters")
+        return n.value, ms.value
 
     def set_tuning(self, stage: int = 0, ctas_per_sm: int = 0):
         _check(lib().mprgp_context_set_tuning(self.h, stage, ctas_per_sm), "set_tuning")
@@ -386,19 +400,49 @@ class Server:
             pass
 
     def submit(self, scene: int, qp: BeamQP, opt: Options, b=None, followup=False) -> int:
+        """Host-memory request: a new scene (qp) or, with followup=True, the
+        next timestep of `scene` with right-hand side b."""
         t = C.c_longlong()
         rhs = np.ascontiguousarray(qp.b if b is None else b, np.float64)
         if followup:
             _check(lib().mprgp_server_submit(self.h, scene, qp.nv, 0, None, None, None, _ptr(rhs),
-                                             None, None, None, C.byref(opt), C.byref(t)),
+                                             None, None, None, -1, 0, C.byref(opt), C.byref(t)),
                    "server_submit")
         else:
             _check(lib().mprgp_server_submit(self.h, scene, qp.nv, qp.nnzb, _ptr(qp.row_ptr),
                                              _ptr(qp.cols), _ptr(qp.vals), _ptr(rhs),
                                              _ptr(qp.plane_ptr), _ptr(qp.planes), _ptr(qp.x0),
-                                             C.byref(opt), C.byref(t)), "server_submit")
+                                             len(qp.planes), 0, C.byref(opt), C.byref(t)),
+                   "server_submit")
         self.nv[t.value] = (qp.nv, len(qp.planes))
         return t.value
+
+    def submit_ref(self, scene: int, nv: int, nnzb: int, m: int, opt: Options, b: int,
+                   row_ptr=0, cols=0, vals=0, plane_ptr=0, planes=0, x0=0,
+                   on_device=True) -> int:
+        """By-reference request from raw pointers (device memory, or host
+        memory with on_device=False) that the caller keeps valid until the
+        request completes; row_ptr == 0 makes it a follow-up of `scene`."""
+        t = C.c_longlong()
+        P = C.c_void_p
+        mode = 1 if on_device else 2
+        if not row_ptr:
+            _check(lib().mprgp_server_submit(self.h, scene, nv, 0, None, None, None, P(b), None,
+                                             None, None, m, mode, C.byref(opt), C.byref(t)),
+                   "server_submit")
+        else:
+            _check(lib().mprgp_server_submit(self.h, scene, nv, nnzb, P(row_ptr), P(cols),
+                                             P(vals), P(b), P(plane_ptr), P(planes), P(x0), m,
+                                             mode, C.byref(opt), C.byref(t)), "server_submit")
+        self.nv[t.value] = (nv, m)
+        return t.value
+
+    def poll(self, capacity=4096):
+        """Tickets completed since the last poll."""
+        arr = (C.c_longlong * capacity)()
+        n = C.c_int()
+        _check(lib().mprgp_server_poll(self.h, arr, capacity, C.byref(n)), "server_poll")
+        return [arr[i] for i in range(n.value)]
 
     def step(self):
         r, q, c = C.c_int(), C.c_int(), C.c_int()

@@ -11,7 +11,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -21,7 +23,11 @@
 
 namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
-cudaError_t launch_power(const EngineArgs &args, cudaStream_t stream);
+cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, cudaGraph_t *graph,
+                              cudaGraphExec_t *exec);
+cudaError_t power_max_blocks_per_sm(int *n);
+cudaError_t launch_power_direct(int grid, int launches, const EngineArgs *d_args, PowCtl *d_pc,
+                                cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,
@@ -41,9 +47,18 @@ struct mprgp_context {
   int nsm = 0, bps = 0, bps_stage = 0;
   int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
+  int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
   int ctas_per_sm = 0;   // persistent CTAs per SM (0 = all resident)
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  mprgp_problem *scratch = nullptr;  // reused by mprgp_solve_bsr
+  cudaMemPool_t pool = nullptr;      // every device array of the context's problems
+  mprgp_problem *scratch = nullptr;
+  // power-method graphs (one per grid size) and their device-side inputs
+  int bps_power = 0;
+  EngineArgs *d_args = nullptr;
+  PowCtl *d_pc = nullptr;
+  std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> power_graphs;
+  long long launches = 0;  // kernels launched (each power-loop iteration counts)
+  double solver_ms = 0.0;  // device time of engine runs (power loop + engine)  // reused by mprgp_solve_bsr
   // per-launch arrays (grown on demand)
   InstDesc *d_desc = nullptr;
   int *d_prefix = nullptr;
@@ -76,6 +91,7 @@ struct mprgp_problem {
   double *stage_vals = nullptr;
   size_t stage_nnzb = 0;
   std::vector<int> h_plane_ptr;
+  int phase_host = 0;  // the instance's phase at the end of its last engine run
 };
 
 namespace {
@@ -98,27 +114,31 @@ int cuda_fail(cudaError_t e, const char *what) {
     if (_e != cudaSuccess) return cuda_fail(_e, #call); \
   } while (0)
 
+// Device memory comes from the context's stream-ordered pool: allocations
+// and frees are ordered on the context stream and freed blocks stay reserved
+// for the next problem, so admitting and evicting problems in a serving loop
+// neither calls cudaMalloc nor synchronises the device (cudaFree would).
 template <typename T>
-int dalloc(T **p, size_t count) {
+int dalloc(mprgp_context *c, T **p, size_t count) {
   *p = nullptr;
   if (count == 0) return MPRGP_OK;
-  CK(cudaMalloc((void **)p, count * sizeof(T)));
+  CK(cudaMallocFromPoolAsync((void **)p, count * sizeof(T), c->pool, c->stream));
   return MPRGP_OK;
 }
 template <typename T>
-void dfree(T *&p) {
-  if (p) cudaFree((void *)p);
+void dfree(mprgp_context *c, T *&p) {
+  if (p) cudaFreeAsync((void *)p, c->stream);
   p = nullptr;
 }
 
 int nitems_of(int nv) { return (nv + kThreads - 1) / kThreads; }
 
 void free_problem_arrays(mprgp_problem *p) {
-  dfree(p->slice_off); dfree(p->cols); dfree(p->v64); dfree(p->v32);
-  dfree(p->dinv); dfree(p->b); dfree(p->plane_ptr); dfree(p->planes_raw);
-  dfree(p->planes); dfree(p->pl_nn); dfree(p->pl_indn); dfree(p->L); dfree(p->U);
-  dfree(p->face); dfree(p->vec); dfree(p->vec32); dfree(p->ev); dfree(p->part); dfree(p->cnt); dfree(p->st);
-  dfree(p->trace); dfree(p->stage_ptr); dfree(p->stage_cols); dfree(p->stage_vals);
+  dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
+  dfree(p->ctx, p->dinv); dfree(p->ctx, p->b); dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw);
+  dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
+  dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->st);
+  dfree(p->ctx, p->trace); dfree(p->ctx, p->stage_ptr); dfree(p->ctx, p->stage_cols); dfree(p->ctx, p->stage_vals);
 }
 
 int resolve_options(const mprgp_problem *p, const mprgp_options *o, int *kind, int *alg,
@@ -169,6 +189,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   if (!p->cols) return fail(MPRGP_INVALID, "matrix not set");
   cudaStream_t st = p->ctx->stream;
   if (p->cons == 1 && p->planes_dirty) {
+    p->ctx->launches++;
     launch_planes_setup(p->nv, p->plane_ptr, p->planes_raw, p->planes, p->pl_nn, p->pl_indn,
                         p->dinv, st);
     CK(cudaGetLastError());
@@ -244,14 +265,35 @@ void fill_stats(const InstState &s, double ms, mprgp_stats *out) {
   out->device_ms = ms;
 }
 
+// Grid of the power kernel over `items` items: every resident CTA, or the
+// items rounded up to a multiple of 32 when that is fewer (few distinct sizes,
+// so few cached graph instantiations).
+int power_grid(mprgp_context *c, int items) {
+  const int cap = std::max(1, c->nsm * c->bps_power);
+  return std::min(cap, (items + 31) / 32 * 32);
+}
+
+// The instantiated power-method graph for `grid` CTAs.
+int power_graph(mprgp_context *c, int grid, cudaGraphExec_t *exec) {
+  auto it = c->power_graphs.find(grid);
+  if (it == c->power_graphs.end()) {
+    cudaGraph_t g;
+    cudaGraphExec_t e;
+    CK(build_power_graph(grid, c->d_args, c->d_pc, &g, &e));
+    it = c->power_graphs.emplace(grid, std::make_pair(g, e)).first;
+  }
+  *exec = it->second.second;
+  return MPRGP_OK;
+}
+
 int ensure_launch_arrays(mprgp_context *c, int ninst) {
   if (ninst <= c->cap_inst) return MPRGP_OK;
-  dfree(c->d_desc);
-  dfree(c->d_prefix);
+  dfree(c, c->d_desc);
+  dfree(c, c->d_prefix);
   int cap = std::max(ninst, 16);
-  int rc = dalloc(&c->d_desc, cap);
+  int rc = dalloc(c, &c->d_desc, cap);
   if (rc) return rc;
-  rc = dalloc(&c->d_prefix, cap + 1);
+  rc = dalloc(c, &c->d_prefix, cap + 1);
   if (rc) return rc;
   c->cap_inst = cap;
   return MPRGP_OK;
@@ -290,6 +332,12 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   }
   if (wait_s <= 0.0) wait_s = 5.0;
   cudaStream_t s = c->stream;
+  unsigned int in_power = 0;
+  for (int i = 0; i < n; ++i) {
+    if (fresh[i]) probs[i]->phase_host = st[i].phase;
+    const int ph = probs[i]->phase_host;
+    in_power += (ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST) ? 1u : 0u;
+  }
   for (int i = 0; i < n; ++i) {
     if (!fresh[i]) continue;
     CK(cudaMemcpyAsync(probs[i]->st, &st[i], sizeof(InstState), cudaMemcpyHostToDevice, s));
@@ -318,24 +366,47 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   int per_sm = stage ? c->bps_stage : c->bps;
   if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
   const int grid = std::max(1, std::min(prefix[n], c->nsm * per_sm));
+  // The power method first (at most 1003 phases: the seeded start, 1001
+  // iterations, the last difference), as a device-driven loop of launches of
+  // the power kernel while any instance is in a power phase; then the engine.
+  const bool power = c->power_kernel && in_power > 0 && power_launches > 0;
+  cudaGraphExec_t pexec = nullptr;
+  const int pgrid = power_grid(c, prefix[n]);
+  if (power) {
+    if (c->power_graph) {
+      rc = power_graph(c, pgrid, &pexec);
+      if (rc) return rc;
+    }
+    PowCtl pc0 = {in_power, 0u, 0u, 0u, (unsigned int)power_launches, 0u};
+    CK(cudaMemcpyAsync(c->d_pc, &pc0, sizeof(PowCtl), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(c->d_args, &args, sizeof(EngineArgs), cudaMemcpyHostToDevice, s));
+  }
   CK(cudaEventRecord(c->e0, s));
-  // The power method first, as ordinary launches (at most 1003 phases: the
-  // seeded start, 1001 iterations, the last difference); then the engine.
-  if (c->power_kernel)
-    for (int k = 0; k < power_launches; ++k) CK(launch_power(args, s));
+  if (power && pexec) CK(cudaGraphLaunch(pexec, s));
+  if (power && !pexec) CK(launch_power_direct(pgrid, power_launches, c->d_args, c->d_pc, s));
   CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(c->e1, s));
-  CK(cudaStreamSynchronize(s));
-  float ms = 0.f;
-  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  PowCtl pc1 = {0u, 0u, 0u, 0u, 0u, 0u};
+  if (power) CK(cudaMemcpyAsync(&pc1, c->d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   Ctl ctl1;
-  CK(cudaMemcpy(&ctl1, c->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&ctl1, c->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   for (int i = 0; i < n; ++i)
     CK(cudaMemcpyAsync(&st[i], probs[i]->st, sizeof(InstState), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  // every body of the power loop issues kPowerUnroll launches, the stream form
+  // all `power_launches` (those after the last working one return at once)
+  if (power && pexec)
+    c->launches += (long long)kPowerUnroll * ((pc1.launches + kPowerUnroll - 1) / kPowerUnroll);
+  else if (power)
+    c->launches += power_launches;
+  c->launches += 1;
+  c->solver_ms += ms;
   int worst = MPRGP_OK;
   for (int i = 0; i < n; ++i) {
     InstState &x = st[i];
+    probs[i]->phase_host = x.phase;
     const bool finished = x.phase == PH_DONE;
     if (ctl1.err) x.code = ctl1.err;
     else if (!finished && quantum <= 0) x.code = MPRGP_TIMEOUT;
@@ -434,8 +505,21 @@ int mprgp_context_create(int device, mprgp_context **out) {
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&c->e0));
   CK(cudaEventCreate(&c->e1));
-  CK(cudaMalloc((void **)&c->ctl, sizeof(Ctl)));
-  CK(cudaMemset(c->ctl, 0, sizeof(Ctl)));
+  cudaMemPoolProps props;
+  std::memset(&props, 0, sizeof(props));
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  CK(cudaMemPoolCreate(&c->pool, &props));
+  unsigned long long keep = ~0ULL;  // never trim: freed blocks serve the next problem
+  CK(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  CK(power_max_blocks_per_sm(&c->bps_power));
+  int rc = dalloc(c, &c->ctl, 1);
+  if (!rc) rc = dalloc(c, &c->d_args, 1);
+  if (!rc) rc = dalloc(c, &c->d_pc, 1);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   *out = c;
   return MPRGP_OK;
 }
@@ -445,12 +529,20 @@ int mprgp_context_destroy(mprgp_context *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   if (c->scratch) mprgp_problem_destroy(c->scratch);
-  dfree(c->ctl);
-  dfree(c->d_desc);
-  dfree(c->d_prefix);
+  dfree(c, c->ctl);
+  dfree(c, c->d_desc);
+  dfree(c, c->d_prefix);
+  dfree(c, c->d_args);
+  dfree(c, c->d_pc);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->power_graphs) {
+    cudaGraphExecDestroy(kv.second.second);
+    cudaGraphDestroy(kv.second.first);
+  }
   cudaEventDestroy(c->e0);
   cudaEventDestroy(c->e1);
   cudaStreamDestroy(c->stream);
+  if (c->pool) cudaMemPoolDestroy(c->pool);
   delete c;
   return MPRGP_OK;
 }
@@ -464,11 +556,19 @@ int mprgp_context_sync(mprgp_context *c) {
 }
 
 int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
-  if (!c || stage < 0 || stage > 3 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  if (!c || stage < 0 || stage > 7 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
   c->power_kernel = (stage & 2) ? 0 : 1;
+  c->power_graph = (stage & 4) ? 0 : 1;
   stage &= 1;
   c->stage = stage;
   c->ctas_per_sm = ctas_per_sm;
+  return MPRGP_OK;
+}
+
+int mprgp_context_counters(mprgp_context *c, long long *launches, double *solver_ms) {
+  if (!c) return fail(MPRGP_INVALID, "context_counters");
+  if (launches) *launches = c->launches;
+  if (solver_ms) *solver_ms = c->solver_ms;
   return MPRGP_OK;
 }
 
@@ -502,11 +602,11 @@ int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
   p->nslices = (nv + kSlice - 1) / kSlice;
   const size_t n = 3 * (size_t)nv;
   int rc = 0;
-  if ((rc = dalloc(&p->vec, n * kNumBuf)) || (rc = dalloc(&p->vec32, n * kNumBuf32)) ||
-      (rc = dalloc(&p->ev, n)) ||
-      (rc = dalloc(&p->b, n)) || (rc = dalloc(&p->dinv, n)) ||
-      (rc = dalloc(&p->part, (size_t)nitems_of(nv) * kPart)) || (rc = dalloc(&p->cnt, 1)) ||
-      (rc = dalloc(&p->st, 1)) || (rc = dalloc(&p->slice_off, p->nslices + 1))) {
+  if ((rc = dalloc(p->ctx, &p->vec, n * kNumBuf)) || (rc = dalloc(p->ctx, &p->vec32, n * kNumBuf32)) ||
+      (rc = dalloc(p->ctx, &p->ev, n)) ||
+      (rc = dalloc(p->ctx, &p->b, n)) || (rc = dalloc(p->ctx, &p->dinv, n)) ||
+      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart)) || (rc = dalloc(p->ctx, &p->cnt, 1)) ||
+      (rc = dalloc(p->ctx, &p->st, 1)) || (rc = dalloc(p->ctx, &p->slice_off, p->nslices + 1))) {
     free_problem_arrays(p);
     delete p;
     return rc;
@@ -519,8 +619,7 @@ int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
 int mprgp_problem_destroy(mprgp_problem *p) {
   if (!p) return MPRGP_OK;
   cudaSetDevice(p->ctx->device);
-  cudaStreamSynchronize(p->ctx->stream);
-  free_problem_arrays(p);
+  free_problem_arrays(p);  // stream-ordered after the problem's last use
   delete p;
   return MPRGP_OK;
 }
@@ -553,12 +652,12 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   }
   const int slots = off[p->nslices];
   if (slots != p->slots || (precisions & 1) != p->has64 || ((precisions >> 1) & 1) != p->has32) {
-    dfree(p->cols);
-    dfree(p->v64);
-    dfree(p->v32);
-    int rc = dalloc(&p->cols, (size_t)slots * kSlice);
-    if (!rc && (precisions & 1)) rc = dalloc(&p->v64, (size_t)slots * kSlice * 9);
-    if (!rc && (precisions & 2)) rc = dalloc(&p->v32, (size_t)slots * kSlice * 9);
+    dfree(p->ctx, p->cols);
+    dfree(p->ctx, p->v64);
+    dfree(p->ctx, p->v32);
+    int rc = dalloc(p->ctx, &p->cols, (size_t)slots * kSlice);
+    if (!rc && (precisions & 1)) rc = dalloc(p->ctx, &p->v64, (size_t)slots * kSlice * 9);
+    if (!rc && (precisions & 2)) rc = dalloc(p->ctx, &p->v32, (size_t)slots * kSlice * 9);
     if (rc) return rc;
     p->slots = slots;
     p->has64 = precisions & 1;
@@ -570,14 +669,14 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   const double *d_vals = vals;
   if (!on_device) {
     if (!p->stage_ptr) {
-      int rc = dalloc(&p->stage_ptr, nv + 1);
+      int rc = dalloc(p->ctx, &p->stage_ptr, nv + 1);
       if (rc) return rc;
     }
     if ((size_t)nnzb > p->stage_nnzb) {
-      dfree(p->stage_cols);
-      dfree(p->stage_vals);
-      int rc = dalloc(&p->stage_cols, nnzb);
-      if (!rc) rc = dalloc(&p->stage_vals, (size_t)nnzb * 9);
+      dfree(p->ctx, p->stage_cols);
+      dfree(p->ctx, p->stage_vals);
+      int rc = dalloc(p->ctx, &p->stage_cols, nnzb);
+      if (!rc) rc = dalloc(p->ctx, &p->stage_vals, (size_t)nnzb * 9);
       if (rc) return rc;
       p->stage_nnzb = nnzb;
     }
@@ -588,6 +687,7 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
     d_cols = p->stage_cols;
     d_vals = p->stage_vals;
   }
+  c->launches++;
   launch_bsr_to_sell(nv, d_ptr, d_cols, d_vals, p->slice_off, p->cols, p->v64, p->v32, p->dinv, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
@@ -620,14 +720,14 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
   if (m > 0 && !planes) return fail(MPRGP_INVALID, "planes");
   cudaStream_t s = p->ctx->stream;
   if (m != p->m || p->cons != 1) {
-    dfree(p->plane_ptr); dfree(p->planes_raw); dfree(p->planes); dfree(p->pl_nn);
-    dfree(p->pl_indn); dfree(p->face);
-    int rc = dalloc(&p->plane_ptr, nv + 1);
-    if (!rc) rc = dalloc(&p->planes_raw, 4 * (size_t)std::max(m, 1));
-    if (!rc) rc = dalloc(&p->planes, 4 * (size_t)std::max(m, 1));
-    if (!rc) rc = dalloc(&p->pl_nn, (size_t)std::max(m, 1));
-    if (!rc) rc = dalloc(&p->pl_indn, (size_t)std::max(m, 1));
-    if (!rc) rc = dalloc(&p->face, (size_t)std::max(m, 1));
+    dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw); dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn);
+    dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->face);
+    int rc = dalloc(p->ctx, &p->plane_ptr, nv + 1);
+    if (!rc) rc = dalloc(p->ctx, &p->planes_raw, 4 * (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(p->ctx, &p->planes, 4 * (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(p->ctx, &p->pl_nn, (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(p->ctx, &p->pl_indn, (size_t)std::max(m, 1));
+    if (!rc) rc = dalloc(p->ctx, &p->face, (size_t)std::max(m, 1));
     if (rc) return rc;
   }
   CK(cudaMemcpyAsync(p->plane_ptr, h.data(), sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
@@ -649,10 +749,10 @@ int mprgp_problem_set_bounds(mprgp_problem *p, const double *L, const double *U)
   const size_t n = 3 * (size_t)p->nv;
   cudaStream_t s = p->ctx->stream;
   if (p->cons < 2) {
-    dfree(p->face);
-    int rc = dalloc(&p->L, n);
-    if (!rc) rc = dalloc(&p->U, n);
-    if (!rc) rc = dalloc(&p->face, n);
+    dfree(p->ctx, p->face);
+    int rc = dalloc(p->ctx, &p->L, n);
+    if (!rc) rc = dalloc(p->ctx, &p->U, n);
+    if (!rc) rc = dalloc(p->ctx, &p->face, n);
     if (rc) return rc;
   }
   CK(cudaMemcpyAsync(p->L, L, sizeof(double) * n, cudaMemcpyHostToDevice, s));
@@ -720,11 +820,11 @@ int mprgp_problem_get_ev(mprgp_problem *p, double *ev, int *valid) {
 
 int mprgp_problem_set_trace(mprgp_problem *p, int capacity) {
   if (!p || capacity < 0) return fail(MPRGP_INVALID, "set_trace");
-  dfree(p->trace);
+  dfree(p->ctx, p->trace);
   p->trace_cap = 0;
   p->trace_n = 0;
   if (capacity == 0) return MPRGP_OK;
-  int rc = dalloc(&p->trace, 4 * (size_t)capacity);
+  int rc = dalloc(p->ctx, &p->trace, 4 * (size_t)capacity);
   if (rc) return rc;
   p->trace_cap = capacity;
   return MPRGP_OK;
@@ -735,8 +835,9 @@ int mprgp_problem_get_trace(mprgp_problem *p, double *out, int capacity, int *co
   const int n = std::min(p->trace_n, p->trace_cap);
   if (count) *count = n;
   if (out && n > 0) {
-    CK(cudaMemcpy(out, p->trace, sizeof(double) * 4 * std::min(n, capacity),
-                  cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(out, p->trace, sizeof(double) * 4 * std::min(n, capacity),
+                       cudaMemcpyDeviceToHost, p->ctx->stream));
+    CK(cudaStreamSynchronize(p->ctx->stream));
   }
   return MPRGP_OK;
 }
@@ -760,6 +861,7 @@ int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int
   A.cols = p->cols;
   A.v64 = p->v64;
   A.v32 = p->v32;
+  p->ctx->launches++;
   launch_spmv(A, p->nv, f32, x_dev, y_dev, p->ctx->stream);
   CK(cudaGetLastError());
   return MPRGP_OK;

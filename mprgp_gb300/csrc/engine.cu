@@ -13,6 +13,7 @@
 // vertex, so all projector work is local to a row and fuses into the SpMV
 // epilogues; only the reductions cross rows.
 #include <cfloat>
+#include <cstring>
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -1633,22 +1634,31 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kern
 }
 
 // ------------------------------------------------------- power kernel ----
-// The power-method phases as ordinary launches: one CTA per item, one launch
-// per phase, the launch boundary as the phase barrier, the same per-row work,
-// reductions and transitions as the persistent engine (hence the same
-// results).  Its small register budget keeps every SM full of warps, which
-// the latency-bound SpMV of these phases needs.
-__global__ void __launch_bounds__(kThreads, 6) power_kernel(EngineArgs args) {
-  __shared__ InstDesc sD;
-  __shared__ InstState sS;
-  __shared__ double red[kPart][kThreads / 32];
-  __shared__ double sums[kPart];
-  __shared__ int s_last;
-  const int item = blockIdx.x;
-  const int inst = find_instance(args.item_prefix, args.ninst, item);
-  if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
+// The power-method phases as ordinary launches of one kernel, the launch
+// boundary as the phase barrier: the same per-row work, reductions and
+// transitions as the persistent engine (hence the same results).  Its small
+// register budget keeps every SM full of warps, which the latency-bound SpMV
+// of these phases needs.  The launches are either the body of a CUDA-graph
+// WHILE node (kPowerUnroll launches per body) or plain stream launches.  The
+// finalize that completes the last power-phase instance of a launch decides
+// whether another launch is needed: it sets a stop flag (the launches after
+// it return at once) and, in the graph, the loop condition -- so the up to
+// 1003 dependent phases run without a host launch each and stop as soon as
+// every instance has left the power phases.
+__device__ __forceinline__ bool power_phase(int ph) {
+  return ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST;
+}
+
+__device__ __forceinline__ void power_item(const InstDesc *desc, const int *item_prefix,
+                                           int ninst, int item, PowCtl *pc,
+                                           cudaGraphConditionalHandle h, int signal,
+                                           InstDesc &sD, InstState &sS,
+                                           double (&red)[kPart][kThreads / 32],
+                                           double (&sums)[kPart], int &s_last) {
+  const int inst = find_instance(item_prefix, ninst, item);
+  __syncthreads();  // the previous item's readers of sD/sS are done
   {
-    const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
+    const int *srcd = reinterpret_cast<const int *>(desc + inst);
     int *dstd = reinterpret_cast<int *>(&sD);
     for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads) dstd[w] = ldro(srcd + w);
   }
@@ -1660,7 +1670,7 @@ __global__ void __launch_bounds__(kThreads, 6) power_kernel(EngineArgs args) {
   }
   __syncthreads();
   const int phase = sS.phase;
-  if (phase != PH_POW_RAND && phase != PH_POW && phase != PH_POW_LAST) return;
+  if (!power_phase(phase)) return;
   const int local = item - sD.item_begin;
   const int v = local * kThreads + threadIdx.x;
   double part[kPart];
@@ -1691,7 +1701,41 @@ __global__ void __launch_bounds__(kThreads, 6) power_kernel(EngineArgs args) {
     advance_power(sD, S, sums);
     *sD.st = S;
     *sD.cnt = 0u;
+    // `active` is read before this finalize is counted: only the last
+    // finalize of the launch rewrites it, after every other one was counted.
+    const unsigned int active = pc->active;
+    if (power_phase(S.phase)) atomicAdd(&pc->busy, 1u);
+    const unsigned int old = atom_add_acq_rel(&pc->fin, 1u);
+    if (old == active - 1u) {
+      const unsigned int busy = atomicAdd(&pc->busy, 0u);
+      const unsigned int launches = pc->launches + 1u;
+      const bool more = busy > 0u && launches < pc->limit;
+      pc->launches = launches;
+      pc->active = busy;
+      pc->busy = 0u;
+      pc->fin = 0u;
+      pc->stop = more ? 0u : 1u;
+      __threadfence();
+      if (signal) cudaGraphSetConditional(h, more ? 1u : 0u);
+    }
   }
+}
+
+__global__ void __launch_bounds__(kThreads, 6)
+    power_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc, cudaGraphConditionalHandle h,
+                 int signal) {
+  __shared__ InstDesc sD;
+  __shared__ InstState sS;
+  __shared__ double red[kPart][kThreads / 32];
+  __shared__ double sums[kPart];
+  __shared__ int s_last;
+  if (*(volatile unsigned int *)&pc->stop) return;  // written by an earlier launch
+  if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
+  const InstDesc *desc = pargs->desc;
+  const int *item_prefix = pargs->item_prefix;
+  const int ninst = pargs->ninst, total = pargs->total_items;
+  for (int item = blockIdx.x; item < total; item += gridDim.x)
+    power_item(desc, item_prefix, ninst, item, pc, h, signal, sD, sS, red, sums, s_last);
 }
 
 // ------------------------------------------------------ setup kernels -----
@@ -1783,9 +1827,65 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, engine_kernel, kThreads, stage_bytes);
 }
-cudaError_t launch_power(const EngineArgs &args, cudaStream_t stream) {
-  power_kernel<<<args.total_items, kThreads, 0, stream>>>(args);
-  return cudaGetLastError();
+// A graph whose WHILE node runs power_kernel over `grid` CTAs until no
+// instance is left in a power phase or PowCtl::limit launches have run.  The
+// kernel reads its EngineArgs and PowCtl from device memory, so one
+// instantiation serves every later run with the same grid.
+cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, cudaGraph_t *graph,
+                              cudaGraphExec_t *exec) {
+  *graph = nullptr;
+  *exec = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cond;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&cond, g, nullptr, nullptr, 0, &cp);
+  if (e == cudaSuccess) {
+    int signal = 1;
+    void *kargs[] = {(void *)&d_args, (void *)&d_pc, (void *)&h, (void *)&signal};
+    cudaKernelNodeParams kp;
+    memset(&kp, 0, sizeof(kp));
+    kp.func = (void *)power_kernel;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(kThreads);
+    kp.kernelParams = kargs;
+    cudaGraphNode_t prev = nullptr;
+    for (int u = 0; u < kPowerUnroll && e == cudaSuccess; ++u) {
+      cudaGraphNode_t kn;
+      e = cudaGraphAddKernelNode(&kn, cp.conditional.phGraph_out[0], prev ? &prev : nullptr,
+                                 prev ? 1 : 0, &kp);
+      prev = kn;
+    }
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    *exec = nullptr;
+    return e;
+  }
+  *graph = g;
+  return cudaSuccess;
+}
+// The same loop as plain stream launches (`launches` of them; those after the
+// last working one return at once).
+cudaError_t launch_power_direct(int grid, int launches, const EngineArgs *d_args, PowCtl *d_pc,
+                                cudaStream_t stream) {
+  for (int k = 0; k < launches; ++k) {
+    power_kernel<<<grid, kThreads, 0, stream>>>(d_args, d_pc, cudaGraphConditionalHandle(0), 0);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+cudaError_t power_max_blocks_per_sm(int *n) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel, kThreads, 0);
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,

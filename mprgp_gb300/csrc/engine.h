@@ -121,6 +121,17 @@ struct Ctl {
   int pad;
 };
 
+// Loop control of the power-method graph (see power_kernel).
+struct PowCtl {
+  unsigned int active;    // instances in a power phase when the current launch began
+  unsigned int fin;       // of those, finalized in the current launch
+  unsigned int busy;      // of those, still in a power phase after their finalize
+  unsigned int launches;  // launches that did work so far
+  unsigned int limit;     // stop after this many launches
+  unsigned int stop;      // set when the loop is over: later launches return at once
+};
+constexpr int kPowerUnroll = 8;  // power launches per evaluation of the loop condition
+
 struct EngineArgs {
   const InstDesc *desc;
   const int *item_prefix;  // ninst + 1

@@ -34,9 +34,14 @@ struct Request {
   long long ticket = 0;
   int scene = 0;
   bool followup = false;
-  int nv = 0, nnzb = 0;
+  int nv = 0, nnzb = 0, m = 0;
   std::vector<int> row_ptr, cols, plane_ptr;
   std::vector<double> vals, b, planes, x0;
+  // by-reference submission (mode 1 device, 2 host): the caller's arrays,
+  // read at admission; mode 0 keeps the copies above
+  int mode = 0;
+  const int *p_row_ptr = nullptr, *p_cols = nullptr, *p_plane_ptr = nullptr;
+  const double *p_vals = nullptr, *p_b = nullptr, *p_planes = nullptr, *p_x0 = nullptr;
   mprgp_options opt{};
   int state = 0;  // 0 queued, 1 running, 2 done
   int code = 0;
@@ -77,6 +82,7 @@ struct mprgp_server {
   std::map<int, Scene> scenes;
   std::vector<long long> running;
   std::vector<char> fresh_flag;  // parallel to running
+  std::deque<long long> completed;  // finished, not yet polled
 };
 
 namespace {
@@ -105,23 +111,32 @@ int admit(mprgp_server *s, Request &r) {
   if (r.followup) {
     auto it = s->scenes.find(r.scene);
     Scene &sc = it->second;
-    int rc = mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
+    int rc = r.mode ? mprgp_problem_set_rhs(sc.prob, r.p_b, r.mode == 1)
+                    : mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
     if (rc) return rc;
     sc.busy = true;
     sc.last_use = ++s->clock;
     return MPRGP_OK;
   }
   const int prec = r.opt.precision == MPRGP_PREC_MIXED ? 3 : 1;
-  const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, (int)(r.planes.size() / 4), prec);
+  const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, r.m, prec);
   auto old = s->scenes.find(r.scene);
   if (old != s->scenes.end() && !old->second.busy) release_scene(s, old);
   Scene sc;
   int rc = mprgp_problem_create(s->ctx, r.nv, &sc.prob);
-  if (!rc) rc = mprgp_problem_set_matrix(sc.prob, r.nnzb, r.row_ptr.data(), r.cols.data(),
-                                         r.vals.data(), prec, 0);
-  if (!rc) rc = mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
-  if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.plane_ptr.data(), r.planes.data(), 0);
-  if (!rc) rc = mprgp_problem_set_x(sc.prob, r.x0.data(), 0);
+  if (r.mode) {
+    const int dev = r.mode == 1;
+    if (!rc) rc = mprgp_problem_set_matrix(sc.prob, r.nnzb, r.p_row_ptr, r.p_cols, r.p_vals, prec, dev);
+    if (!rc) rc = mprgp_problem_set_rhs(sc.prob, r.p_b, dev);
+    if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.p_plane_ptr, r.p_planes, dev);
+    if (!rc) rc = mprgp_problem_set_x(sc.prob, r.p_x0, dev);
+  } else {
+    if (!rc) rc = mprgp_problem_set_matrix(sc.prob, r.nnzb, r.row_ptr.data(), r.cols.data(),
+                                           r.vals.data(), prec, 0);
+    if (!rc) rc = mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
+    if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.plane_ptr.data(), r.planes.data(), 0);
+    if (!rc) rc = mprgp_problem_set_x(sc.prob, r.x0.data(), 0);
+  }
   if (rc) {
     if (sc.prob) mprgp_problem_destroy(sc.prob);
     return rc;
@@ -129,7 +144,7 @@ int admit(mprgp_server *s, Request &r) {
   sc.bytes = bytes;
   sc.busy = true;
   sc.last_use = ++s->clock;
-  sc.m = (int)(r.planes.size() / 4);
+  sc.m = r.m;
   s->used += bytes;
   s->scenes[r.scene] = sc;
   // host copies are no longer needed
@@ -152,6 +167,7 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
   s->budget = (cfg && cfg->hbm_budget) ? cfg->hbm_budget : (size_t)(0.8 * (double)fr);
   if (cfg && cfg->max_slots > 0) s->max_slots = cfg->max_slots;
   if (cfg && cfg->quantum_phases > 0) s->quantum = cfg->quantum_phases;
+  if (cfg && cfg->quantum_phases < 0) s->quantum = 0;  // each step runs to completion
   if (cfg && cfg->power_launches >= 0) s->power_launches = std::min(cfg->power_launches, 1003);
   *out = s;
   return MPRGP_OK;
@@ -167,36 +183,56 @@ int mprgp_server_destroy(mprgp_server *s) {
 int mprgp_server_submit(mprgp_server *s, int scene, int nv, int nnzb, const int *row_ptr,
                         const int *cols, const double *vals, const double *b,
                         const int *plane_ptr, const double *planes, const double *x0,
-                        const mprgp_options *opt, long long *ticket) {
+                        int num_planes, int mode, const mprgp_options *opt,
+                        long long *ticket) {
   if (!s || !opt || !ticket || nv <= 0 || !b) return err(MPRGP_INVALID, "server_submit");
   if (opt->kind != MPRGP_KIND_DECOUPLED && opt->kind != MPRGP_KIND_PLANES)
     return err(MPRGP_INVALID, "server_submit: plane kinds only");
   Request r;
-  r.ticket = s->next_ticket++;
   r.scene = scene;
   r.opt = *opt;
   r.nv = nv;
+  if (mode < 0 || mode > 2) return err(MPRGP_INVALID, "server_submit: mode");
+  r.mode = mode;
   const size_t n = 3 * (size_t)nv;
-  r.b.assign(b, b + n);
+  if (r.mode) r.p_b = b;
+  else r.b.assign(b, b + n);
   if (row_ptr == nullptr) {  // follow-up timestep of a live scene
     auto it = s->scenes.find(scene);
     if (it == s->scenes.end()) return err(MPRGP_INVALID, "server_submit: scene not resident");
     r.followup = true;
     r.opt.project_x0 = 0;  // x is the scene's last solution (feasible)
-    r.face.assign(std::max(it->second.m, 1), 0);
+    r.m = it->second.m;
   } else {
     if (!cols || !vals || !plane_ptr || !x0 || nnzb <= 0)
       return err(MPRGP_INVALID, "server_submit: missing arrays");
     r.nnzb = nnzb;
-    r.row_ptr.assign(row_ptr, row_ptr + nv + 1);
-    r.cols.assign(cols, cols + nnzb);
-    r.vals.assign(vals, vals + 9 * (size_t)nnzb);
-    r.plane_ptr.assign(plane_ptr, plane_ptr + nv + 1);
-    const int m = plane_ptr[nv];
-    r.planes.assign(planes, planes + 4 * (size_t)m);
-    r.x0.assign(x0, x0 + n);
-    r.face.assign(std::max(m, 1), 0);
+    if (r.mode == 1) {
+      if (num_planes < 0) return err(MPRGP_INVALID, "server_submit: num_planes");
+      r.m = num_planes;
+    } else {
+      r.m = plane_ptr[nv];
+      if (num_planes >= 0 && num_planes != r.m)
+        return err(MPRGP_INVALID, "server_submit: num_planes != plane_ptr[nv]");
+    }
+    if (r.mode) {
+      r.p_row_ptr = row_ptr;
+      r.p_cols = cols;
+      r.p_vals = vals;
+      r.p_plane_ptr = plane_ptr;
+      r.p_planes = planes;
+      r.p_x0 = x0;
+    } else {
+      r.row_ptr.assign(row_ptr, row_ptr + nv + 1);
+      r.cols.assign(cols, cols + nnzb);
+      r.vals.assign(vals, vals + 9 * (size_t)nnzb);
+      r.plane_ptr.assign(plane_ptr, plane_ptr + nv + 1);
+      r.planes.assign(planes, planes + 4 * (size_t)r.m);
+      r.x0.assign(x0, x0 + n);
+    }
   }
+  r.face.assign(std::max(r.m, 1), 0);
+  r.ticket = s->next_ticket++;
   r.x.assign(n, 0.0);
   r.t_submit = now_s();
   *ticket = r.ticket;
@@ -217,13 +253,14 @@ int mprgp_server_step(mprgp_server *s, int *running, int *queued, int *completed
       if (sc == s->scenes.end()) {  // evicted meanwhile: cannot warm start
         r.state = 2;
         r.code = MPRGP_INVALID;
+        s->completed.push_back(r.ticket);
         it = s->queue.erase(it);
         continue;
       }
       ok = !sc->second.busy;
     } else {
       const int prec = r.opt.precision == MPRGP_PREC_MIXED ? 3 : 1;
-      const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, (int)(r.planes.size() / 4), prec);
+      const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, r.m, prec);
       auto sc = s->scenes.find(r.scene);
       ok = (sc == s->scenes.end() || !sc->second.busy) && make_room(s, bytes);
     }
@@ -235,6 +272,7 @@ int mprgp_server_step(mprgp_server *s, int *running, int *queued, int *completed
     if (rc) {
       r.state = 2;
       r.code = rc;
+      s->completed.push_back(r.ticket);
       it = s->queue.erase(it);
       continue;
     }
@@ -277,6 +315,7 @@ int mprgp_server_step(mprgp_server *s, int *running, int *queued, int *completed
       sc.busy = false;
       r.state = 2;
       r.t_done = now_s();
+      s->completed.push_back(r.ticket);
       ++ncomp;
     }
     s->running.swap(still);
@@ -307,6 +346,18 @@ int mprgp_server_result(mprgp_server *s, long long ticket, double *x, unsigned c
   const int code = r.code;
   s->reqs.erase(it);
   return code;
+}
+
+int mprgp_server_poll(mprgp_server *s, long long *tickets, int capacity, int *count) {
+  if (!s || !count || capacity < 0 || (capacity > 0 && !tickets))
+    return err(MPRGP_INVALID, "server_poll");
+  int k = 0;
+  while (k < capacity && !s->completed.empty()) {
+    tickets[k++] = s->completed.front();
+    s->completed.pop_front();
+  }
+  *count = k;
+  return MPRGP_OK;
 }
 
 int mprgp_server_info(mprgp_server *s, size_t *budget, size_t *used, int *scenes) {

@@ -5,7 +5,8 @@
                     (up to 3 planes per vertex); v0 ~ N(0, 0.2^2).
   serving_stream()  Poisson arrivals of beams log-uniform from 4x4x4 to
                     32x32x64 with 1-3 planes per vertex, 30 % of them
-                    follow-up timesteps of a live scene (warm start).
+                    follow-up timesteps of a live scene (warm start);
+  serving_window()  the same stream cut to a fixed number of requests.
 Every instance is solved to ||g_P|| <= 1e-8 ||b||.
 """
 from __future__ import annotations
@@ -64,6 +65,39 @@ class Request:
     scene: int              # scene id (follow-ups refer to a live scene)
     followup: bool = False
     extra: dict = field(default_factory=dict)
+
+
+@dataclass
+class Window:
+    """A fixed window of the serving stream: requests in arrival order and
+    their arrival times at unit rate (divide by the rate for seconds)."""
+    reqs: list
+    t_unit: np.ndarray
+
+    def arrivals(self, rate_hz: float) -> np.ndarray:
+        return self.t_unit / rate_hz
+
+
+def serving_window(count=128, seed=7, followup_frac=0.3, lo=(4, 4, 4), hi=(32, 32, 64),
+                   v0_sigma=0.2) -> Window:
+    """`count` requests of the serving stream with Poisson arrival gaps: beams
+    log-uniform from lo to hi cubes, floor plus 0-2 walls (1-3 planes per
+    vertex), 30 % follow-up timesteps of an earlier scene of the window."""
+    rng = np.random.default_rng(seed)
+    t, reqs, times, scenes = 0.0, [], [], 0
+    while len(reqs) < count:
+        t += rng.exponential(1.0)
+        times.append(t)
+        if scenes > 0 and rng.uniform() < followup_frac:
+            reqs.append(Request(t, None, int(rng.integers(0, scenes)), followup=True))
+            continue
+        dims = tuple(log_uniform_int(rng, l, h) for l, h in zip(lo, hi))
+        extra = int(rng.integers(0, 3))
+        qp = beam(*dims, extra_planes_max=extra, extra_planes_min=extra, plane_mode=2,
+                  v0_sigma=v0_sigma, seed=int(rng.integers(1, 2**31)))
+        reqs.append(Request(t, qp, scenes, extra={"dims": dims, "walls": extra}))
+        scenes += 1
+    return Window(reqs, np.asarray(times))
 
 
 def serving_stream(rate_hz: float, duration_s: float, seed=7, followup_frac=0.3,
