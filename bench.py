@@ -54,6 +54,10 @@ def parse():
                     help="plain FP64 or mixed precision (default: mixed for c2/c4, plain else)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="c4: skip the arrival-rate sweep")
+    ap.add_argument("--tuning", type=int, default=None,
+                    help="launch-form bits for mprgp_context_set_tuning (bit 2: power loop from "
+                         "host-stream launches instead of the CUDA-graph WHILE loop)")
     return ap.parse_args()
 
 
@@ -189,11 +193,14 @@ def run_gb300(args):
     qp = workload_qp(args.config)
     tol = REL_TOL * float(np.linalg.norm(qp.b))
     ctx = M.Context(local)
+    if args.tuning is not None:
+        ctx.set_tuning(args.tuning, 0)
     mixed = args.form == "mixed"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
     opt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=1, seed=SEED,
                             precision=prec)
     prob = M.load_beam(ctx, qp, precisions=3 if mixed else 1)
+    prob.set_power_cache(False)  # every timed solve runs its power method
     x0_dev = torch.from_numpy(qp.x0).cuda()
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
@@ -373,9 +380,12 @@ def run_batch(args):
     M.build()
     qps = W.batch()
     ctx = M.Context(local)
+    if args.tuning is not None:
+        ctx.set_tuning(args.tuning, 0)
     probs, opts64, optsmx, x0s = [], [], [], []
     for qp in qps:
         pr = M.load_beam(ctx, qp, precisions=3)
+        pr.set_power_cache(False)  # every timed solve runs its power method
         probs.append(pr)
         tol = REL_TOL * float(np.linalg.norm(qp.b))
         kind = M.KIND_PLANES
@@ -460,7 +470,7 @@ def run_batch(args):
         print(json.dumps(line))
 
 
-SERVE_COUNT = 128          # requests per window (one step)
+SERVE_COUNT = 512          # requests per window (one step)
 SERVE_SEED = 7
 SERVE_RATE = 5000.0        # headline arrival rate, req/s (saturates the server)
 SERVE_SWEEP = (100.0, 1000.0, 5000.0)
@@ -520,6 +530,8 @@ def run_serve(args):
     M.build()
     win = W.serving_window(SERVE_COUNT, SERVE_SEED)
     ctx = M.Context(local)
+    if args.tuning is not None:
+        ctx.set_tuning(args.tuning, 0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -529,7 +541,7 @@ def run_serve(args):
     mixed = args.form != "plain"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
     pl = StreamPlayer(ctx, win, rel_tol=REL_TOL, seed=SEED)
-    served = dict(max_slots=128, quantum=256, power_launches=256)
+    served = dict(max_slots=512, quantum=512, power_launches=1003, cluster_quantum=0)
     plain = dict(max_slots=1, quantum=-1, power_launches=1003)
 
     def check(res, what):
@@ -573,7 +585,7 @@ def run_serve(args):
         same_face += int(np.array_equal(timed[0].faces[i], base.faces[i]))
     # arrival-rate sweep (one window each)
     sweep = []
-    for rate in SERVE_SWEEP:
+    for rate in (() if args.no_sweep else SERVE_SWEEP):
         a = check(pl.play(rate, prec, "device", flush=flush, stream=stream, **served), "sweep")
         b = check(pl.play(rate, M.PREC_FP64, "device", flush=flush, stream=stream, **plain),
                   "sweep plain")
@@ -607,7 +619,8 @@ def run_serve(args):
                    "form": "served-" + ("mixed" if mixed else "fp64"),
                    "arrival_rate_hz": SERVE_RATE,
                    "server": {"slots": served["max_slots"], "quantum_phases": served["quantum"],
-                              "power_loop_per_step": served["power_launches"]},
+                              "power_loop_per_step": served["power_launches"],
+                              "small_instances": "cluster solver, to completion within a step"},
                    "inputs": "staged in device memory before the timed region (e2e: pinned host)",
                    "l2": "flushed before every window (256 MB device write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},

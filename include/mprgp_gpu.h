@@ -124,6 +124,14 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * CUDA-graph WHILE loop; ctas_per_sm caps the persistent grid (0 = every
  * resident CTA). */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
+/* Small instances -- up to `cluster` items of 256 vertices -- are solved by
+ * one thread-block cluster each, one CTA per item (state in shared memory,
+ * reductions through distributed shared memory, cluster barriers between
+ * phases), grouped by cluster size (1, 2, 4, 8, 16) and run concurrently; the
+ * others by the persistent engine.  `cluster` is the largest cluster size (a
+ * power of two, 16 by default where the device allows it); 0 sends every
+ * instance to the engine. */
+int mprgp_context_set_cluster(mprgp_context *ctx, int cluster);
 
 /* ---- problem: one QP instance resident in device memory ----------------- */
 /* Replaces the reference's FixedSparseMatrix<T> + projector objects
@@ -146,6 +154,14 @@ int mprgp_problem_get_x(mprgp_problem *prob, double *x, int on_device);
  * (planes, in plane_ptr order) or one per unknown (bounds). */
 int mprgp_problem_num_constraints(mprgp_problem *prob, int *m);
 int mprgp_problem_get_face(mprgp_problem *prob, unsigned char *face);
+/* Power-method reuse (on by default): a solve whose power method starts from
+ * the seeded random vector (no stored start vector in use) reuses the result
+ * of the problem's last such power method when A, the seed and the precision
+ * form are unchanged -- the power method is a deterministic function of
+ * those, so alpha_bar, and with it the solve, are bitwise the same; the
+ * skipped matrix passes do not appear in the stats.  set_matrix invalidates
+ * it; enable = 0 turns it off (every solve runs the power method). */
+int mprgp_problem_set_power_cache(mprgp_problem *prob, int enable);
 int mprgp_problem_set_ev(mprgp_problem *prob, const double *ev);
 int mprgp_problem_get_ev(mprgp_problem *prob, double *ev, int *valid);
 /* Device-resident solve: x (set_x) is solved in place.  Mirrors
@@ -222,7 +238,8 @@ typedef struct mprgp_server_config {
   int quantum_phases; /* engine macro-phases per step (0 = 256, < 0 = run
                          every admitted request to completion in one step) */
   int power_launches; /* power-method loop iterations per step (0..1003) */
-  int pad;
+  int cluster_quantum; /* phases per step of the small instances (cluster
+                          solver; 0 = run them to completion in the step) */
 } mprgp_server_config;
 typedef struct mprgp_server mprgp_server;
 int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out);

@@ -45,7 +45,7 @@ class Stats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_slots", C.c_int), ("quantum_phases", C.c_int),
-                ("power_launches", C.c_int), ("pad", C.c_int)]
+                ("power_launches", C.c_int), ("cluster_quantum", C.c_int)]
 
 
 class BeamParams(C.Structure):
@@ -81,6 +81,7 @@ def _sig(lib):
     s("mprgp_context_sync", C.c_int, _P)
     s("mprgp_context_info", C.c_int, _P, _IP, _IP)
     s("mprgp_context_set_tuning", C.c_int, _P, C.c_int, C.c_int)
+    s("mprgp_context_set_cluster", C.c_int, _P, C.c_int)
     s("mprgp_problem_create", C.c_int, _P, C.c_int, C.POINTER(_P))
     s("mprgp_problem_destroy", C.c_int, _P)
     s("mprgp_problem_set_matrix", C.c_int, _P, C.c_int, _P, _P, _P, C.c_int, C.c_int)
@@ -92,6 +93,7 @@ def _sig(lib):
     s("mprgp_problem_num_constraints", C.c_int, _P, _IP)
     s("mprgp_problem_get_face", C.c_int, _P, _P)
     s("mprgp_problem_set_ev", C.c_int, _P, _P)
+    s("mprgp_problem_set_power_cache", C.c_int, _P, C.c_int)
     s("mprgp_problem_get_ev", C.c_int, _P, _P, _IP)
     s("mprgp_problem_solve", C.c_int, _P, C.POINTER(Options), C.POINTER(Stats))
     s("mprgp_problem_spmv", C.c_int, _P, _P, _P, C.c_int)
@@ -238,6 +240,10 @@ class Context:
         _check(lib().mprgp_context_counters(self.h, C.byref(n), C.byref(ms)), "context_counters")
         return n.value, ms.value
 
+    def set_cluster(self, cluster: int = 8):
+        """CTAs per cluster of the small-instance solver (0 = engine only)."""
+        _check(lib().mprgp_context_set_cluster(self.h, cluster), "set_cluster")
+
     def set_tuning(self, stage: int = 0, ctas_per_sm: int = 0):
         _check(lib().mprgp_context_set_tuning(self.h, stage, ctas_per_sm), "set_tuning")
 
@@ -339,6 +345,9 @@ class Problem:
         _check(lib().mprgp_problem_get_face(self.h, _ptr(f)), "get_face")
         return f[:m.value]
 
+    def set_power_cache(self, enable: bool):
+        _check(lib().mprgp_problem_set_power_cache(self.h, int(bool(enable))), "set_power_cache")
+
     def set_ev(self, ev):
         _check(lib().mprgp_problem_set_ev(self.h, _ptr(ev)), "set_ev")
 
@@ -381,9 +390,9 @@ class Server:
     """Continuous-batching QP server (mprgp_server_*)."""
 
     def __init__(self, ctx: Context, hbm_budget=0, max_slots=0, quantum_phases=0,
-                 power_launches=256):
+                 power_launches=256, cluster_quantum=0):
         self.ctx = ctx
-        cfg = ServerConfig(hbm_budget, max_slots, quantum_phases, power_launches, 0)
+        cfg = ServerConfig(hbm_budget, max_slots, quantum_phases, power_launches, cluster_quantum)
         self.h = C.c_void_p()
         _check(lib().mprgp_server_create(ctx.h, C.byref(cfg), C.byref(self.h)), "server_create")
         self.nv = {}

@@ -26,6 +26,8 @@ cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream)
 cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, cudaGraph_t *graph,
                               cudaGraphExec_t *exec);
 cudaError_t power_max_blocks_per_sm(int *n);
+cudaError_t launch_cluster(const ClusterArgs &args, int csize, cudaStream_t stream);
+cudaError_t cluster_max_active(int csize, int *n);
 cudaError_t launch_power_direct(int grid, int launches, const EngineArgs *d_args, PowCtl *d_pc,
                                 cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
@@ -48,6 +50,10 @@ struct mprgp_context {
   int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
   int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
+  int cluster = 16;      // largest cluster of the small-instance solver (0 = off)
+  int cluster_ok[kClusterClasses] = {0, 0, 0, 0, 0};  // cluster sizes 1, 2, 4, 8, 16 usable
+  cudaStream_t side[kClusterClasses] = {};  // one per cluster size (run concurrently)
+  cudaEvent_t fork_ev = nullptr, join_ev[kClusterClasses] = {};
   int ctas_per_sm = 0;   // persistent CTAs per SM (0 = all resident)
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaMemPool_t pool = nullptr;      // every device array of the context's problems
@@ -92,6 +98,19 @@ struct mprgp_problem {
   size_t stage_nnzb = 0;
   std::vector<int> h_plane_ptr;
   int phase_host = 0;  // the instance's phase at the end of its last engine run
+  // Result of the last power method that started from the seeded random
+  // vector.  That power method is a deterministic function of (A, seed,
+  // precision form), so a later solve with the same three and the same start
+  // reuses it and gets a bitwise identical alpha_bar (a timestep re-solve of
+  // a resident scene keeps A and the seed).
+  struct {
+    int valid = 0, prec = 0, power_iters = 0;
+    unsigned long long seed = 0, gen = 0;
+    double spec_rad = 0.0;
+  } pcache;
+  int pcache_on = 1;
+  unsigned long long matrix_gen = 0;  // bumped by every set_matrix
+  int run_random = 0, run_cached = 0;  // how the current solve's power method starts
 };
 
 namespace {
@@ -265,6 +284,17 @@ void fill_stats(const InstState &s, double ms, mprgp_stats *out) {
   out->device_ms = ms;
 }
 
+// Cluster-size class (log2 of the cluster size) of an instance of `items`
+// items on the cluster solver, or -1 for the persistent engine.
+int cluster_class(const mprgp_context *c, int items) {
+  for (int q = 0; q < kClusterClasses; ++q) {
+    const int cs = 1 << q;
+    if (cs > c->cluster) break;
+    if (c->cluster_ok[q] && items <= cs * kClusterItems) return q;
+  }
+  return -1;
+}
+
 // Grid of the power kernel over `items` items: every resident CTA, or the
 // items rounded up to a multiple of 32 when that is fewer (few distinct sizes,
 // so few cached graph instantiations).
@@ -305,24 +335,55 @@ namespace mprgp {
 
 // One engine run over `n` problems.  Instances with fresh[i] != 0 start a
 // solve (their initial state is uploaded); the others resume from the state
-// left in device memory by the previous run.  The run advances everything by
-// at most `quantum` engine macro-phases (0: until all are done) after up to
-// `power_launches` launches of the power kernel.  done[i] reports instances
-// that finished (or failed); stats are filled for every instance.
+// left in device memory by the previous run.  The run advances the large
+// instances by at most `quantum` engine macro-phases (0: until all are done)
+// after up to `power_launches` launches of the power kernel, and the small
+// ones (cluster solver) by at most `cluster_quantum` phases (0: until done).
+// done[i] reports instances that finished (or failed); stats are filled for
+// every instance.
 int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
-               const int *fresh, int quantum, int power_launches, mprgp_stats *stats, int *done) {
+               const int *fresh, int quantum, int power_launches, int cluster_quantum,
+               mprgp_stats *stats, int *done) {
   int rc = ensure_launch_arrays(c, n);
   if (rc) return rc;
+  // Small instances run on the cluster solver, one cluster each, grouped by
+  // cluster size (the smallest usable size that gives every CTA its items);
+  // the others on the power loop and the persistent engine.  The desc array
+  // holds the large instances first, then each cluster-size class.
+  std::vector<int> pos(n), cls(n);
+  int n_large = 0, class_n[kClusterClasses] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    mprgp_problem *p = probs[i];
+    if (!p || p->ctx != c) return fail(MPRGP_INVALID, "problem/context mismatch");
+    cls[i] = cluster_class(c, nitems_of(p->nv));
+    if (cls[i] < 0) pos[i] = n_large++;
+    else class_n[cls[i]]++;
+  }
+  int class_off[kClusterClasses];
+  {
+    int k = n_large;
+    for (int q = 0; q < kClusterClasses; ++q) {
+      class_off[q] = k;
+      k += class_n[q];
+    }
+    int fill[kClusterClasses];
+    for (int q = 0; q < kClusterClasses; ++q) fill[q] = class_off[q];
+    for (int i = 0; i < n; ++i)
+      if (cls[i] >= 0) pos[i] = fill[cls[i]]++;
+  }
+  const int n_small = n - n_large;
   std::vector<InstDesc> desc(n);
   std::vector<InstState> st(n);
-  std::vector<int> prefix(n + 1, 0);
+  std::vector<int> prefix(n_large + 1, 0);
+  for (int i = 0; i < n; ++i)
+    if (pos[i] < n_large) prefix[pos[i] + 1] = nitems_of(probs[i]->nv);
+  for (int j = 0; j < n_large; ++j) prefix[j + 1] += prefix[j];
   double wait_s = 0.0;
   long long phase_bound = 0;
   for (int i = 0; i < n; ++i) {
     mprgp_problem *p = probs[i];
-    if (!p || p->ctx != c) return fail(MPRGP_INVALID, "problem/context mismatch");
-    prefix[i + 1] = prefix[i] + nitems_of(p->nv);
-    rc = prepare(p, &opts[i], prefix[i], &desc[i], &st[i]);
+    const int j = pos[i];
+    rc = prepare(p, &opts[i], j < n_large ? prefix[j] : 0, &desc[j], &st[i]);
     if (rc) return rc;
     wait_s = std::max(wait_s, opts[i].wait_limit_s);
     // Each MPRGP iteration takes at most 4 phases (CG: spmv, candidate,
@@ -332,29 +393,50 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   }
   if (wait_s <= 0.0) wait_s = 5.0;
   cudaStream_t s = c->stream;
-  unsigned int in_power = 0;
-  for (int i = 0; i < n; ++i) {
+  for (int i = 0; i < n; ++i)
     if (fresh[i]) probs[i]->phase_host = st[i].phase;
-    const int ph = probs[i]->phase_host;
-    in_power += (ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST) ? 1u : 0u;
+  for (int i = 0; i < n; ++i) {
+    if (!fresh[i]) continue;
+    mprgp_problem *p = probs[i];
+    InstState &S = st[i];
+    const InstDesc &D = desc[pos[i]];
+    p->run_random = S.phase == PH_POW_RAND;
+    p->run_cached = 0;
+    if (p->run_random && p->pcache_on && p->pcache.valid && p->pcache.seed == opts[i].seed &&
+        p->pcache.prec == D.prec && p->pcache.gen == p->matrix_gen) {
+      // the state advance_power leaves when the power method ends
+      S.spec_rad = p->pcache.spec_rad;
+      S.power_iters = p->pcache.power_iters;
+      S.alpha_bar = 2.0 / S.spec_rad;
+      S.ev_upd = 0;  // the vector it would store is the one already stored
+      S.phase = D.project_x0 ? PH_PROJ0 : PH_INIT;
+      p->run_cached = 1;
+      p->phase_host = S.phase;
+    }
   }
   for (int i = 0; i < n; ++i) {
     if (!fresh[i]) continue;
     CK(cudaMemcpyAsync(probs[i]->st, &st[i], sizeof(InstState), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(probs[i]->cnt, 0, sizeof(unsigned int), s));
   }
+  unsigned int in_power = 0;  // large instances in a power phase
+  for (int i = 0; i < n; ++i) {
+    const int ph = probs[i]->phase_host;
+    if (pos[i] < n_large)
+      in_power += (ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST) ? 1u : 0u;
+  }
   CK(cudaMemcpyAsync(c->d_desc, desc.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(c->d_prefix, prefix.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->d_prefix, prefix.data(), sizeof(int) * (n_large + 1), cudaMemcpyHostToDevice, s));
   Ctl ctl0;
   std::memset(&ctl0, 0, sizeof(ctl0));
-  ctl0.active = n;
-  ctl0.snap[0] = ctl0.snap[1] = n;
+  ctl0.active = n_large;
+  ctl0.snap[0] = ctl0.snap[1] = n_large;
   CK(cudaMemcpyAsync(c->ctl, &ctl0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   EngineArgs args;
   args.desc = c->d_desc;
   args.item_prefix = c->d_prefix;
-  args.ninst = n;
-  args.total_items = prefix[n];
+  args.ninst = n_large;
+  args.total_items = prefix[n_large];
   long long maxp = phase_bound;
   if (quantum > 0) maxp = std::min<long long>(maxp, quantum);
   args.max_phases = (int)std::min<long long>(maxp, INT_MAX);
@@ -365,13 +447,14 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   args.ctl = c->ctl;
   int per_sm = stage ? c->bps_stage : c->bps;
   if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
-  const int grid = std::max(1, std::min(prefix[n], c->nsm * per_sm));
+  const int grid = std::max(1, std::min(prefix[n_large], c->nsm * per_sm));
+
   // The power method first (at most 1003 phases: the seeded start, 1001
   // iterations, the last difference), as a device-driven loop of launches of
   // the power kernel while any instance is in a power phase; then the engine.
   const bool power = c->power_kernel && in_power > 0 && power_launches > 0;
   cudaGraphExec_t pexec = nullptr;
-  const int pgrid = power_grid(c, prefix[n]);
+  const int pgrid = power_grid(c, prefix[n_large]);
   if (power) {
     if (c->power_graph) {
       rc = power_graph(c, pgrid, &pexec);
@@ -382,9 +465,27 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
     CK(cudaMemcpyAsync(c->d_args, &args, sizeof(EngineArgs), cudaMemcpyHostToDevice, s));
   }
   CK(cudaEventRecord(c->e0, s));
+  // The cluster-size classes run on side streams, concurrently with each
+  // other and with the power loop; the engine (a cooperative launch, whose
+  // CTAs must all be resident) starts once they are done.
+  if (n_small > 0) CK(cudaEventRecord(c->fork_ev, s));
+  for (int q = 0; q < kClusterClasses; ++q) {
+    if (!class_n[q]) continue;
+    ClusterArgs cargs;
+    cargs.desc = c->d_desc + class_off[q];
+    cargs.ninst = class_n[q];
+    cargs.max_phases = (int)std::min<long long>(
+        cluster_quantum > 0 ? std::min<long long>(phase_bound, cluster_quantum) : phase_bound,
+        INT_MAX);
+    CK(cudaStreamWaitEvent(c->side[q], c->fork_ev, 0));
+    CK(launch_cluster(cargs, 1 << q, c->side[q]));
+    CK(cudaEventRecord(c->join_ev[q], c->side[q]));
+  }
   if (power && pexec) CK(cudaGraphLaunch(pexec, s));
   if (power && !pexec) CK(launch_power_direct(pgrid, power_launches, c->d_args, c->d_pc, s));
-  CK(launch_engine(args, grid, s));
+  for (int q = 0; q < kClusterClasses; ++q)
+    if (class_n[q]) CK(cudaStreamWaitEvent(s, c->join_ev[q], 0));
+  if (n_large > 0) CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(c->e1, s));
   PowCtl pc1 = {0u, 0u, 0u, 0u, 0u, 0u};
   if (power) CK(cudaMemcpyAsync(&pc1, c->d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
@@ -401,21 +502,36 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
     c->launches += (long long)kPowerUnroll * ((pc1.launches + kPowerUnroll - 1) / kPowerUnroll);
   else if (power)
     c->launches += power_launches;
-  c->launches += 1;
+  for (int q = 0; q < kClusterClasses; ++q) c->launches += class_n[q] ? 1 : 0;
+  c->launches += n_large > 0 ? 1 : 0;
   c->solver_ms += ms;
   int worst = MPRGP_OK;
   for (int i = 0; i < n; ++i) {
     InstState &x = st[i];
     probs[i]->phase_host = x.phase;
     const bool finished = x.phase == PH_DONE;
-    if (ctl1.err) x.code = ctl1.err;
-    else if (!finished && quantum <= 0) x.code = MPRGP_TIMEOUT;
+    const bool large = pos[i] < n_large;
+    // an engine error concerns the engine's instances; an instance left
+    // unfinished by a run that had no phase limit hit the hard phase bound
+    const bool err = large && ctl1.err;
+    const bool unbounded = (large ? quantum : cluster_quantum) <= 0;
+    if (err) x.code = ctl1.err;
+    else if (!finished && unbounded) x.code = MPRGP_TIMEOUT;
     probs[i]->xc = x.xc;
     probs[i]->trace_n = x.trace_n;
     if (finished && x.ev_upd && x.code > MPRGP_BREAKDOWN) probs[i]->ev_valid = 1;
+    if (finished && !err && probs[i]->run_random && !probs[i]->run_cached) {
+      auto &pc = probs[i]->pcache;
+      pc.valid = 1;
+      pc.seed = opts[i].seed;
+      pc.prec = desc[pos[i]].prec;
+      pc.gen = probs[i]->matrix_gen;
+      pc.spec_rad = x.spec_rad;
+      pc.power_iters = x.power_iters;
+    }
     fill_stats(x, ms, stats ? &stats[i] : nullptr);
-    if (done) done[i] = finished || ctl1.err || (!finished && quantum <= 0);
-    if ((finished || quantum <= 0) && x.code < worst) worst = x.code;
+    if (done) done[i] = finished || err || (!finished && unbounded);
+    if ((finished || err || unbounded) && x.code < worst) worst = x.code;
   }
   if (ctl1.err) return fail(ctl1.err, "device wait limit reached");
   return worst < MPRGP_NOT_CONVERGED ? worst : MPRGP_OK;
@@ -429,7 +545,7 @@ namespace {
 int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
                mprgp_stats *stats) {
   std::vector<int> fresh(n, 1);
-  return mprgp::engine_run(c, n, probs, opts, fresh.data(), 0, 1003, stats, nullptr);
+  return mprgp::engine_run(c, n, probs, opts, fresh.data(), 0, 1003, 0, stats, nullptr);
 }
 
 }  // namespace
@@ -514,6 +630,19 @@ int mprgp_context_create(int device, mprgp_context **out) {
   unsigned long long keep = ~0ULL;  // never trim: freed blocks serve the next problem
   CK(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   CK(power_max_blocks_per_sm(&c->bps_power));
+  {
+    int largest = 0;
+    for (int q = 0; q < kClusterClasses; ++q) {
+      int nc = 0;
+      c->cluster_ok[q] = cluster_max_active(1 << q, &nc) == cudaSuccess && nc >= 1;
+      cudaGetLastError();
+      if (c->cluster_ok[q]) largest = 1 << q;
+      CK(cudaStreamCreateWithFlags(&c->side[q], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&c->join_ev[q], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
+    c->cluster = std::min(c->cluster, largest);
+  }
   int rc = dalloc(c, &c->ctl, 1);
   if (!rc) rc = dalloc(c, &c->d_args, 1);
   if (!rc) rc = dalloc(c, &c->d_pc, 1);
@@ -535,6 +664,11 @@ int mprgp_context_destroy(mprgp_context *c) {
   dfree(c, c->d_args);
   dfree(c, c->d_pc);
   cudaStreamSynchronize(c->stream);
+  for (int q = 0; q < kClusterClasses; ++q) {
+    if (c->side[q]) cudaStreamDestroy(c->side[q]);
+    if (c->join_ev[q]) cudaEventDestroy(c->join_ev[q]);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   for (auto &kv : c->power_graphs) {
     cudaGraphExecDestroy(kv.second.second);
     cudaGraphDestroy(kv.second.first);
@@ -569,6 +703,18 @@ int mprgp_context_counters(mprgp_context *c, long long *launches, double *solver
   if (!c) return fail(MPRGP_INVALID, "context_counters");
   if (launches) *launches = c->launches;
   if (solver_ms) *solver_ms = c->solver_ms;
+  return MPRGP_OK;
+}
+
+int mprgp_context_set_cluster(mprgp_context *c, int cluster) {
+  if (!c || cluster < 0 || cluster > kClusterMax || (cluster & (cluster - 1)))
+    return fail(MPRGP_INVALID, "set_cluster: 0 or a power of two up to 16");
+  if (cluster > 0) {
+    int q = 0;
+    while ((1 << q) < cluster) ++q;
+    if (!c->cluster_ok[q]) return fail(MPRGP_INVALID, "set_cluster: size not available");
+  }
+  c->cluster = cluster;
   return MPRGP_OK;
 }
 
@@ -693,6 +839,8 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
   p->nnzb = nnzb;
   p->planes_dirty = 1;  // 1/diag(J D^-1 J^T) depends on D
+  p->matrix_gen++;      // a new A: the cached power method no longer applies
+  p->pcache.valid = 0;
   return MPRGP_OK;
 }
 
@@ -795,6 +943,13 @@ int mprgp_problem_get_face(mprgp_problem *p, unsigned char *face) {
   if (p->face_len == 0) return MPRGP_OK;
   CK(cudaMemcpyAsync(face, p->face, p->face_len, cudaMemcpyDeviceToHost, p->ctx->stream));
   CK(cudaStreamSynchronize(p->ctx->stream));
+  return MPRGP_OK;
+}
+
+int mprgp_problem_set_power_cache(mprgp_problem *p, int enable) {
+  if (!p) return fail(MPRGP_INVALID, "set_power_cache");
+  p->pcache_on = enable ? 1 : 0;
+  if (!enable) p->pcache.valid = 0;
   return MPRGP_OK;
 }
 

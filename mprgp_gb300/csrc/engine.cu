@@ -202,9 +202,9 @@ __device__ __forceinline__ void st3f(float *b, int v, const double o[3]) {
   q[2] = (float)o[2];
 }
 
-template <typename VT, typename Src>
+template <typename VT, typename Src, typename OT = double>
 __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
-                                         const Src &src, double out[3]) {
+                                         const Src &src, OT out[3]) {
   const int s = v >> 5, lane = v & 31;
   const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
   VT a0 = 0, a1 = 0, a2 = 0;
@@ -229,9 +229,9 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
       a2 = fma(m6, x0, a2); a2 = fma(m7, x1, a2); a2 = fma(m8, x2, a2);
     }
   }
-  out[0] = (double)a0;
-  out[1] = (double)a1;
-  out[2] = (double)a2;
+  out[0] = (OT)a0;
+  out[1] = (OT)a1;
+  out[2] = (OT)a2;
 }
 
 // Two products with one pass over A (both FP64).
@@ -269,9 +269,9 @@ __device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &
 
 // Same product with this item's block columns and values read from the
 // shared-memory stage.
-template <typename VT, typename Src>
+template <typename VT, typename Src, typename OT = double>
 __device__ __forceinline__ void spmv_row_staged(const SellMatrix &A, int v, const Src &src,
-                                                double out[3]) {
+                                                OT out[3]) {
   const int s = v >> 5, lane = v & 31;
   const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
   const int base = g_stage_first;
@@ -294,9 +294,9 @@ __device__ __forceinline__ void spmv_row_staged(const SellMatrix &A, int v, cons
       a2 = fma(q[192], x0, a2); a2 = fma(q[224], x1, a2); a2 = fma(q[256], x2, a2);
     }
   }
-  out[0] = (double)a0;
-  out[1] = (double)a1;
-  out[2] = (double)a2;
+  out[0] = (OT)a0;
+  out[1] = (OT)a1;
+  out[2] = (OT)a2;
 }
 
 template <typename Src64, typename Src32>
@@ -735,9 +735,70 @@ __device__ void epilogue_full(const InstDesc &D, const InstState &S, const VCons
 }
 
 // ------------------------------------------------------------- row work --
+// Mixed form of the power method: the iterate t_k and w = A t_k live only in
+// FP32 (A is FP32 in this form), products and per-row sums in FP32, the
+// block and instance sums (norms, the convergence test) in FP64.  t_k uses
+// the FP32 shadows of z (F_Z0/F_Z1), which are idle until PH_INIT.
+__device__ __forceinline__ void ld3f(const float *b, int v, float o[3]) {
+  const float *q = b + 3 * (size_t)v;
+  o[0] = q[0];
+  o[1] = q[1];
+  o[2] = q[2];
+}
+__device__ __forceinline__ void st3ff(float *b, int v, const float o[3]) {
+  float *q = b + 3 * (size_t)v;
+  q[0] = o[0];
+  q[1] = o[1];
+  q[2] = o[2];
+}
+
+__device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, int v,
+                                         double *part) {
+  const int k = S.pow_k;
+  const float sc = (float)S.pow_scale;  // 1/||w|| (tmpOut /= norm)
+  float u[3];
+  if (S.pow_src < 0) {  // the stored start vector (FP64)
+    double e[3];
+    ld3(D.ev, v, e);
+    u[0] = (float)e[0];
+    u[1] = (float)e[1];
+    u[2] = (float)e[2];
+  } else {
+    ld3f(D.buf32[S.pow_src == B_W ? F_W0 : F_W1], v, u);
+  }
+  u[0] *= sc;
+  u[1] *= sc;
+  u[2] *= sc;
+  if (S.phase == PH_POW_LAST || k >= 1) {
+    float t[3];
+    ld3f(D.buf32[F_Z0 + ((k - 1) & 1)], v, t);
+    const float d0 = u[0] - t[0], d1 = u[1] - t[1], d2 = u[2] - t[2];
+    part[0] += (double)fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+  }
+  if (S.phase == PH_POW_LAST) return;
+  st3ff(D.buf32[F_Z0 + (k & 1)], v, u);
+  float w[3];
+  if (S.pow_src < 0) {
+    spmv_row<float, SrcVtoF, float>(D.A, D.A.v32, v, SrcVtoF{D.ev}, w);
+  } else {
+    const SrcF src{D.buf32[S.pow_src == B_W ? F_W0 : F_W1]};
+    if (g_staged) spmv_row_staged<float, SrcF, float>(D.A, v, src, w);
+    else spmv_row<float, SrcF, float>(D.A, D.A.v32, v, src, w);
+  }
+  w[0] *= sc;
+  w[1] *= sc;
+  w[2] *= sc;
+  st3ff(D.buf32[(k & 1) ? F_W1 : F_W0], v, w);
+  part[1] += (double)fmaf(w[0], w[0], fmaf(w[1], w[1], w[2] * w[2]));
+}
+
 __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, int v,
                                        double *part) {
   const bool f32 = D.prec == PREC_MIXED;
+  if (f32 && S.phase != PH_POW_RAND) {
+    row_power32(D, S, v, part);
+    return;
+  }
   if (S.phase == PH_POW_RAND) {
     double t[3];
 #pragma unroll
@@ -790,7 +851,15 @@ __device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int
   // PH_INIT, PH_EXP_C, PH_PL_EXP_B: g = A x - b, then the full epilogue.
   if (S.phase == PH_INIT && S.ev_upd) {
     double t[3];
-    ld3(B(D, S.ev_src), v, t);
+    if (D.prec == PREC_MIXED) {
+      float f[3];
+      ld3f(D.buf32[F_Z0 + (S.ev_src - B_T0)], v, f);
+      t[0] = f[0];
+      t[1] = f[1];
+      t[2] = f[2];
+    } else {
+      ld3(B(D, S.ev_src), v, t);
+    }
     st3(D.ev, v, t);
   }
   double x[3], ax[3];
@@ -1738,6 +1807,115 @@ __global__ void __launch_bounds__(kThreads, 6)
     power_item(desc, item_prefix, ninst, item, pc, h, signal, sD, sS, red, sums, s_last);
 }
 
+// ---------------------------------------------------- cluster solver -----
+// One thread-block cluster per small instance.  Every CTA of the cluster
+// holds the instance's desc and state in shared memory and advances its own
+// copy of the state from the same sums, so the copies never diverge and no
+// state travels through global memory between phases.  A phase: each CTA runs
+// the per-row work of its items and reduces each item in the block (as the
+// engine does); the item partials stay in shared memory; one cluster barrier
+// (release/acquire, which also orders the phase's global vector writes); then
+// every CTA reads all item partials through distributed shared memory in item
+// order and reduces them exactly as the engine's finalize does -- so results
+// are bitwise those of the persistent engine.  The partials are double
+// buffered by phase parity, so one barrier per phase suffices.
+__device__ __forceinline__ void cluster_sync_acq_rel() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+               ::: "memory");
+}
+__device__ __forceinline__ unsigned int cluster_rank() {
+  unsigned int r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned int cluster_size() {
+  unsigned int r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned int cluster_index() {
+  unsigned int r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+// Address of `p` (this CTA's shared memory) in the shared memory of CTA `rank`.
+__device__ __forceinline__ unsigned int dsmem_addr(const void *p, unsigned int rank) {
+  const unsigned int a = (unsigned int)__cvta_generic_to_shared(p);
+  unsigned int r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ double ld_dsmem(unsigned int addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) cluster_kernel(ClusterArgs args) {
+  __shared__ InstDesc sD;
+  __shared__ InstState sS;
+  __shared__ double red[kPart][kThreads / 32];
+  __shared__ double sums[kPart];
+  __shared__ __align__(8) double cpart[2][kClusterItems][kPart];
+  const unsigned int rank = cluster_rank(), csize = cluster_size();
+  const int inst = (int)cluster_index();
+  if (inst >= args.ninst) return;  // the whole cluster leaves together
+  {
+    const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
+    int *dstd = reinterpret_cast<int *>(&sD);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads) dstd[w] = ldro(srcd + w);
+  }
+  __syncthreads();
+  {
+    const int *srcs = reinterpret_cast<const int *>(sD.st);
+    int *dsts = reinterpret_cast<int *>(&sS);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads) dsts[w] = srcs[w];
+  }
+  if (threadIdx.x == 0) {
+    g_staged = 0;
+    if (rank != 0) sD.trace = nullptr;  // CTA 0 alone records the trace
+  }
+  __syncthreads();
+  const int nitems = sD.nitems;
+  int par = 0;
+  for (int ph = 0; ph < args.max_phases && sS.phase != PH_DONE; ++ph) {
+    const int phase = sS.phase;
+    const int ns = nslots(phase);
+    const bool wmin = phase == PH_PL_SPMV;
+    int li = 0;
+    for (int item = (int)rank; item < nitems && li < kClusterItems; item += (int)csize, ++li) {
+      double part[kPart];
+#pragma unroll
+      for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+      const int v = item * kThreads + threadIdx.x;
+      if (v < sD.nv) row_op(sD, sS, v, part);
+      const double r = block_reduce(part, red, ns, wmin);
+      if (threadIdx.x < ns || (wmin && threadIdx.x == kMinSlot)) cpart[par][li][threadIdx.x] = r;
+    }
+    cluster_sync_acq_rel();
+    double acc[kPart];
+#pragma unroll
+    for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+    for (int it = threadIdx.x; it < nitems; it += kThreads) {
+      const unsigned int base = dsmem_addr(&cpart[par][it / (int)csize][0], (unsigned int)it % csize);
+#pragma unroll
+      for (int k = 0; k < kPart; ++k) {
+        if (k == kMinSlot ? !wmin : k >= ns) continue;
+        const double x = ld_dsmem(base + 8u * (unsigned int)k);
+        acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+      }
+    }
+    const double t = block_reduce(acc, red, ns, wmin);
+    if (threadIdx.x < kPart) sums[threadIdx.x] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) advance(sD, sS, sums);  // in place: no copy of the state
+    __syncthreads();
+    par ^= 1;
+  }
+  if (rank == 0 && threadIdx.x == 0) *sD.st = sS;
+  cluster_sync_acq_rel();  // no CTA leaves while another may read its partials
+}
+
 // ------------------------------------------------------ setup kernels -----
 // BSR (row_ptr, cols, 9 values per block, row-major) -> SELL-32, plus
 // D^-1 = 1/diag(A) (getDiagonal, MPRGPUtility.h:503-515).
@@ -1883,6 +2061,41 @@ cudaError_t launch_power_direct(int grid, int launches, const EngineArgs *d_args
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+cudaError_t launch_cluster(const ClusterArgs &args, int csize, cudaStream_t stream) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned int)(args.ninst * csize));
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned int)csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, cluster_kernel, args);
+}
+// Clusters of `csize` CTAs that can be resident at once (0 if none).
+cudaError_t cluster_max_active(int csize, int *n) {
+  *n = 0;
+  if (csize > 8) {
+    cudaError_t e = cudaFuncSetAttribute(cluster_kernel,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned int)csize);
+  cfg.blockDim = dim3(kThreads);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned int)csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaOccupancyMaxActiveClusters(n, cluster_kernel, &cfg);
 }
 cudaError_t power_max_blocks_per_sm(int *n) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel, kThreads, 0);

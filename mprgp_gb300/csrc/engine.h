@@ -132,6 +132,20 @@ struct PowCtl {
 };
 constexpr int kPowerUnroll = 8;  // power launches per evaluation of the loop condition
 
+// Small instances run on the cluster solver: one thread-block cluster per
+// instance, CTA r covering items r, r + cluster, ... (at most kClusterItems
+// of them); the host picks the smallest cluster size (a power of two up to
+// kClusterMax) that gives every CTA one item.
+constexpr int kClusterItems = 1;
+constexpr int kClusterMax = 16;
+constexpr int kClusterClasses = 5;  // cluster sizes 1, 2, 4, 8, 16
+
+struct ClusterArgs {
+  const InstDesc *desc;  // the small instances, one per cluster
+  int ninst;
+  int max_phases;        // quantum / hard bound on phases
+};
+
 struct EngineArgs {
   const InstDesc *desc;
   const int *item_prefix;  // ninst + 1

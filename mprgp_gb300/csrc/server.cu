@@ -6,9 +6,10 @@
 // reference's FEM driver re-solves each frame, MprgpFemSolver.cpp:521-533).
 // Each mprgp_server_step admits queued requests into free slots while their
 // device footprint fits the HBM budget (evicting idle scenes, least recently
-// used first), then advances every admitted request by one engine quantum --
-// all of them in the same launches, so their work overlaps on the device --
-// and retires the ones that finished.  A request's result does not depend on
+// used first), then advances every admitted request -- small ones on the
+// cluster solver to completion (or by cluster_quantum phases), large ones by
+// one engine quantum, all in the same run, so their work overlaps on the
+// device -- and retires the ones that finished.  A request's result does not depend on
 // what else is in flight: each instance's reductions run in a fixed order.
 #include <algorithm>
 #include <chrono>
@@ -24,7 +25,8 @@
 
 namespace mprgp {
 int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
-               const int *fresh, int quantum, int power_launches, mprgp_stats *stats, int *done);
+               const int *fresh, int quantum, int power_launches, int cluster_quantum,
+               mprgp_stats *stats, int *done);
 void set_last_error(const char *what);
 }  // namespace mprgp
 
@@ -75,7 +77,7 @@ int err(int code, const char *what) {
 struct mprgp_server {
   mprgp_context *ctx = nullptr;
   size_t budget = 0, used = 0;
-  int max_slots = 64, quantum = 256, power_launches = 256;
+  int max_slots = 64, quantum = 256, power_launches = 256, cluster_quantum = 0;
   long long next_ticket = 1, clock = 0;
   std::deque<long long> queue;
   std::map<long long, Request> reqs;
@@ -168,6 +170,7 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
   if (cfg && cfg->max_slots > 0) s->max_slots = cfg->max_slots;
   if (cfg && cfg->quantum_phases > 0) s->quantum = cfg->quantum_phases;
   if (cfg && cfg->quantum_phases < 0) s->quantum = 0;  // each step runs to completion
+  if (cfg && cfg->cluster_quantum > 0) s->cluster_quantum = cfg->cluster_quantum;
   if (cfg && cfg->power_launches >= 0) s->power_launches = std::min(cfg->power_launches, 1003);
   *out = s;
   return MPRGP_OK;
@@ -296,7 +299,8 @@ int mprgp_server_step(mprgp_server *s, int *running, int *queued, int *completed
       fresh[i] = s->fresh_flag[i];
     }
     const int rc = mprgp::engine_run(s->ctx, n, probs.data(), opts.data(), fresh.data(),
-                                     s->quantum, s->power_launches, st.data(), done.data());
+                                     s->quantum, s->power_launches, s->cluster_quantum,
+                                     st.data(), done.data());
     if (rc < MPRGP_NOT_CONVERGED) return rc;
     std::vector<long long> still;
     std::vector<char> still_fresh;

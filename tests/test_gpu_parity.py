@@ -211,6 +211,103 @@ def test_batch_equals_single(ctx):
         pr.close()
 
 
+def _solve_all(c, qps, precision):
+    out = []
+    for qp in qps:
+        tol = 1e-10 * np.linalg.norm(qp.b)
+        opt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=1, seed=SEED,
+                                precision=precision)
+        out.append(c.solve_bsr(qp, opt, qp.x0))
+    return out
+
+
+@pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
+def test_cluster_solver_equals_engine(precision):
+    """Small instances run on the thread-block-cluster solver; its results are
+    bitwise those of the persistent engine (the per-item and per-instance
+    reductions run in the same order), for every cluster size (instances of
+    1, 2, 3, 7 and 10 items of 256 vertices, the last item partial) and with
+    the largest cluster size capped so some of them go to the engine."""
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(2, 2, 3, 1, 3), (5, 5, 10, 2, 4), (6, 6, 14, 0, 7),
+                                   (8, 8, 20, 1, 11), (9, 9, 24, 1, 5)]]
+    c = M.Context(0)
+    try:
+        c.set_cluster(0)
+        ref = _solve_all(c, qps, precision)
+        tried = 0
+        for cluster in (2, 4, 8, 16):
+            try:
+                c.set_cluster(cluster)
+            except M.MPRGPError:
+                continue  # cluster size not available on this device
+            tried += 1
+            got = _solve_all(c, qps, precision)
+            for (xe, fe, se), (xc, fc, sc) in zip(ref, got):
+                assert se.code == 0 and sc.code == 0
+                assert np.array_equal(xe, xc)
+                assert np.array_equal(fe, fc)
+                assert (se.iterations, se.phases, se.power_iters) == (sc.iterations, sc.phases,
+                                                                     sc.power_iters)
+                assert se.spec_rad == sc.spec_rad and se.residual == sc.residual
+        assert tried >= 2
+    finally:
+        c.close()
+
+
+def test_batch_mixes_cluster_and_engine(ctx):
+    """One batch with instances on both paths equals the single solves."""
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(4, 4, 6, 1, 8), (16, 16, 40, 2, 9), (9, 9, 24, 0, 10)]]
+    singles = _solve_all(ctx, qps, M.PREC_MIXED)
+    probs, opts = [], []
+    for qp in qps:
+        probs.append(M.load_beam(ctx, qp, precisions=3))
+        opts.append(M.default_options(tol=1e-10 * np.linalg.norm(qp.b), max_it=20000,
+                                      kind=M.KIND_PLANES, project_x0=1, seed=SEED,
+                                      precision=M.PREC_MIXED))
+    stats = ctx.solve_batch(probs, opts)
+    for pr, st, (xs, fs, ss) in zip(probs, stats, singles):
+        assert st.code == 0
+        assert np.array_equal(pr.get_x(), xs)
+        assert st.iterations == ss.iterations
+        pr.close()
+
+
+@pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
+def test_power_cache_is_exact(ctx, precision):
+    """A re-solve of a resident problem with the same A, seed and form reuses
+    the power method's result: the solution and every reported quantity are
+    bitwise those of a solve that runs the power method again."""
+    qp = M.beam(6, 5, 12, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=12)
+    opt = M.default_options(tol=1e-10 * np.linalg.norm(qp.b), max_it=20000, kind=M.KIND_PLANES,
+                            project_x0=1, seed=SEED, precision=precision)
+    pr = M.load_beam(ctx, qp, precisions=3)
+    runs = []
+    for cache in (True, True, False):
+        pr.set_power_cache(cache)
+        pr.set_x(qp.x0)
+        st = pr.solve(opt)
+        assert st.code == 0
+        runs.append((pr.get_x(), pr.get_face(), st))
+    (x0, f0, s0), (x1, f1, s1), (x2, f2, s2) = runs
+    for x, f, st in ((x1, f1, s1), (x2, f2, s2)):
+        assert np.array_equal(x, x0) and np.array_equal(f, f0)
+        assert (st.iterations, st.power_iters, st.spec_rad, st.alpha_bar, st.residual) == \
+            (s0.iterations, s0.power_iters, s0.spec_rad, s0.alpha_bar, s0.residual)
+    # the cached run skipped the power method's matrix passes, the uncached did not
+    assert s1.spmv_fp64 + s1.spmv_fp32 < s0.spmv_fp64 + s0.spmv_fp32
+    assert s2.spmv_fp64 + s2.spmv_fp32 == s0.spmv_fp64 + s0.spmv_fp32
+    # a new A invalidates it
+    pr.set_power_cache(True)
+    pr.set_matrix(qp.row_ptr, qp.cols, qp.vals, 3)
+    pr.set_x(qp.x0)
+    s3 = pr.solve(opt)
+    assert s3.spmv_fp64 + s3.spmv_fp32 == s0.spmv_fp64 + s0.spmv_fp32
+    assert np.array_equal(pr.get_x(), x0)
+    pr.close()
+
+
 GOLDEN = sorted(__import__("glob").glob(__import__("os").path.join(
     __import__("os").path.dirname(__file__), "golden", "*.npz")))
 
