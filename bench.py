@@ -1,16 +1,24 @@
 #!/usr/bin/env python3
 """MPRGP QP solves/s on GB300 (one JSON line on rank 0).
 
-Workload (default): one implicit-Euler FEM beam QP of 32x32x128 Kuhn-tet cubes
-(140,481 vertices, 421,443 DOF, 2,031,169 3x3 blocks; E=1e5, nu=0.45,
-rho=1000, h=0.01), contact with the floor and two walls (up to 3 planes per
-vertex), solved to ||g_P|| <= 1e-8 ||b||.  Synthetic, seeded inputs.
+Default workload (--config c4): the serving stream.  A window of 512 seeded
+requests with Poisson arrivals at 5000 req/s: beams of 4x4x4..32x32x64
+Kuhn-tet cubes (E=1e5, nu=0.45, rho=1000, h=0.01) in contact with the floor
+and 0-2 walls (1-3 planes per vertex), 30 % of them follow-up timesteps of a
+live scene; every request solved to ||g_P|| <= 1e-8 ||b||.  A step is one
+window served by the continuous-batching server (mixed form):
+  value  solves/s with every request's arrays staged in device memory
+         before the timed region (the server copies them at admission);
+  e2e    the same stream submitted by reference to pinned host buffers,
+         copied host->device at admission, x and face read back;
+beside it the plain FP64 GPU solve of the same stream one request at a time,
+the error of every served result against it, an arrival-rate sweep, the
+roofline of the solver kernels and the CPU restatement (oracle/) on a
+bounded sample.
 
-A step is one full solve (power method + MPRGP) of that QP:
-  value  solves/s with A, b, planes and x0 resident in HBM (x reset per step
-         by a device copy), L2 flushed between steps;
-  e2e    the same solve through the C ABI entry mprgp_solve_bsr with pinned
-         host buffers: upload of A/b/planes/x0, solve, download of x and face.
+Other workloads: c1 (one 32x32x128 beam, 421,443 DOF; --form plain|mixed),
+c0 (4x4x16, floor), c2 (256 uneven beams in one batched run), c3 (48x48x144,
+E=1e6, nu=0.49, 20 warm-started timesteps, mixed vs FP64 per step).
 --impl reference times the CPU restatement of the reference MPRGP (oracle/)
 on the host cores instead.
 """
@@ -79,8 +87,9 @@ def workload_desc(name, qp):
 
 
 def spmv_bytes(qp, s_a):
-    """Algorithmic bytes of one y = A x: A (values + block column), row pointers, x, y."""
-    return qp.nnzb * (9 * s_a + 4) + (qp.nv + 1) * 4 + qp.n * 8 + qp.n * 8
+    """Algorithmic bytes of one y = A x at matrix precision s_a (8 or 4 bytes):
+    A (values + block column), row pointers, x and y at the same precision."""
+    return qp.nnzb * (9 * s_a + 4) + (qp.nv + 1) * 4 + 2 * qp.n * s_a
 
 
 def measured_peaks():
@@ -92,15 +101,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic(name, form):
-    """Per-launch DRAM bytes of the engine kernel from a committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "engine_traffic.json")
+def committed_traffic(name, form, kernel="engine_kernel"):
+    """Per-launch DRAM bytes (read + write) of a kernel from the committed ncu
+    summary profiles/traffic.json, keyed "<config>:<form>:<kernel>"."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    e = d.get(f"{name}:{form}")
-    return None if e is None else e
+    return d.get(f"{name}:{form}:{kernel}")
 
 
 class ClockSampler:
@@ -223,7 +232,7 @@ def run_gb300(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     times, stats = [], []
-    launches0, _ = ctx.counters()
+    launches0, solver0, power0 = ctx.counters()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -232,7 +241,8 @@ def run_gb300(args):
             stats.append(st)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    launches = ctx.counters()[0] - launches0
+    launches1, solver1, power1 = ctx.counters()
+    launches = launches1 - launches0
     if world > 1:
         torch.distributed.barrier()
     total_ms = sum(times)
@@ -245,13 +255,23 @@ def run_gb300(args):
         if s.code != 0:
             raise RuntimeError(f"solve did not converge: {s.as_dict()}")
     value = world * args.steps / (total_ms / 1e3)
-    # roofline of the engine kernel (the only kernel of a resident solve)
-    bytes64, bytes32 = spmv_bytes(qp, 8), spmv_bytes(qp, 4)
-    alg_bytes = st.spmv_fp64 * bytes64 + st.spmv_fp32 * bytes32
-    dev_ms = statistics.mean(s.device_ms for s in stats)
+    # Roofline.  The dominant kernel of a solve is the power kernel (1001 of
+    # its ~1150 matrix passes, one pass per launch of the graph loop): bytes
+    # of one matrix pass / the loop's device time per working launch.  The
+    # engine (the MPRGP phases) is reported beside it.
+    s_pow = 4 if mixed else 8
+    pass_bytes = spmv_bytes(qp, s_pow)
+    passes = sum(s.power_passes for s in stats)
+    power_ms = power1 - power0
+    pow_launch_ms = power_ms / max(1, passes)
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (dev_ms / 1e3) / 1e9
-    traffic = committed_traffic(args.config, args.form)
+    achieved = pass_bytes / (pow_launch_ms / 1e3) / 1e9
+    traffic = committed_traffic(args.config, args.form, "power_kernel")
+    eng_bytes = sum((s.spmv_fp64 - (0 if mixed else s.power_passes)) * spmv_bytes(qp, 8) +
+                    (s.spmv_fp32 - (s.power_passes if mixed else 0)) * spmv_bytes(qp, 4)
+                    for s in stats)
+    eng_ms = (solver1 - solver0) - power_ms
+    eng_achieved = eng_bytes / (eng_ms / 1e3) / 1e9 if eng_ms > 0 else None
     line = {
         "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
         "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -268,12 +288,20 @@ def run_gb300(args):
                   "prop": st.num_prop, "power_iters": st.power_iters, "active": st.active,
                   "residual": st.residual, "tol": tol, "spmv_fp64": st.spmv_fp64,
                   "spmv_fp32": st.spmv_fp32, "phases": st.phases},
-        "roofline": {"bound": "hbm", "kernel": "mprgp::engine_kernel",
+        "roofline": {"bound": "hbm", "kernel": "mprgp::power_kernel (CUDA-graph loop)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "traffic": traffic,
-                     "bytes_per_launch": alg_bytes, "launch_ms": round(dev_ms, 4),
-                     "bytes_rule": "per matrix pass: nnzb*(9*s_A+4) + (nv+1)*4 + n*8 + n*8"},
+                     "traffic": traffic, "bytes_per_launch": int(pass_bytes),
+                     "launch_ms": round(pow_launch_ms, 5), "launches": int(passes),
+                     "share_of_solve": round(power_ms / max(1e-9, solver1 - solver0), 3),
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
+        "roofline_engine": {"kernel": "mprgp::engine_kernel (MPRGP phases)",
+                            "achieved": None if eng_achieved is None else round(eng_achieved, 2),
+                            "frac": None if eng_achieved is None else round(eng_achieved / peak, 4),
+                            "bytes": int(eng_bytes), "ms": round(eng_ms, 3),
+                            "traffic": committed_traffic(args.config, args.form, "engine_kernel"),
+                            "note": "matrix-pass bytes only; the MPRGP phases also move ~8-10 "
+                                    "n-vectors per phase and are FP64-issue bound (ncu)"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "wall_s_timed": round(wall, 3),
@@ -470,6 +498,134 @@ def run_batch(args):
         print(json.dumps(line))
 
 
+def run_timesteps(args):
+    """configs c3: one 48x48x144 stiff beam (E=1e6, nu=0.49, up to 3 planes
+    per vertex) advanced W + K implicit-Euler timesteps, each a QP solve
+    warm-started from the previous x (b from the previous step's solution).
+    A step is one timestep solved in the mixed form; every timestep's result
+    is compared with the plain FP64 solve of the same QP from the same start."""
+    import torch
+    import mprgp_gb300 as M
+    from mprgp_gb300 import workloads as W
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    M.build()
+    qp = workload_qp("c3")
+    ctx = M.Context(local)
+    if args.tuning is not None:
+        ctx.set_tuning(args.tuning, 0)
+    mixed = args.form != "plain"
+    prec = M.PREC_MIXED if mixed else M.PREC_FP64
+    prob = M.load_beam(ctx, qp, precisions=3)
+    ref = M.load_beam(ctx, qp, precisions=1)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    m = np.repeat(W.lumped_mass(qp), 3)
+    dt = qp.params["dt"]
+    b, x_prev, v_prev = qp.b.copy(), qp.x0.copy(), np.zeros(qp.n)
+    x_start = qp.x0.copy()
+    records, times, stats = [], [], []
+    n0 = None
+    total = args.warmup + args.steps
+    clk = ClockSampler(local)
+    for k in range(total):
+        if k == args.warmup:
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            n0 = ctx.counters()
+            clk.__enter__()
+        tol = REL_TOL * float(np.linalg.norm(b))
+        proj = 1 if k == 0 else 0
+        opt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=proj,
+                                seed=SEED, precision=prec, use_ev=1)
+        prob.set_rhs(b)
+        if k == 0:
+            prob.set_x(x_start)
+        flush_buf.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = prob.solve(opt)
+        e1.record(stream)
+        e1.synchronize()
+        if st.code != 0:
+            raise RuntimeError(f"timestep {k} did not converge: {st.as_dict()}")
+        x = prob.get_x()
+        face = prob.get_face()
+        # the same QP in plain FP64 from the same start
+        ref.set_rhs(b)
+        ref.set_x(x_start)
+        ropt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=proj,
+                                 seed=SEED, precision=M.PREC_FP64, use_ev=1)
+        rst = ref.solve(ropt)
+        xr = ref.get_x()
+        fr = ref.get_face()
+        records.append({"step": k, "iterations": st.iterations, "fp64_iterations": rst.iterations,
+                        "rel_err_x": float(np.linalg.norm(x - xr) / np.linalg.norm(xr)),
+                        "active": int(st.active), "active_fp64": int(rst.active),
+                        "face_mismatch": int(np.count_nonzero(face != fr)),
+                        "power_iters": st.power_iters, "ms": round(e0.elapsed_time(e1), 3)})
+        if k >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+            stats.append(st)
+        b, v_prev = W.next_step_rhs(qp, b, x_prev, x, v_prev, dt)
+        x_prev = x
+        x_start = x
+    clk.__exit__(None, None, None)
+    launches = ctx.counters()[0] - n0[0]
+    total_ms = sum(times)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms / 1e3)
+    alg = sum(s.spmv_fp64 * spmv_bytes(qp, 8) + s.spmv_fp32 * spmv_bytes(qp, 4) for s in stats)
+    dev_ms = sum(s.device_ms for s in stats)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (dev_ms / 1e3) / 1e9
+    line = {
+        "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
+        "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 A (f32 accumulate) + f64 steps/projection/residual" if mixed else "f64",
+        "data": "synthetic (seeded beam QP, no dataset)",
+        "config": dict(workload_desc("c3", qp), form="timesteps-" + ("mixed" if mixed else "fp64"),
+                       timesteps=total, warm_start="x from the previous timestep, b from its solution",
+                       power_method="reused across timesteps while A and the seed are unchanged "
+                                    "(bitwise the same alpha_bar)",
+                       l2="flushed before every timestep (256 MB device write)"),
+        "latency_ms": {"p50": round(float(np.percentile(times, 50)), 3),
+                       "p99": round(float(np.percentile(times, 99)), 3)},
+        "per_timestep": records,
+        "roofline": {"bound": "hbm",
+                     "kernel": "all solver kernels (cluster_kernel, power_kernel, engine_kernel; "
+                               "no single one dominates the stream)",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": None,
+                     "bytes_per_launch": int(alg / max(1, launches)),
+                     "launch_ms": round(dev_ms / max(1, launches), 5),
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": None,
+        "cpu_baseline_note": "not run for this workload: one solve of the CPU restatement on "
+                             "1.04M DOF exceeds the bounded sample (use c1 or c4)",
+    }
+    prob.close()
+    ref.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
 SERVE_COUNT = 512          # requests per window (one step)
 SERVE_SEED = 7
 SERVE_RATE = 5000.0        # headline arrival rate, req/s (saturates the server)
@@ -635,13 +791,15 @@ def run_serve(args):
                           "identical_active_sets": same_face, "of": n_req},
         "sweep": sweep,
         "solve": {"iterations_max": int(max(its)), "iterations_mean": round(float(np.mean(its)), 1)},
-        "roofline": {"bound": "hbm", "kernel": "mprgp::engine_kernel + mprgp::power_kernel",
+        "roofline": {"bound": "hbm",
+                     "kernel": "all solver kernels (cluster_kernel, power_kernel, engine_kernel; "
+                               "no single one dominates the stream)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "traffic": committed_traffic("c4", "mixed" if mixed else "plain"),
+                     "traffic": None,
                      "bytes_per_launch": int(alg / max(1, launches)),
                      "launch_ms": round(solver_ms / max(1, launches), 5),
-                     "bytes_rule": "per matrix pass: nnzb*(9*s_A+4) + (nv+1)*4 + n*8 + n*8"},
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
@@ -722,7 +880,7 @@ def run_reference_serve(args):
 def main():
     args = parse()
     if args.form is None:
-        args.form = "mixed" if args.config in ("c2", "c4") else "plain"
+        args.form = "mixed" if args.config in ("c2", "c3", "c4") else "plain"
     if args.impl == "reference":
         if args.config == "c4":
             run_reference_serve(args)
@@ -732,6 +890,8 @@ def main():
         run_batch(args)
     elif args.config == "c4":
         run_serve(args)
+    elif args.config == "c3":
+        run_timesteps(args)
     else:
         run_gb300(args)
 

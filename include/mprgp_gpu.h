@@ -93,6 +93,7 @@ typedef struct mprgp_stats {
   long long spmv_fp64, spmv_fp32; /* matrix passes by precision */
   long long phases;               /* device phases executed */
   double device_ms;               /* kernel time of the solve */
+  long long power_passes;         /* matrix passes of the power method (in spmv_*) */
 } mprgp_stats;
 
 /* ---- library ------------------------------------------------------------ */
@@ -112,9 +113,11 @@ int mprgp_context_sync(mprgp_context *ctx);
 /* SM count and resident engine CTAs per SM (the persistent grid's shape). */
 int mprgp_context_info(mprgp_context *ctx, int *nsm, int *blocks_per_sm);
 /* Counters since the context was created: kernels launched (engine runs,
- * setup kernels and every iteration of the power-method graph loop) and the
- * device time of the solver runs (power loop + engine), in milliseconds. */
-int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solver_ms);
+ * cluster-solver launches, setup kernels and every iteration of the
+ * power-method graph loop), the device time of the solver runs (power loop,
+ * cluster solver and engine) and of the power loop alone, in milliseconds. */
+int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solver_ms,
+                           double *power_ms);
 /* Launch shape of later solves on this context (chosen by the autotuner,
  * mprgp_gb300/autotune.py): bit 0 of stage = 1 brings each item's FP32
  * matrix slice into shared memory with bulk async copies (one CTA per SM),

@@ -37,7 +37,8 @@ class Stats(C.Structure):
                 ("active", C.c_int), ("ev_updated", C.c_int), ("residual", C.c_double),
                 ("alpha_bar", C.c_double), ("spec_rad", C.c_double),
                 ("spmv_fp64", C.c_longlong), ("spmv_fp32", C.c_longlong),
-                ("phases", C.c_longlong), ("device_ms", C.c_double)]
+                ("phases", C.c_longlong), ("device_ms", C.c_double),
+                ("power_passes", C.c_longlong)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -112,7 +113,8 @@ def _sig(lib):
       C.c_int, C.c_int, C.POINTER(Options), C.POINTER(C.c_longlong))
     s("mprgp_server_step", C.c_int, _P, _IP, _IP, _IP)
     s("mprgp_server_poll", C.c_int, _P, C.POINTER(C.c_longlong), C.c_int, _IP)
-    s("mprgp_context_counters", C.c_int, _P, C.POINTER(C.c_longlong), C.POINTER(C.c_double))
+    s("mprgp_context_counters", C.c_int, _P, C.POINTER(C.c_longlong), C.POINTER(C.c_double),
+      C.POINTER(C.c_double))
     s("mprgp_server_result", C.c_int, _P, C.c_longlong, _P, _P, C.POINTER(Stats), _P, _IP)
     s("mprgp_server_info", C.c_int, _P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), _IP)
     s("mprgp_beam_default", None, C.POINTER(BeamParams))
@@ -235,10 +237,12 @@ class Context:
         _check(lib().mprgp_context_sync(self.h), "sync")
 
     def counters(self):
-        """(kernels launched, device ms of solver runs) since creation."""
-        n, ms = C.c_longlong(), C.c_double()
-        _check(lib().mprgp_context_counters(self.h, C.byref(n), C.byref(ms)), "context_counters")
-        return n.value, ms.value
+        """(kernels launched, device ms of solver runs, device ms of the power
+        loop) since creation."""
+        n, ms, pms = C.c_longlong(), C.c_double(), C.c_double()
+        _check(lib().mprgp_context_counters(self.h, C.byref(n), C.byref(ms), C.byref(pms)),
+               "context_counters")
+        return n.value, ms.value, pms.value
 
     def set_cluster(self, cluster: int = 8):
         """CTAs per cluster of the small-instance solver (0 = engine only)."""

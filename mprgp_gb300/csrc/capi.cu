@@ -64,7 +64,9 @@ struct mprgp_context {
   PowCtl *d_pc = nullptr;
   std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> power_graphs;
   long long launches = 0;  // kernels launched (each power-loop iteration counts)
-  double solver_ms = 0.0;  // device time of engine runs (power loop + engine)  // reused by mprgp_solve_bsr
+  double solver_ms = 0.0;  // device time of engine runs (power loop + engine)
+  double power_ms = 0.0;   // device time of the power loop alone
+  cudaEvent_t e_pow = nullptr;  // reused by mprgp_solve_bsr
   // per-launch arrays (grown on demand)
   InstDesc *d_desc = nullptr;
   int *d_prefix = nullptr;
@@ -282,6 +284,7 @@ void fill_stats(const InstState &s, double ms, mprgp_stats *out) {
   out->spmv_fp32 = s.spmv32;
   out->phases = s.phases;
   out->device_ms = ms;
+  out->power_passes = s.pow_spmv;
 }
 
 // Cluster-size class (log2 of the cluster size) of an instance of `items`
@@ -483,6 +486,7 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   }
   if (power && pexec) CK(cudaGraphLaunch(pexec, s));
   if (power && !pexec) CK(launch_power_direct(pgrid, power_launches, c->d_args, c->d_pc, s));
+  CK(cudaEventRecord(c->e_pow, s));  // the main stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
     if (class_n[q]) CK(cudaStreamWaitEvent(s, c->join_ev[q], 0));
   if (n_large > 0) CK(launch_engine(args, grid, s));
@@ -494,8 +498,10 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   for (int i = 0; i < n; ++i)
     CK(cudaMemcpyAsync(&st[i], probs[i]->st, sizeof(InstState), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  float ms = 0.f;
+  float ms = 0.f, pms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
+  if (power) CK(cudaEventElapsedTime(&pms, c->e0, c->e_pow));
+  c->power_ms += pms;
   // every body of the power loop issues kPowerUnroll launches, the stream form
   // all `power_launches` (those after the last working one return at once)
   if (power && pexec)
@@ -621,6 +627,7 @@ int mprgp_context_create(int device, mprgp_context **out) {
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&c->e0));
   CK(cudaEventCreate(&c->e1));
+  CK(cudaEventCreate(&c->e_pow));
   cudaMemPoolProps props;
   std::memset(&props, 0, sizeof(props));
   props.allocType = cudaMemAllocationTypePinned;
@@ -675,6 +682,7 @@ int mprgp_context_destroy(mprgp_context *c) {
   }
   cudaEventDestroy(c->e0);
   cudaEventDestroy(c->e1);
+  cudaEventDestroy(c->e_pow);
   cudaStreamDestroy(c->stream);
   if (c->pool) cudaMemPoolDestroy(c->pool);
   delete c;
@@ -699,10 +707,12 @@ int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
   return MPRGP_OK;
 }
 
-int mprgp_context_counters(mprgp_context *c, long long *launches, double *solver_ms) {
+int mprgp_context_counters(mprgp_context *c, long long *launches, double *solver_ms,
+                           double *power_ms) {
   if (!c) return fail(MPRGP_INVALID, "context_counters");
   if (launches) *launches = c->launches;
   if (solver_ms) *solver_ms = c->solver_ms;
+  if (power_ms) *power_ms = c->power_ms;
   return MPRGP_OK;
 }
 

@@ -1275,6 +1275,7 @@ __device__ void advance_power(const InstDesc &D, InstState &S, const double *s) 
       const int k = S.pow_k;
       const double nrm = sqrt(s[1]);
       if (D.prec == PREC_MIXED) S.spmv32++; else S.spmv64++;
+      S.pow_spmv++;
       if (k >= 1 && sqrt(s[0]) <= eps) {  // iteration k-1 converged
         S.spec_rad = S.pow_nrm_prev;
         S.ev_upd = 1;

@@ -85,6 +85,7 @@ struct InstState {
   double dfy, corr, pow_scale, pow_nrm_prev, ru_ref;
   double s_zap, s_zg, s_gp2, s_bb, s_ptp;  // speculative CG sums
   long long spmv64, spmv32, phases;
+  long long pow_spmv;  // matrix passes of the power method (included in spmv64/spmv32)
 };
 
 struct InstDesc {

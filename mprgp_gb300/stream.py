@@ -120,7 +120,7 @@ class StreamPlayer:
         if flush is not None:
             flush()
         torch.cuda.synchronize()
-        n0, ms0 = self.ctx.counters()
+        n0, ms0, _ = self.ctx.counters()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -192,7 +192,7 @@ class StreamPlayer:
         e1.record(stream)
         e1.synchronize()
         wall = time.perf_counter() - t0
-        n1, ms1 = self.ctx.counters()
+        n1, ms1, _ = self.ctx.counters()
         srv.close()
         return PlayResult(rate_hz, wall, e0.elapsed_time(e1), lat, codes, stats, xs, faces,
                           n1 - n0, ms1 - ms0, h2d, d2h)
