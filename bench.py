@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="c4: skip the arrival-rate sweep")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the launch-shape autotuner (mprgp_gb300.autotune) before warm-up")
     ap.add_argument("--tuning", type=int, default=None,
                     help="launch-form bits for mprgp_context_set_tuning (bit 2: power loop from "
                          "host-stream launches instead of the CUDA-graph WHILE loop)")
@@ -169,6 +171,21 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def autotune_ctx(args, ctx, sample, precision):
+    """Untimed: pick launch shapes for this workload on a sample of it (an
+    explicit --tuning wins)."""
+    if args.tuning is not None:
+        ctx.set_tuning(args.tuning, 0)
+        return {"explicit_tuning_bits": args.tuning}
+    if args.no_autotune:
+        return None
+    from mprgp_gb300 import autotune
+    r = autotune.tune(ctx, sample, precision=precision, reps=1, use_cache=False)
+    return {"config": r["config"], "sample_ms": round(r["ms"], 3),
+            "default_ms": round(r["default_ms"], 3), "candidates": len(r["tried"]),
+            "seconds": round(r["seconds"], 2), "sample_size": len(sample)}
+
+
 def cpu_baseline(qp, threads=1):
     """One full solve of the same QP by the CPU restatement of the reference."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -202,10 +219,9 @@ def run_gb300(args):
     qp = workload_qp(args.config)
     tol = REL_TOL * float(np.linalg.norm(qp.b))
     ctx = M.Context(local)
-    if args.tuning is not None:
-        ctx.set_tuning(args.tuning, 0)
     mixed = args.form == "mixed"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
+    tuning = autotune_ctx(args, ctx, [qp], prec)
     opt = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=1, seed=SEED,
                             precision=prec)
     prob = M.load_beam(ctx, qp, precisions=3 if mixed else 1)
@@ -281,7 +297,7 @@ def run_gb300(args):
         "data": "synthetic (seeded beam QP, no dataset)",
         "config": dict(workload_desc(args.config, qp), form=args.form + "-" + ("mixed" if mixed else "fp64"),
                        l2="flushed between solves (256 MB device write)",
-                       parallelism="replicas" if world > 1 else "single GPU"),
+                       parallelism="replicas" if world > 1 else "single GPU", autotune=tuning),
         "latency_ms": {"p50": round(float(np.percentile(times, 50)), 4),
                        "p99": round(float(np.percentile(times, 99)), 4)},
         "solve": {"iterations": st.iterations, "cg": st.num_cg, "exp": st.num_exp,
@@ -408,8 +424,7 @@ def run_batch(args):
     M.build()
     qps = W.batch()
     ctx = M.Context(local)
-    if args.tuning is not None:
-        ctx.set_tuning(args.tuning, 0)
+    tuning = autotune_ctx(args, ctx, qps[:48], M.PREC_MIXED if args.form != "plain" else M.PREC_FP64)
     probs, opts64, optsmx, x0s = [], [], [], []
     for qp in qps:
         pr = M.load_beam(ctx, qp, precisions=3)
@@ -478,7 +493,8 @@ def run_batch(args):
                                f"({min(nvs)}..{max(nvs)} vertices, {3 * sum(nvs)} DOF total), floor + 0-2 walls, "
                                f"v0 ~ N(0, 0.2^2), tol 1e-8||b|| each", "config": "c2",
                    "form": "batched-" + ("mixed" if args.form != "plain" else "fp64"),
-                   "l2": "flushed between batched solves (256 MB device write)"},
+                   "l2": "flushed between batched solves (256 MB device write)",
+                   "autotune": tuning},
         "plain_fp64_one_at_a_time": {"value": round(len(qps) / t_plain, 3), "unit": "solves/s",
                                      "speedup_of_value": round(value / (len(qps) / t_plain), 2)},
         "solve": {"iterations_max": max(s.iterations for s in stats),
@@ -515,10 +531,9 @@ def run_timesteps(args):
     M.build()
     qp = workload_qp("c3")
     ctx = M.Context(local)
-    if args.tuning is not None:
-        ctx.set_tuning(args.tuning, 0)
     mixed = args.form != "plain"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
+    tuning = autotune_ctx(args, ctx, [qp], prec)
     prob = M.load_beam(ctx, qp, precisions=3)
     ref = M.load_beam(ctx, qp, precisions=1)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -598,7 +613,7 @@ def run_timesteps(args):
                        timesteps=total, warm_start="x from the previous timestep, b from its solution",
                        power_method="reused across timesteps while A and the seed are unchanged "
                                     "(bitwise the same alpha_bar)",
-                       l2="flushed before every timestep (256 MB device write)"),
+                       l2="flushed before every timestep (256 MB device write)", autotune=tuning),
         "latency_ms": {"p50": round(float(np.percentile(times, 50)), 3),
                        "p99": round(float(np.percentile(times, 99)), 3)},
         "per_timestep": records,
@@ -684,10 +699,9 @@ def run_serve(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     M.build()
-    win = W.serving_window(SERVE_COUNT, SERVE_SEED)
+    # replicas: each rank serves its own window of the stream (weak scaling)
+    win = W.serving_window(SERVE_COUNT, SERVE_SEED + rank)
     ctx = M.Context(local)
-    if args.tuning is not None:
-        ctx.set_tuning(args.tuning, 0)
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush_buf = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -696,6 +710,7 @@ def run_serve(args):
 
     mixed = args.form != "plain"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
+    tuning = autotune_ctx(args, ctx, serve_sample(win, 48), prec)
     pl = StreamPlayer(ctx, win, rel_tol=REL_TOL, seed=SEED)
     served = dict(max_slots=512, quantum=512, power_launches=1003, cluster_quantum=0)
     plain = dict(max_slots=1, quantum=-1, power_launches=1003)
@@ -722,13 +737,11 @@ def run_serve(args):
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    total_ms = sum(r.event_ms for r in timed)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from mprgp_gb300 import replicas
     n_req = len(win.reqs)
-    value = world * n_req * args.steps / (total_ms / 1e3)
+    local_ms = sum(r.event_ms for r in timed)
+    value = replicas.aggregate_throughput(n_req * args.steps, local_ms / 1e3)
+    total_ms = replicas.max_over_ranks(local_ms)
     lat = np.concatenate([r.latency_s for r in timed]) * 1e3
     # plain FP64, one request at a time, same stream and arrivals
     base = check(pl.play(SERVE_RATE, M.PREC_FP64, "device", flush=flush, stream=stream,
@@ -778,6 +791,7 @@ def run_serve(args):
                               "power_loop_per_step": served["power_launches"],
                               "small_instances": "cluster solver, to completion within a step"},
                    "inputs": "staged in device memory before the timed region (e2e: pinned host)",
+                   "autotune": tuning,
                    "l2": "flushed before every window (256 MB device write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
@@ -809,7 +823,8 @@ def run_serve(args):
                for _ in range(args.steps)]
         ems = sum(r.event_ms for r in e2e)
         elat = np.concatenate([r.latency_s for r in e2e]) * 1e3
-        line["e2e"] = {"value": round(world * n_req * args.steps / (ems / 1e3), 3), "unit": "solves/s",
+        line["e2e"] = {"value": round(replicas.aggregate_throughput(n_req * args.steps, ems / 1e3), 3),
+                       "unit": "solves/s",
                        "h2d_bytes_per_step": int(e2e[0].h2d_bytes),
                        "d2h_bytes_per_step": int(e2e[0].d2h_bytes),
                        "p50_ms": round(float(np.percentile(elat, 50)), 3),

@@ -23,13 +23,13 @@
 
 namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
-cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, cudaGraph_t *graph,
-                              cudaGraphExec_t *exec);
-cudaError_t power_max_blocks_per_sm(int *n);
+cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, PowCtl *d_pc,
+                              cudaGraph_t *graph, cudaGraphExec_t *exec);
+cudaError_t power_max_blocks_per_sm(int variant, int *n);
 cudaError_t launch_cluster(const ClusterArgs &args, int csize, cudaStream_t stream);
 cudaError_t cluster_max_active(int csize, int *n);
-cudaError_t launch_power_direct(int grid, int launches, const EngineArgs *d_args, PowCtl *d_pc,
-                                cudaStream_t stream);
+cudaError_t launch_power_direct(int grid, int variant, int launches, const EngineArgs *d_args,
+                                PowCtl *d_pc, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,
@@ -50,6 +50,8 @@ struct mprgp_context {
   int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
   int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
+  int power_variant = 0; // power kernel with 40 registers (0, 6 CTAs/SM) or 64 (1, 4 CTAs/SM)
+  int bps_power_v[2] = {0, 0};
   int cluster = 16;      // largest cluster of the small-instance solver (0 = off)
   int cluster_ok[kClusterClasses] = {0, 0, 0, 0, 0};  // cluster sizes 1, 2, 4, 8, 16 usable
   cudaStream_t side[kClusterClasses] = {};  // one per cluster size (run concurrently)
@@ -306,14 +308,16 @@ int power_grid(mprgp_context *c, int items) {
   return std::min(cap, (items + 31) / 32 * 32);
 }
 
-// The instantiated power-method graph for `grid` CTAs.
+// The instantiated power-method graph for `grid` CTAs of the context's
+// power-kernel variant.
 int power_graph(mprgp_context *c, int grid, cudaGraphExec_t *exec) {
-  auto it = c->power_graphs.find(grid);
+  const int key = grid * 2 + c->power_variant;
+  auto it = c->power_graphs.find(key);
   if (it == c->power_graphs.end()) {
     cudaGraph_t g;
     cudaGraphExec_t e;
-    CK(build_power_graph(grid, c->d_args, c->d_pc, &g, &e));
-    it = c->power_graphs.emplace(grid, std::make_pair(g, e)).first;
+    CK(build_power_graph(grid, c->power_variant, c->d_args, c->d_pc, &g, &e));
+    it = c->power_graphs.emplace(key, std::make_pair(g, e)).first;
   }
   *exec = it->second.second;
   return MPRGP_OK;
@@ -485,7 +489,8 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
     CK(cudaEventRecord(c->join_ev[q], c->side[q]));
   }
   if (power && pexec) CK(cudaGraphLaunch(pexec, s));
-  if (power && !pexec) CK(launch_power_direct(pgrid, power_launches, c->d_args, c->d_pc, s));
+  if (power && !pexec)
+    CK(launch_power_direct(pgrid, c->power_variant, power_launches, c->d_args, c->d_pc, s));
   CK(cudaEventRecord(c->e_pow, s));  // the main stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
     if (class_n[q]) CK(cudaStreamWaitEvent(s, c->join_ev[q], 0));
@@ -636,7 +641,9 @@ int mprgp_context_create(int device, mprgp_context **out) {
   CK(cudaMemPoolCreate(&c->pool, &props));
   unsigned long long keep = ~0ULL;  // never trim: freed blocks serve the next problem
   CK(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
-  CK(power_max_blocks_per_sm(&c->bps_power));
+  CK(power_max_blocks_per_sm(0, &c->bps_power_v[0]));
+  CK(power_max_blocks_per_sm(1, &c->bps_power_v[1]));
+  c->bps_power = c->bps_power_v[0];
   {
     int largest = 0;
     for (int q = 0; q < kClusterClasses; ++q) {
@@ -698,9 +705,11 @@ int mprgp_context_sync(mprgp_context *c) {
 }
 
 int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
-  if (!c || stage < 0 || stage > 7 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  if (!c || stage < 0 || stage > 15 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
   c->power_kernel = (stage & 2) ? 0 : 1;
   c->power_graph = (stage & 4) ? 0 : 1;
+  c->power_variant = (stage & 8) ? 1 : 0;
+  c->bps_power = c->bps_power_v[c->power_variant];
   stage &= 1;
   c->stage = stage;
   c->ctas_per_sm = ctas_per_sm;

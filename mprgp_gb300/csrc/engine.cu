@@ -1791,7 +1791,11 @@ __device__ __forceinline__ void power_item(const InstDesc *desc, const int *item
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 6)
+// Two register budgets: 40 registers (6 CTAs per SM, for grids that fill
+// the SMs) or 64 (4 CTAs per SM, more loads in flight per thread); the
+// context's tuning picks one.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     power_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc, cudaGraphConditionalHandle h,
                  int signal) {
   __shared__ InstDesc sD;
@@ -2010,8 +2014,11 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
 // instance is left in a power phase or PowCtl::limit launches have run.  The
 // kernel reads its EngineArgs and PowCtl from device memory, so one
 // instantiation serves every later run with the same grid.
-cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, cudaGraph_t *graph,
-                              cudaGraphExec_t *exec) {
+const void *power_kernel_fn(int variant) {
+  return variant ? (const void *)power_kernel<4> : (const void *)power_kernel<6>;
+}
+cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, PowCtl *d_pc,
+                              cudaGraph_t *graph, cudaGraphExec_t *exec) {
   *graph = nullptr;
   *exec = nullptr;
   cudaGraph_t g = nullptr;
@@ -2031,7 +2038,7 @@ cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, 
     void *kargs[] = {(void *)&d_args, (void *)&d_pc, (void *)&h, (void *)&signal};
     cudaKernelNodeParams kp;
     memset(&kp, 0, sizeof(kp));
-    kp.func = (void *)power_kernel;
+    kp.func = (void *)power_kernel_fn(variant);
     kp.gridDim = dim3(grid);
     kp.blockDim = dim3(kThreads);
     kp.kernelParams = kargs;
@@ -2054,10 +2061,13 @@ cudaError_t build_power_graph(int grid, const EngineArgs *d_args, PowCtl *d_pc, 
 }
 // The same loop as plain stream launches (`launches` of them; those after the
 // last working one return at once).
-cudaError_t launch_power_direct(int grid, int launches, const EngineArgs *d_args, PowCtl *d_pc,
-                                cudaStream_t stream) {
+cudaError_t launch_power_direct(int grid, int variant, int launches, const EngineArgs *d_args,
+                                PowCtl *d_pc, cudaStream_t stream) {
   for (int k = 0; k < launches; ++k) {
-    power_kernel<<<grid, kThreads, 0, stream>>>(d_args, d_pc, cudaGraphConditionalHandle(0), 0);
+    if (variant)
+      power_kernel<4><<<grid, kThreads, 0, stream>>>(d_args, d_pc, cudaGraphConditionalHandle(0), 0);
+    else
+      power_kernel<6><<<grid, kThreads, 0, stream>>>(d_args, d_pc, cudaGraphConditionalHandle(0), 0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -2098,8 +2108,8 @@ cudaError_t cluster_max_active(int csize, int *n) {
   cfg.numAttrs = 1;
   return cudaOccupancyMaxActiveClusters(n, cluster_kernel, &cfg);
 }
-cudaError_t power_max_blocks_per_sm(int *n) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel, kThreads, 0);
+cudaError_t power_max_blocks_per_sm(int variant, int *n) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel_fn(variant), kThreads, 0);
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, int *out_cols, double *out64, float *out32,

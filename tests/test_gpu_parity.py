@@ -335,3 +335,21 @@ def test_gpu_matches_golden(ctx, path):
     assert st.code == 0
     assert rel(x, xr) <= 1e-8
     assert np.array_equal(act, act_r)
+
+
+def test_autotune_pick_is_result_invariant(tmp_path, monkeypatch):
+    """The autotuner's launch shapes never change a solution: it verifies its
+    pick against the default bitwise, and the pick round-trips its cache."""
+    from mprgp_gb300 import autotune
+    monkeypatch.setenv("MPRGP_TUNING_CACHE", str(tmp_path / "tuning.json"))
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(4, 4, 6, 1, 21), (9, 9, 24, 2, 22), (16, 16, 40, 1, 23)]]
+    c = M.Context(0)
+    try:
+        r = autotune.tune(c, qps, precision=M.PREC_MIXED, reps=1)
+        assert not r["cached"] and r["ms"] <= r["default_ms"] * 1.0001
+        assert set(r["config"]) == set(autotune.DEFAULT)
+        r2 = autotune.tune(c, qps, precision=M.PREC_MIXED, reps=1)
+        assert r2["cached"] and r2["config"] == r["config"]
+    finally:
+        c.close()
