@@ -32,8 +32,8 @@ cudaError_t launch_power_direct(int grid, int variant, int launches, const Engin
                                 PowCtl *d_pc, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
-                        const int *slice_off, int *out_cols, double *out64, float *out32,
-                        double *dinv, cudaStream_t st);
+                        const int *slice_off, const int *rowmap, int *out_cols, double *out64,
+                        float *out32, double *dinv, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st);
 void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
@@ -101,6 +101,10 @@ struct mprgp_problem {
   double *stage_vals = nullptr;
   size_t stage_nnzb = 0;
   std::vector<int> h_plane_ptr;
+  std::vector<int> h_len;     // blocks per row of A
+  int *rowmap = nullptr;      // SELL row -> vertex (nullptr: identity)
+  unsigned long long layout = 0;
+  int want64 = 0, want32 = 0;
   int phase_host = 0;  // the instance's phase at the end of its last engine run
   // Result of the last power method that started from the seeded random
   // vector.  That power method is a deterministic function of (A, seed,
@@ -162,6 +166,80 @@ void free_problem_arrays(mprgp_problem *p) {
   dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
   dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->st);
   dfree(p->ctx, p->trace); dfree(p->ctx, p->stage_ptr); dfree(p->ctx, p->stage_cols); dfree(p->ctx, p->stage_vals);
+  dfree(p->ctx, p->rowmap);
+}
+
+// The SELL row order of a problem: vertices with at most one constraint
+// plane first, those with several after them (stable), so that the
+// multi-plane projection runs in few, uniform warps.  Identity when no
+// vertex has several planes.  The key identifies the order.
+unsigned long long layout_key(const mprgp_problem *p) {
+  unsigned long long h = 1469598103934665603ull;
+  if (p->cons != 1 || p->h_plane_ptr.empty()) return h;
+  for (int v = 0; v < p->nv; ++v)
+    if (p->h_plane_ptr[v + 1] - p->h_plane_ptr[v] >= 2) {
+      h ^= (unsigned long long)v + 0x9E3779B97F4A7C15ull;
+      h *= 1099511628211ull;
+    }
+  return h;
+}
+
+// (Re)builds the SELL copy of A from the device BSR in the order above.
+int build_layout(mprgp_problem *p, unsigned long long key) {
+  mprgp_context *c = p->ctx;
+  cudaStream_t s = c->stream;
+  const int nv = p->nv;
+  std::vector<int> order;  // slot -> vertex
+  if (p->cons == 1 && !p->h_plane_ptr.empty()) {
+    std::vector<int> multi;
+    order.reserve(nv);
+    for (int v = 0; v < nv; ++v) {
+      if (p->h_plane_ptr[v + 1] - p->h_plane_ptr[v] >= 2) multi.push_back(v);
+      else order.push_back(v);
+    }
+    if (multi.empty()) order.clear();
+    else order.insert(order.end(), multi.begin(), multi.end());
+  }
+  const bool ident = order.empty();
+  std::vector<int> off(p->nslices + 1, 0);
+  for (int sl = 0; sl < p->nslices; ++sl) {
+    int w = 0;
+    for (int q = sl * kSlice; q < std::min(nv, (sl + 1) * kSlice); ++q)
+      w = std::max(w, p->h_len[ident ? q : order[q]]);
+    off[sl + 1] = off[sl] + w;
+  }
+  const int slots = off[p->nslices];
+  if (slots != p->slots || p->want64 != p->has64 || p->want32 != p->has32) {
+    dfree(c, p->cols);
+    dfree(c, p->v64);
+    dfree(c, p->v32);
+    int rc = dalloc(c, &p->cols, (size_t)slots * kSlice);
+    if (!rc && p->want64) rc = dalloc(c, &p->v64, (size_t)slots * kSlice * 9);
+    if (!rc && p->want32) rc = dalloc(c, &p->v32, (size_t)slots * kSlice * 9);
+    if (rc) return rc;
+    p->slots = slots;
+    p->has64 = p->want64;
+    p->has32 = p->want32;
+  }
+  CK(cudaMemcpyAsync(p->slice_off, off.data(), sizeof(int) * (p->nslices + 1),
+                     cudaMemcpyHostToDevice, s));
+  if (ident) {
+    dfree(c, p->rowmap);
+  } else {
+    if (!p->rowmap) {
+      int rc = dalloc(c, &p->rowmap, nv);
+      if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(p->rowmap, order.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s));
+  }
+  c->launches++;
+  launch_bsr_to_sell(nv, p->stage_ptr, p->stage_cols, p->stage_vals, p->slice_off, p->rowmap,
+                     p->cols, p->v64, p->v32, p->dinv, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
+  CK(cudaStreamSynchronize(s));  // `order` and `off` are released next
+  p->layout = key;
+  return MPRGP_OK;
 }
 
 int resolve_options(const mprgp_problem *p, const mprgp_options *o, int *kind, int *alg,
@@ -224,6 +302,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->A.cols = p->cols;
   d->A.v64 = p->v64;
   d->A.v32 = p->v32;
+  d->A.rowmap = p->rowmap;
   d->nv = p->nv;
   d->nitems = nitems_of(p->nv);
   d->item_begin = item_begin;
@@ -754,6 +833,7 @@ size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {
   by += n * 8 * (kNumBuf + 3) + n * 4 * kNumBuf32;  // vectors, dinv, b, ev, FP32 shadows
   by += (size_t)nplanes * (8 * 4 * 2 + 8 * 2 + 1) + (size_t)(nv + 1) * 4 + n * 16 + n;
   by += (size_t)nitems_of(nv) * kPart * 8 + sizeof(InstState) + 64;
+  by += (size_t)nnzb * (9 * 8 + 4) + (size_t)(nv + 1) * 4 + (size_t)nv * 4;  // BSR copy, rowmap
   return by;
 }
 
@@ -808,55 +888,31 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   if (!on_device)
     for (int q = 0; q < nnzb; ++q)
       if (cols[q] < 0 || cols[q] >= nv) return fail(MPRGP_INVALID, "column out of range");
-  std::vector<int> off(p->nslices + 1, 0);
-  for (int sl = 0; sl < p->nslices; ++sl) {
-    int w = 0;
-    for (int r = sl * kSlice; r < std::min(nv, (sl + 1) * kSlice); ++r)
-      w = std::max(w, h_ptr[r + 1] - h_ptr[r]);
-    off[sl + 1] = off[sl] + w;
-  }
-  const int slots = off[p->nslices];
-  if (slots != p->slots || (precisions & 1) != p->has64 || ((precisions >> 1) & 1) != p->has32) {
-    dfree(p->ctx, p->cols);
-    dfree(p->ctx, p->v64);
-    dfree(p->ctx, p->v32);
-    int rc = dalloc(p->ctx, &p->cols, (size_t)slots * kSlice);
-    if (!rc && (precisions & 1)) rc = dalloc(p->ctx, &p->v64, (size_t)slots * kSlice * 9);
-    if (!rc && (precisions & 2)) rc = dalloc(p->ctx, &p->v32, (size_t)slots * kSlice * 9);
+  // The BSR stays on the device (the SELL layout is rebuilt from it when the
+  // constraint planes change which vertices have several planes).
+  if (!p->stage_ptr) {
+    int rc = dalloc(p->ctx, &p->stage_ptr, nv + 1);
     if (rc) return rc;
-    p->slots = slots;
-    p->has64 = precisions & 1;
-    p->has32 = (precisions >> 1) & 1;
   }
-  CK(cudaMemcpyAsync(p->slice_off, off.data(), sizeof(int) * (p->nslices + 1),
-                     cudaMemcpyHostToDevice, s));
-  const int *d_ptr = row_ptr, *d_cols = cols;
-  const double *d_vals = vals;
-  if (!on_device) {
-    if (!p->stage_ptr) {
-      int rc = dalloc(p->ctx, &p->stage_ptr, nv + 1);
-      if (rc) return rc;
-    }
-    if ((size_t)nnzb > p->stage_nnzb) {
-      dfree(p->ctx, p->stage_cols);
-      dfree(p->ctx, p->stage_vals);
-      int rc = dalloc(p->ctx, &p->stage_cols, nnzb);
-      if (!rc) rc = dalloc(p->ctx, &p->stage_vals, (size_t)nnzb * 9);
-      if (rc) return rc;
-      p->stage_nnzb = nnzb;
-    }
-    CK(cudaMemcpyAsync(p->stage_ptr, row_ptr, sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(p->stage_cols, cols, sizeof(int) * nnzb, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(p->stage_vals, vals, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
-    d_ptr = p->stage_ptr;
-    d_cols = p->stage_cols;
-    d_vals = p->stage_vals;
+  if ((size_t)nnzb > p->stage_nnzb) {
+    dfree(p->ctx, p->stage_cols);
+    dfree(p->ctx, p->stage_vals);
+    int rc = dalloc(p->ctx, &p->stage_cols, nnzb);
+    if (!rc) rc = dalloc(p->ctx, &p->stage_vals, (size_t)nnzb * 9);
+    if (rc) return rc;
+    p->stage_nnzb = nnzb;
   }
-  c->launches++;
-  launch_bsr_to_sell(nv, d_ptr, d_cols, d_vals, p->slice_off, p->cols, p->v64, p->v32, p->dinv, s);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  CK(cudaMemcpyAsync(p->stage_ptr, row_ptr, sizeof(int) * (nv + 1), kind, s));
+  CK(cudaMemcpyAsync(p->stage_cols, cols, sizeof(int) * nnzb, kind, s));
+  CK(cudaMemcpyAsync(p->stage_vals, vals, sizeof(double) * 9 * nnzb, kind, s));
+  p->h_len.resize(nv);
+  for (int r = 0; r < nv; ++r) p->h_len[r] = h_ptr[r + 1] - h_ptr[r];
   p->nnzb = nnzb;
+  p->want64 = precisions & 1;
+  p->want32 = (precisions >> 1) & 1;
+  const int rc = build_layout(p, layout_key(p));
+  if (rc) return rc;
   p->planes_dirty = 1;  // 1/diag(J D^-1 J^T) depends on D
   p->matrix_gen++;      // a new A: the cached power method no longer applies
   p->pcache.valid = 0;
@@ -908,6 +964,10 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
   p->planes_dirty = 1;
   p->h_plane_ptr.swap(h);
   CK(cudaStreamSynchronize(s));  // host staging vector `h` is released next
+  if (p->cols && p->stage_vals) {
+    const unsigned long long key = layout_key(p);
+    if (key != p->layout) return build_layout(p, key);
+  }
   return MPRGP_OK;
 }
 
@@ -1033,6 +1093,7 @@ int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int
   A.nslices = p->nslices;
   A.slice_off = p->slice_off;
   A.cols = p->cols;
+  A.rowmap = p->rowmap;
   A.v64 = p->v64;
   A.v32 = p->v32;
   p->ctx->launches++;

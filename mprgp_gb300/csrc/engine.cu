@@ -300,13 +300,13 @@ __device__ __forceinline__ void spmv_row_staged(const SellMatrix &A, int v, cons
 }
 
 template <typename Src64, typename Src32>
-__device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int v, const Src64 &src64,
+__device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int slot, const Src64 &src64,
                                          const Src32 &src32, double out[3]) {
   if (fp32) {
-    if (g_staged) spmv_row_staged<float>(D.A, v, src32, out);
-    else spmv_row<float>(D.A, D.A.v32, v, src32, out);
+    if (g_staged) spmv_row_staged<float>(D.A, slot, src32, out);
+    else spmv_row<float>(D.A, D.A.v32, slot, src32, out);
   } else {
-    spmv_row<double>(D.A, D.A.v64, v, src64, out);
+    spmv_row<double>(D.A, D.A.v64, slot, src64, out);
   }
 }
 
@@ -752,7 +752,7 @@ __device__ __forceinline__ void st3ff(float *b, int v, const float o[3]) {
   q[2] = o[2];
 }
 
-__device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, int v, int slot,
                                          double *part) {
   const int k = S.pow_k;
   const float sc = (float)S.pow_scale;  // 1/||w|| (tmpOut /= norm)
@@ -779,11 +779,11 @@ __device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, 
   st3ff(D.buf32[F_Z0 + (k & 1)], v, u);
   float w[3];
   if (S.pow_src < 0) {
-    spmv_row<float, SrcVtoF, float>(D.A, D.A.v32, v, SrcVtoF{D.ev}, w);
+    spmv_row<float, SrcVtoF, float>(D.A, D.A.v32, slot, SrcVtoF{D.ev}, w);
   } else {
     const SrcF src{D.buf32[S.pow_src == B_W ? F_W0 : F_W1]};
-    if (g_staged) spmv_row_staged<float, SrcF, float>(D.A, v, src, w);
-    else spmv_row<float, SrcF, float>(D.A, D.A.v32, v, src, w);
+    if (g_staged) spmv_row_staged<float, SrcF, float>(D.A, slot, src, w);
+    else spmv_row<float, SrcF, float>(D.A, D.A.v32, slot, src, w);
   }
   w[0] *= sc;
   w[1] *= sc;
@@ -792,11 +792,11 @@ __device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, 
   part[1] += (double)fmaf(w[0], w[0], fmaf(w[1], w[1], w[2] * w[2]));
 }
 
-__device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, int v, int slot,
                                        double *part) {
   const bool f32 = D.prec == PREC_MIXED;
   if (f32 && S.phase != PH_POW_RAND) {
-    row_power32(D, S, v, part);
+    row_power32(D, S, v, slot, part);
     return;
   }
   if (S.phase == PH_POW_RAND) {
@@ -827,7 +827,7 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
   // A (src / ||w||) = (A src) / ||w||; the FP32 pass reads src's FP32 shadow
   // (the stored start vector ev has none and takes the FP64 pass).
   const bool f32src = f32 && S.pow_src >= 0;
-  spmv_any(D, f32src, v, SrcV{src},
+  spmv_any(D, f32src, slot, SrcV{src},
            SrcF{f32src ? D.buf32[S.pow_src == B_W ? F_W0 : F_W1] : nullptr}, w);
   w[0] *= S.pow_scale;
   w[1] *= S.pow_scale;
@@ -837,7 +837,7 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
   part[1] += dot3(w, w);
 }
 
-__device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int v, int slot,
                                       double *part) {
   VCons C;
   load_cons(D, v, C);
@@ -864,13 +864,13 @@ __device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int
   }
   double x[3], ax[3];
   ld3(B(D, B_X0 + S.xc), v, x);
-  spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
+  spmv_row<double>(D.A, D.A.v64, slot, SrcV{B(D, B_X0 + S.xc)}, ax);
   const double g[3] = {ax[0] - ldro(D.b + 3 * (size_t)v), ax[1] - ldro(D.b + 3 * (size_t)v + 1),
                        ax[2] - ldro(D.b + 3 * (size_t)v + 2)};
   epilogue_full(D, S, C, v, x, g, part);
 }
 
-__device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, int v, int slot,
                                          double *part) {
   const bool f32 = D.prec == PREC_MIXED;
   double p[3], ap[3], g[3];
@@ -880,14 +880,14 @@ __device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, 
     ld3(pp, v, p);
     if (S.phase == PH_CG_ENTRY && !S.g_cons) {
       double ax[3];
-      spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
+      spmv_row<double>(D.A, D.A.v64, slot, SrcV{B(D, B_X0 + S.xc)}, ax);
       double e[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) e[d] = (ax[d] - ldro(D.b + 3 * (size_t)v + d)) - g[d];
       st3(B(D, B_E), v, e);
       part[2] += dot3(p, e);
     }
-    spmv_any(D, f32 && S.phase != PH_PL_SPMV, v, SrcV{pp},
+    spmv_any(D, f32 && S.phase != PH_PL_SPMV, slot, SrcV{pp},
              SrcF{f32 ? D.buf32[F_P0 + S.pc] : nullptr}, ap);
   } else {
     const double *zz = B(D, B_Z0 + S.zc), *po = B(D, B_P0 + S.pc);
@@ -899,7 +899,7 @@ __device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, 
     st3(B(D, B_P0 + (S.pc ^ 1)), v, p);
     const bool f32p = f32 && S.phase != PH_PL_SPMV;
     if (f32p) st3f(D.buf32[F_P0 + (S.pc ^ 1)], v, p);
-    spmv_any(D, f32p, v, SrcPNew{zz, po, S.beta_cg},
+    spmv_any(D, f32p, slot, SrcPNew{zz, po, S.beta_cg},
              SrcPNewF{f32p ? D.buf32[F_Z0 + S.zc] : nullptr,
                       f32p ? D.buf32[F_P0 + S.pc] : nullptr, (float)S.beta_cg}, ap);
     if (S.e_nz && S.phase == PH_CG_SPMV) {
@@ -922,7 +922,7 @@ __device__ __noinline__ void row_cg_spmv(const InstDesc &D, const InstState &S, 
 
 // Candidate y = x - alpha p: feasibility, the f(P(y)) correction terms and
 // the CG state that committing y would produce (CGMonotonicStep, :287-313).
-__device__ __noinline__ void row_cg_yf(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_cg_yf(const InstDesc &D, const InstState &S, int v, int slot,
                                        double *part) {
   VCons C;
   load_cons(D, v, C);
@@ -973,27 +973,27 @@ __device__ __noinline__ void row_cg_yf(const InstDesc &D, const InstState &S, in
 }
 
 // delta^T A delta over the rows where P(y) moved y (rare).
-__device__ __noinline__ void row_cg_dad(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_cg_dad(const InstDesc &D, const InstState &S, int v, int slot,
                                         double *part) {
   (void)S;
   double dl[3];
   ld3(B(D, B_W), v, dl);
   if (dl[0] == 0.0 && dl[1] == 0.0 && dl[2] == 0.0) return;
   double ad[3];
-  spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_W)}, ad);
+  spmv_row<double>(D.A, D.A.v64, slot, SrcV{B(D, B_W)}, ad);
   part[0] += dot3(dl, ad);
 }
 
 // FP64 residual replacement for the mixed form: g = A64 x - b with the face
 // kept, then phi, z, beta and the sums for the current x.
-__device__ __noinline__ void row_ru(const InstDesc &D, const InstState &S, int v, double *part) {
+__device__ __noinline__ void row_ru(const InstDesc &D, const InstState &S, int v, int slot, double *part) {
   VCons C;
   load_cons(D, v, C);
   const int f = load_face(D, C);
   double x[3], ax[3], ap[3];
   ld3(B(D, B_X0 + S.xc), v, x);
   ld3(B(D, B_AP), v, ap);
-  spmv_row<double>(D.A, D.A.v64, v, SrcV{B(D, B_X0 + S.xc)}, ax);
+  spmv_row<double>(D.A, D.A.v64, slot, SrcV{B(D, B_X0 + S.xc)}, ax);
   const double g[3] = {ax[0] - ldro(D.b + 3 * (size_t)v), ax[1] - ldro(D.b + 3 * (size_t)v + 1),
                        ax[2] - ldro(D.b + 3 * (size_t)v + 2)};
   double phi[3], z[3], beta[3];
@@ -1012,7 +1012,7 @@ __device__ __noinline__ void row_ru(const InstDesc &D, const InstState &S, int v
   part[4] += dot3(z, ap);
 }
 
-__device__ __noinline__ void row_exp(const InstDesc &D, const InstState &S, int v, double *part) {
+__device__ __noinline__ void row_exp(const InstDesc &D, const InstState &S, int v, int slot, double *part) {
   VCons C;
   load_cons(D, v, C);
   if (S.phase == PH_EXP_A) {  // y = P(x)
@@ -1026,7 +1026,7 @@ __device__ __noinline__ void row_exp(const InstDesc &D, const InstState &S, int 
     const double *yb = B(D, B_X0 + (S.xc ^ 1));
     double y[3], ay[3];
     ld3(yb, v, y);
-    spmv_row<double>(D.A, D.A.v64, v, SrcV{yb}, ay);
+    spmv_row<double>(D.A, D.A.v64, slot, SrcV{yb}, ay);
     const double g[3] = {ay[0] - ldro(D.b + 3 * (size_t)v),
                          ay[1] - ldro(D.b + 3 * (size_t)v + 1),
                          ay[2] - ldro(D.b + 3 * (size_t)v + 2)};
@@ -1068,7 +1068,7 @@ __device__ __noinline__ void row_exp(const InstDesc &D, const InstState &S, int 
   st3(B(D, B_X0 + S.xc), v, xn);
 }
 
-__device__ __noinline__ void row_prop(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_prop(const InstDesc &D, const InstState &S, int v, int slot,
                                       double *part) {
   const double *db = B(D, B_BT0 + S.bc);
   if (S.phase == PH_PROP_A || S.phase == PH_PL_PROP_A) {
@@ -1076,13 +1076,13 @@ __device__ __noinline__ void row_prop(const InstDesc &D, const InstState &S, int
     ld3(db, v, dd);
     if (S.phase == PH_PROP_A) {  // g = A x - B and AD = A D in one pass
       double ax[3];
-      spmv2_row(D.A, v, SrcV{B(D, B_X0 + S.xc)}, SrcV{db}, ax, ad);
+      spmv2_row(D.A, slot, SrcV{B(D, B_X0 + S.xc)}, SrcV{db}, ax, ad);
 #pragma unroll
       for (int d = 0; d < 3; ++d) g[d] = ax[d] - ldro(D.b + 3 * (size_t)v + d);
       st3(B(D, B_G0 + S.gc), v, g);
     } else {
       ld3(B(D, B_G0 + S.gc), v, g);
-      spmv_row<double>(D.A, D.A.v64, v, SrcV{db}, ad);
+      spmv_row<double>(D.A, D.A.v64, slot, SrcV{db}, ad);
     }
     st3(B(D, B_W), v, ad);
     part[0] += dot3(g, dd);
@@ -1110,7 +1110,7 @@ __device__ __noinline__ void row_prop(const InstDesc &D, const InstState &S, int
   epilogue_full(D, S, C, v, xn, g, part);
 }
 
-__device__ __noinline__ void row_pl_cg(const InstDesc &D, const InstState &S, int v,
+__device__ __noinline__ void row_pl_cg(const InstDesc &D, const InstState &S, int v, int slot,
                                        double *part) {
   // CGStep (:182-195) then the loop top's BETA and sums.
   VCons C;
@@ -1142,29 +1142,29 @@ __device__ __noinline__ void row_pl_cg(const InstDesc &D, const InstState &S, in
   part[5] += dot3(z, ap);
 }
 
-__device__ void row_op(const InstDesc &D, const InstState &S, int v, double *part) {
+__device__ void row_op(const InstDesc &D, const InstState &S, int v, int slot, double *part) {
   switch (S.phase) {
     case PH_POW_RAND:
     case PH_POW:
-    case PH_POW_LAST: row_power(D, S, v, part); break;
+    case PH_POW_LAST: row_power(D, S, v, slot, part); break;
     case PH_PROJ0:
     case PH_FINAL:
     case PH_INIT:
     case PH_EXP_C:
-    case PH_PL_EXP_B: row_init(D, S, v, part); break;
+    case PH_PL_EXP_B: row_init(D, S, v, slot, part); break;
     case PH_CG_ENTRY:
     case PH_CG_SPMV:
-    case PH_PL_SPMV: row_cg_spmv(D, S, v, part); break;
-    case PH_CG_YF: row_cg_yf(D, S, v, part); break;
-    case PH_CG_DAD: row_cg_dad(D, S, v, part); break;
-    case PH_RU: row_ru(D, S, v, part); break;
+    case PH_PL_SPMV: row_cg_spmv(D, S, v, slot, part); break;
+    case PH_CG_YF: row_cg_yf(D, S, v, slot, part); break;
+    case PH_CG_DAD: row_cg_dad(D, S, v, slot, part); break;
+    case PH_RU: row_ru(D, S, v, slot, part); break;
     case PH_EXP_A:
     case PH_EXP_B:
-    case PH_PL_EXP_A: row_exp(D, S, v, part); break;
+    case PH_PL_EXP_A: row_exp(D, S, v, slot, part); break;
     case PH_PROP_A:
     case PH_PROP_B:
-    case PH_PL_PROP_A: row_prop(D, S, v, part); break;
-    case PH_PL_CG: row_pl_cg(D, S, v, part); break;
+    case PH_PL_PROP_A: row_prop(D, S, v, slot, part); break;
+    case PH_PL_CG: row_pl_cg(D, S, v, slot, part); break;
     default: break;
   }
 }
@@ -1616,7 +1616,8 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kern
         continue;
       }
       const int local = item - sD.item_begin;
-      const int v = local * kThreads + threadIdx.x;
+      const int slot = local * kThreads + threadIdx.x;
+      const int v = (slot < sD.nv && sD.A.rowmap) ? ldro(sD.A.rowmap + slot) : slot;
       // Stage A for the FP32 matrix passes when the item's slice fits.
       const bool fp32_pass = sD.prec == PREC_MIXED &&
                              (sS.phase == PH_POW || sS.phase == PH_CG_SPMV ||
@@ -1655,7 +1656,7 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kern
       double part[kPart];
 #pragma unroll
       for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-      if (v < sD.nv) row_op(sD, sS, v, part);
+      if (slot < sD.nv) row_op(sD, sS, v, slot, part);
       const int ns = nslots(sS.phase);
       const bool wmin = sS.phase == PH_PL_SPMV;
       const double r = block_reduce(part, red, ns, wmin);
@@ -1742,11 +1743,14 @@ __device__ __forceinline__ void power_item(const InstDesc *desc, const int *item
   const int phase = sS.phase;
   if (!power_phase(phase)) return;
   const int local = item - sD.item_begin;
-  const int v = local * kThreads + threadIdx.x;
+  const int slot = local * kThreads + threadIdx.x;
   double part[kPart];
 #pragma unroll
   for (int k = 0; k < kPart; ++k) part[k] = 0.0;
-  if (v < sD.nv) row_power(sD, sS, v, part);
+  if (slot < sD.nv) {
+    const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
+    row_power(sD, sS, v, slot, part);
+  }
   const int ns = nslots(phase);
   const double r = block_reduce(part, red, ns, false);
   if (threadIdx.x < ns) sD.part[(size_t)local * kPart + threadIdx.x] = r;
@@ -1892,8 +1896,11 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) cluster_ker
       double part[kPart];
 #pragma unroll
       for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-      const int v = item * kThreads + threadIdx.x;
-      if (v < sD.nv) row_op(sD, sS, v, part);
+      const int slot = item * kThreads + threadIdx.x;
+      if (slot < sD.nv) {
+        const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
+        row_op(sD, sS, v, slot, part);
+      }
       const double r = block_reduce(part, red, ns, wmin);
       if (threadIdx.x < ns || (wmin && threadIdx.x == kMinSlot)) cpart[par][li][threadIdx.x] = r;
     }
@@ -1926,15 +1933,17 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) cluster_ker
 // D^-1 = 1/diag(A) (getDiagonal, MPRGPUtility.h:503-515).
 __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
                                    const int *__restrict__ cols, const double *__restrict__ vals,
-                                   const int *__restrict__ slice_off, int *out_cols,
+                                   const int *__restrict__ slice_off,
+                                   const int *__restrict__ rowmap, int *out_cols,
                                    double *out64, float *out32, double *dinv) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = r >> 5, lane = r & 31;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;  // SELL row (slot)
+  const int s = q >> 5, lane = q & 31;
   const int nslices = (nv + kSlice - 1) / kSlice;
   if (s >= nslices) return;
+  const int r = (q < nv && rowmap) ? rowmap[q] : q;      // its vertex
   const int j0 = slice_off[s], w = slice_off[s + 1] - j0;
-  const int b = (r < nv) ? row_ptr[r] : 0;
-  const int len = (r < nv) ? row_ptr[r + 1] - b : 0;
+  const int b = (q < nv) ? row_ptr[r] : 0;
+  const int len = (q < nv) ? row_ptr[r + 1] - b : 0;
   double dg[3] = {0.0, 0.0, 0.0};
   for (int j = 0; j < w; ++j) {
     const size_t slot = (size_t)(j0 + j);
@@ -1949,7 +1958,7 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
         dg[2] = m[8];
       }
     } else {
-      c = (r < nv) ? r : 0;
+      c = (q < nv) ? r : 0;
       for (int e = 0; e < 9; ++e) m[e] = 0.0;
     }
     out_cols[slot * kSlice + lane] = c;
@@ -1958,7 +1967,7 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
       if (out32) out32[(slot * 9 + e) * kSlice + lane] = (float)m[e];
     }
   }
-  if (r < nv)
+  if (q < nv)
     for (int d = 0; d < 3; ++d) dinv[3 * (size_t)r + d] = 1.0 / dg[d];
 }
 
@@ -1989,11 +1998,12 @@ template <typename VT>
 __global__ void __launch_bounds__(256) spmv_kernel(SellMatrix A, const VT *__restrict__ vals,
                                                    int nv, const double *__restrict__ x,
                                                    double *__restrict__ y) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= nv) return;
+  const int v = A.rowmap ? A.rowmap[slot] : slot;
   double o[3];
-  if constexpr (sizeof(VT) == 4) spmv_row<VT>(A, vals, v, SrcVtoF{x}, o);
-  else spmv_row<VT>(A, vals, v, SrcV{x}, o);
+  if constexpr (sizeof(VT) == 4) spmv_row<VT>(A, vals, slot, SrcVtoF{x}, o);
+  else spmv_row<VT>(A, vals, slot, SrcV{x}, o);
   st3(y, v, o);
 }
 
@@ -2112,12 +2122,12 @@ cudaError_t power_max_blocks_per_sm(int variant, int *n) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel_fn(variant), kThreads, 0);
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
-                        const int *slice_off, int *out_cols, double *out64, float *out32,
-                        double *dinv, cudaStream_t st) {
+                        const int *slice_off, const int *rowmap, int *out_cols, double *out64,
+                        float *out32, double *dinv, cudaStream_t st) {
   const int nslices = (nv + kSlice - 1) / kSlice;
   const int threads = nslices * kSlice;
   bsr_to_sell_kernel<<<(threads + 255) / 256, 256, 0, st>>>(nv, row_ptr, cols, vals, slice_off,
-                                                            out_cols, out64, out32, dinv);
+                                                            rowmap, out_cols, out64, out32, dinv);
 }
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st) {

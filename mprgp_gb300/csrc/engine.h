@@ -65,7 +65,10 @@ enum Phase : int {
 };
 
 // SELL-32 copy of a 3x3-block CSR matrix: slices of 32 block rows; slot j of
-// slice s holds, for lanes t = 0..31, one block per row.  cols[(off+j)*32+t]
+// slice s holds, for lanes t = 0..31, one block per row.  The rows are laid
+// out in `rowmap` order (a performance layout: vertices with several
+// constraint planes are grouped after the others, so the warps that run the
+// multi-plane projection are few and uniform); vectors stay in vertex order.  cols[(off+j)*32+t]
 // and vals[((off+j)*9+e)*32+t] with e the row-major entry of the block, so a
 // warp reads each of the nine entries as one coalesced 256 B (FP64) line.
 struct SellMatrix {
@@ -74,6 +77,7 @@ struct SellMatrix {
   const int *cols;       // vertex index; padding points at a valid row, value 0
   const double *v64;
   const float *v32;
+  const int *rowmap;     // SELL row (slot) -> vertex; nullptr: slot == vertex
 };
 
 struct InstState {

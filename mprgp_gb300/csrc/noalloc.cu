@@ -40,7 +40,8 @@ namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
-                        const int *slice_off, int *out_cols, double *out64, float *out32,
+                        const int *slice_off, const int *rowmap, int *out_cols, double *out64,
+                        float *out32,
                         double *dinv, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st);
@@ -219,7 +220,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
 
   // A -> SELL-32 (+ D^-1), planes -> (n, c) rows, x -> X0; zero what counts.
   NCK(cudaMemcpyAsync(d_soff, off.data(), sizeof(int) * (nslices + 1), cudaMemcpyHostToDevice, s));
-  launch_bsr_to_sell(nv, row_ptr, cols, vals, d_soff, d_cols, d_v64, d_v32, d_dinv, s);
+  launch_bsr_to_sell(nv, row_ptr, cols, vals, d_soff, nullptr, d_cols, d_v64, d_v32, d_dinv, s);
   NCK(cudaGetLastError());
   if (m > 0) {
     launch_planes_setup(nv, plane_ptr, planes, d_pl, d_nn, d_indn, d_dinv, s);
@@ -235,6 +236,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   D.A.cols = d_cols;
   D.A.v64 = d_v64;
   D.A.v32 = d_v32;
+  D.A.rowmap = nullptr;
   D.nv = nv;
   D.nitems = nitems;
   D.item_begin = 0;

@@ -353,3 +353,35 @@ def test_autotune_pick_is_result_invariant(tmp_path, monkeypatch):
         assert r2["cached"] and r2["config"] == r["config"]
     finally:
         c.close()
+
+
+def test_relayout_when_planes_change(ctx):
+    """The SELL row order groups vertices with several planes; changing the
+    planes after the matrix rebuilds it, and the solve equals that of a
+    problem loaded with the final planes from the start."""
+    corner = M.beam(7, 6, 12, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=31)
+    floor = M.beam(7, 6, 12, extra_planes_max=0, extra_planes_min=0, plane_mode=2, seed=31)
+    assert np.array_equal(corner.vals, floor.vals)
+    opt = M.default_options(tol=1e-10 * np.linalg.norm(corner.b), max_it=20000,
+                            kind=M.KIND_PLANES, project_x0=1, seed=SEED, precision=M.PREC_MIXED)
+    pr = M.load_beam(ctx, floor, precisions=3)        # identity layout (one plane each)
+    pr.set_planes(corner.plane_ptr, corner.planes)    # walls: multi-plane rows regrouped
+    pr.set_rhs(corner.b)
+    pr.set_x(corner.x0)
+    st = pr.solve(opt)
+    x_re = pr.get_x()
+    pr.close()
+    fresh = M.load_beam(ctx, corner, precisions=3)
+    st2 = fresh.solve(opt)
+    assert st.code == 0 and st2.code == 0
+    assert np.array_equal(x_re, fresh.get_x())
+    # and the standalone product follows the layout
+    import torch
+    xd = torch.from_numpy(np.random.default_rng(5).standard_normal(corner.n)).cuda()
+    yd = torch.zeros(corner.n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    fresh.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_FP64)
+    ctx.sync()
+    A, _, _, _ = H.qp_from_beam(corner)
+    assert rel(yd.cpu().numpy(), A.matvec(xd.cpu().numpy())) < 1e-14
+    fresh.close()
