@@ -169,10 +169,12 @@ void free_problem_arrays(mprgp_problem *p) {
   dfree(p->ctx, p->rowmap);
 }
 
-// The SELL row order of a problem: vertices with at most one constraint
-// plane first, those with several after them (stable), so that the
-// multi-plane projection runs in few, uniform warps.  Identity when no
-// vertex has several planes.  The key identifies the order.
+// The SELL row order of a problem: vertices with several constraint planes
+// are gathered into whole warps (slices of 32 rows), and those slices are
+// spread evenly over the matrix, so that the multi-plane projection runs in
+// few, uniform warps whose extra work is shared by all SMs; the other
+// vertices keep their order.  Identity when no vertex has several planes.
+// The key identifies the order.
 unsigned long long layout_key(const mprgp_problem *p) {
   unsigned long long h = 1469598103934665603ull;
   if (p->cons != 1 || p->h_plane_ptr.empty()) return h;
@@ -191,14 +193,27 @@ int build_layout(mprgp_problem *p, unsigned long long key) {
   const int nv = p->nv;
   std::vector<int> order;  // slot -> vertex
   if (p->cons == 1 && !p->h_plane_ptr.empty()) {
-    std::vector<int> multi;
-    order.reserve(nv);
+    std::vector<int> multi, single;
     for (int v = 0; v < nv; ++v) {
       if (p->h_plane_ptr[v + 1] - p->h_plane_ptr[v] >= 2) multi.push_back(v);
-      else order.push_back(v);
+      else single.push_back(v);
     }
-    if (multi.empty()) order.clear();
-    else order.insert(order.end(), multi.begin(), multi.end());
+    if (!multi.empty()) {
+      const long long nsl = p->nslices;
+      const long long heavy = ((long long)multi.size() + kSlice - 1) / kSlice;
+      std::vector<char> is_heavy(nsl, 0);
+      for (long long h = 0; h < heavy; ++h)
+        is_heavy[std::min(nsl - 1, (2 * h + 1) * nsl / (2 * heavy))] = 1;
+      order.reserve(nv);
+      size_t im = 0, is = 0;
+      for (long long sl = 0; sl < nsl; ++sl) {
+        const int cap = (int)std::min<long long>(kSlice, nv - sl * kSlice);
+        for (int t = 0; t < cap; ++t) {
+          const bool want_multi = is_heavy[sl] ? im < multi.size() : is >= single.size();
+          order.push_back(want_multi ? multi[im++] : single[is++]);
+        }
+      }
+    }
   }
   const bool ident = order.empty();
   std::vector<int> off(p->nslices + 1, 0);
