@@ -1508,23 +1508,45 @@ __device__ __forceinline__ int nslots(int phase) {
   }
 }
 
-// Block-reduce the first `ns` slots of part[] (and the min slot when
-// `with_min`) in a fixed order; thread k gets slot k.
-__device__ double block_reduce(double *part, double (*red)[kThreads / 32], int ns, bool with_min) {
+// Block reduction of the first `ns` slots of part[] (and the min slot when
+// `with_min`; at most kRedSlots slots in all), in a fixed order: every
+// thread's values go to shared memory; warp w reduces slot w -- lane l takes
+// the values of threads l, l+32, ..., l+224 in that order, then a 5-level
+// shuffle tree -- and thread k gets slot k.  One warp per slot keeps the FP64
+// work at about a dozen warp instructions per slot (GB300 issues FP64 warp
+// instructions slowly), against five per warp and slot for a shuffle tree in
+// every warp.
+constexpr int kRedSlots = 8;
+struct RedBuf {
+  double v[kRedSlots][kThreads];
+  double out[kRedSlots];
+};
+
+__device__ double block_reduce(double *part, RedBuf &red, int ns, bool with_min) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < kPart; ++k) {
     if (k == kMinSlot ? !with_min : k >= ns) continue;
-    const double v = (k == kMinSlot) ? warp_min(part[k]) : warp_sum(part[k]);
-    if (lane == 0) red[k][warp] = v;
+    red.v[k == kMinSlot ? ns : k][threadIdx.x] = part[k];
+  }
+  __syncthreads();
+  const int nrows = ns + (with_min ? 1 : 0);
+  if (warp < nrows) {
+    const bool is_min = with_min && warp == ns;
+    const double *src = red.v[warp];
+    double acc = src[lane];
+#pragma unroll
+    for (int i = 1; i < kThreads / 32; ++i) {
+      const double x = src[lane + 32 * i];
+      acc = is_min ? fmin(acc, x) : acc + x;
+    }
+    acc = is_min ? warp_min(acc) : warp_sum(acc);
+    if (lane == 0) red.out[warp] = acc;
   }
   __syncthreads();
   double r = 0.0;
-  if (threadIdx.x < kPart && (threadIdx.x < ns || (threadIdx.x == kMinSlot && with_min))) {
-    const int k = threadIdx.x;
-    r = red[k][0];
-    for (int w = 1; w < kThreads / 32; ++w) r = (k == kMinSlot) ? fmin(r, red[k][w]) : r + red[k][w];
-  }
+  if (threadIdx.x < ns) r = red.out[threadIdx.x];
+  else if (with_min && threadIdx.x == kMinSlot) r = red.out[ns];
   __syncthreads();
   return r;
 }
@@ -1578,7 +1600,7 @@ __device__ __forceinline__ int find_instance(const int *prefix, int n, int item)
 __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kernel(EngineArgs args) {
   __shared__ InstDesc sD;
   __shared__ InstState sS;
-  __shared__ double red[kPart][kThreads / 32];
+  __shared__ RedBuf red;
   __shared__ double sums[kPart];
   __shared__ int s_last;
   Ctl *ctl = args.ctl;
@@ -1724,7 +1746,7 @@ __device__ __forceinline__ void power_item(const InstDesc *desc, const int *item
                                            int ninst, int item, PowCtl *pc,
                                            cudaGraphConditionalHandle h, int signal,
                                            InstDesc &sD, InstState &sS,
-                                           double (&red)[kPart][kThreads / 32],
+                                           RedBuf &red,
                                            double (&sums)[kPart], int &s_last) {
   const int inst = find_instance(item_prefix, ninst, item);
   __syncthreads();  // the previous item's readers of sD/sS are done
@@ -1804,7 +1826,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                  int signal) {
   __shared__ InstDesc sD;
   __shared__ InstState sS;
-  __shared__ double red[kPart][kThreads / 32];
+  __shared__ RedBuf red;
   __shared__ double sums[kPart];
   __shared__ int s_last;
   if (*(volatile unsigned int *)&pc->stop) return;  // written by an earlier launch
@@ -1863,7 +1885,7 @@ __device__ __forceinline__ double ld_dsmem(unsigned int addr) {
 __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) cluster_kernel(ClusterArgs args) {
   __shared__ InstDesc sD;
   __shared__ InstState sS;
-  __shared__ double red[kPart][kThreads / 32];
+  __shared__ RedBuf red;
   __shared__ double sums[kPart];
   __shared__ __align__(8) double cpart[2][kClusterItems][kPart];
   const unsigned int rank = cluster_rank(), csize = cluster_size();
