@@ -17,8 +17,9 @@ the tuner checks that for the setting it picks.
 
 The tuner times batched solves of a sample of the workload (device time of
 the solver runs, best of `reps`), walks the knobs one at a time from the
-default (coordinate descent), and caches the winner per device and workload
-signature (JSON; MPRGP_TUNING_CACHE overrides the path).
+default (coordinate descent; the power form and register budget together),
+and caches the winner per device and workload signature (JSON;
+MPRGP_TUNING_CACHE overrides the path).
 """
 from __future__ import annotations
 
@@ -130,9 +131,16 @@ def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5
         best = dict(DEFAULT)
         best_ms, ref_x = run(best)
         default_ms = best_ms
-        for knob in ("cluster", "power", "power_regs", "ctas_per_sm", "stage"):
-            for v in SPACE[knob]:
-                cand = dict(best, **{knob: v})
+        # coordinate descent; the power form and the power kernel's register
+        # budget interact, so they are searched together
+        steps = [[{"cluster": v} for v in SPACE["cluster"]],
+                 [{"power": f, "power_regs": r} for f in SPACE["power"]
+                  for r in (SPACE["power_regs"] if f != "engine" else [40])],
+                 [{"ctas_per_sm": v} for v in SPACE["ctas_per_sm"]],
+                 [{"stage": v} for v in SPACE["stage"]]]
+        for step in steps:
+            for change in step:
+                cand = dict(best, **change)
                 try:
                     ms, _ = run(cand)
                 except Exception:  # a shape the device does not offer

@@ -25,6 +25,9 @@ namespace mprgp {
 constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:9)
 
 // Resident CTAs per SM the engine is compiled for (register budget).
+#ifndef MPRGP_SPMV_CHUNK
+#define MPRGP_SPMV_CHUNK 4
+#endif
 #ifndef MPRGP_ENGINE_MIN_BLOCKS
 #define MPRGP_ENGINE_MIN_BLOCKS 4
 #endif
@@ -208,27 +211,69 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
   const int s = v >> 5, lane = v & 31;
   const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
   VT a0 = 0, a1 = 0, a2 = 0;
-  // Columns of 8 slots are fetched together so that the neighbour gathers
-  // and block loads of those slots are all in flight at once.
-  for (int jb = j0; jb < j1; jb += 8) {
-    int c[8];
+  // Every slot below j1 is valid (padding blocks are zero and point at a
+  // real row), so whole chunks of MPRGP_SPMV_CHUNK slots carry no per-slot
+  // condition and all their column, value and neighbour loads can be in
+  // flight together (0: columns of 8 slots fetched together, then one slot
+  // at a time).  The products are accumulated slot by slot in order either
+  // way, so the results are the same.
+  int jb = j0;
+#if MPRGP_SPMV_CHUNK == 0
+  for (; jb < j1; jb += 8) {
+    int cc[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) c[u] = (jb + u < j1) ? ldro(A.cols + (size_t)(jb + u) * kSlice + lane) : -1;
+    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? ldro(A.cols + (size_t)(jb + u) * kSlice + lane) : -1;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      if (c[u] < 0) break;
+      if (cc[u] < 0) break;
       const VT *q = vals + (size_t)(jb + u) * (9 * kSlice) + lane;
       const VT m0 = ldro(q), m1 = ldro(q + 32), m2 = ldro(q + 64);
       const VT m3 = ldro(q + 96), m4 = ldro(q + 128), m5 = ldro(q + 160);
       const VT m6 = ldro(q + 192), m7 = ldro(q + 224), m8 = ldro(q + 256);
       VT xv[3];
-      src(c[u], xv);
-      const VT x0 = xv[0], x1 = xv[1], x2 = xv[2];
-      a0 = fma(m0, x0, a0); a0 = fma(m1, x1, a0); a0 = fma(m2, x2, a0);
-      a1 = fma(m3, x0, a1); a1 = fma(m4, x1, a1); a1 = fma(m5, x2, a1);
-      a2 = fma(m6, x0, a2); a2 = fma(m7, x1, a2); a2 = fma(m8, x2, a2);
+      src(cc[u], xv);
+      a0 = fma(m0, xv[0], a0); a0 = fma(m1, xv[1], a0); a0 = fma(m2, xv[2], a0);
+      a1 = fma(m3, xv[0], a1); a1 = fma(m4, xv[1], a1); a1 = fma(m5, xv[2], a1);
+      a2 = fma(m6, xv[0], a2); a2 = fma(m7, xv[1], a2); a2 = fma(m8, xv[2], a2);
     }
   }
+#else
+  for (; jb + MPRGP_SPMV_CHUNK <= j1; jb += MPRGP_SPMV_CHUNK) {
+    constexpr int K = MPRGP_SPMV_CHUNK;
+    int c[K];
+#pragma unroll
+    for (int u = 0; u < K; ++u) c[u] = ldro(A.cols + (size_t)(jb + u) * kSlice + lane);
+    VT m[K][9];
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+      const VT *q = vals + (size_t)(jb + u) * (9 * kSlice) + lane;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) m[u][e] = ldro(q + 32 * e);
+    }
+    VT xv[K][3];
+#pragma unroll
+    for (int u = 0; u < K; ++u) src(c[u], xv[u]);
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+      const VT x0 = xv[u][0], x1 = xv[u][1], x2 = xv[u][2];
+      a0 = fma(m[u][0], x0, a0); a0 = fma(m[u][1], x1, a0); a0 = fma(m[u][2], x2, a0);
+      a1 = fma(m[u][3], x0, a1); a1 = fma(m[u][4], x1, a1); a1 = fma(m[u][5], x2, a1);
+      a2 = fma(m[u][6], x0, a2); a2 = fma(m[u][7], x1, a2); a2 = fma(m[u][8], x2, a2);
+    }
+  }
+  for (; jb < j1; ++jb) {  // the last slots of the row
+    const int c = ldro(A.cols + (size_t)jb * kSlice + lane);
+    const VT *q = vals + (size_t)jb * (9 * kSlice) + lane;
+    VT m[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) m[e] = ldro(q + 32 * e);
+    VT xv[3];
+    src(c, xv);
+    a0 = fma(m[0], xv[0], a0); a0 = fma(m[1], xv[1], a0); a0 = fma(m[2], xv[2], a0);
+    a1 = fma(m[3], xv[0], a1); a1 = fma(m[4], xv[1], a1); a1 = fma(m[5], xv[2], a1);
+    a2 = fma(m[6], xv[0], a2); a2 = fma(m[7], xv[1], a2); a2 = fma(m[8], xv[2], a2);
+  }
+#endif
   out[0] = (OT)a0;
   out[1] = (OT)a1;
   out[2] = (OT)a2;
