@@ -292,6 +292,35 @@ int mprgp_beam_sizes(const mprgp_beam_params *p, int *nv, int *nnzb, int *nplane
  * on the upper hemisphere) on the vertices within plane_band of it. */
 int mprgp_beam_build(const mprgp_beam_params *p, int *row_ptr, int *cols, double *vals,
                      double *b, double *x0, int *plane_ptr, double *planes);
+/* The beam's tetrahedral mesh: tets[4 * 6abc] (vertex ids, the six Kuhn
+ * tets of each cube), rest shape X[3 nv], and optionally the initial
+ * positions x0[3 nv] and velocities v0[3 nv] that mprgp_beam_build uses. */
+int mprgp_beam_mesh(const mprgp_beam_params *p, int *tets, double *X, double *x0, double *v0);
+
+/* ---- FEM assembly on the GPU ------------------------------------------- */
+/* The system the reference's FEM driver builds before each solve
+ * (MprgpFemSolver.cpp:315-356, FEMSystem::buildSystem FEMSystem.cpp:167-193)
+ * for a linear material (FEMEnergy.cpp:657) and lumped mass
+ * (FEMMesh.cpp:501-511):  A = M + h^2 K,  b = M (x + h v) + h^2 M g + h^2 K X.
+ * mprgp_fem_create builds the block pattern (host, once per mesh) and the
+ * per-tet geometry (device) from tets[4 ntet] and the rest shape X[3 nv];
+ * mprgp_fem_assemble computes A and b on the device (one thread per block
+ * row, deterministic) and loads them into `prob` (matrix with `precisions`,
+ * right-hand side); mprgp_fem_rhs recomputes only b for a later timestep.
+ * x, v: current positions and velocities (host, or device with
+ * on_device = 1; v may be NULL).  mprgp_fem_get copies the last assembly
+ * (row_ptr[nv+1], cols[nnzb], vals[9 nnzb], b[3 nv], mass[nv]) to the host. */
+typedef struct mprgp_fem mprgp_fem;
+int mprgp_fem_create(mprgp_context *ctx, int nv, int ntet, const int *tets, const double *X,
+                     double young, double poisson, double rho, mprgp_fem **out);
+int mprgp_fem_destroy(mprgp_fem *fem);
+int mprgp_fem_sizes(mprgp_fem *fem, int *nv, int *nnzb);
+int mprgp_fem_assemble(mprgp_fem *fem, double h, const double gravity[3], const double *x,
+                       const double *v, int on_device, mprgp_problem *prob, int precisions);
+int mprgp_fem_rhs(mprgp_fem *fem, double h, const double gravity[3], const double *x,
+                  const double *v, int on_device, mprgp_problem *prob);
+int mprgp_fem_get(mprgp_fem *fem, int *row_ptr, int *cols, double *vals, double *b,
+                  double *mass);
 
 #ifdef __cplusplus
 }

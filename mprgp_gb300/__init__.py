@@ -117,6 +117,14 @@ def _sig(lib):
       C.POINTER(C.c_double))
     s("mprgp_server_result", C.c_int, _P, C.c_longlong, _P, _P, C.POINTER(Stats), _P, _IP)
     s("mprgp_server_info", C.c_int, _P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), _IP)
+    s("mprgp_beam_mesh", C.c_int, C.POINTER(BeamParams), _P, _P, _P, _P)
+    s("mprgp_fem_create", C.c_int, _P, C.c_int, C.c_int, _P, _P, C.c_double, C.c_double,
+      C.c_double, C.POINTER(_P))
+    s("mprgp_fem_destroy", C.c_int, _P)
+    s("mprgp_fem_sizes", C.c_int, _P, _IP, _IP)
+    s("mprgp_fem_assemble", C.c_int, _P, C.c_double, _P, _P, _P, C.c_int, _P, C.c_int)
+    s("mprgp_fem_rhs", C.c_int, _P, C.c_double, _P, _P, _P, C.c_int, _P)
+    s("mprgp_fem_get", C.c_int, _P, _P, _P, _P, _P, _P)
     s("mprgp_beam_default", None, C.POINTER(BeamParams))
     s("mprgp_beam_sizes", C.c_int, C.POINTER(BeamParams), _IP, _IP, _IP)
     s("mprgp_beam_build", C.c_int, C.POINTER(BeamParams), _P, _P, _P, _P, _P, _P, _P)
@@ -216,6 +224,76 @@ def beam(a: int, b: int, c: int, **kw) -> BeamQP:
                               _ptr(x0), _ptr(pptr), _ptr(planes)), "beam_build")
     params = {k: getattr(p, k) for k, _ in BeamParams._fields_}
     return BeamQP(nv, row_ptr, cols, vals, rhs, x0, pptr, planes, params)
+
+
+def beam_mesh(a: int, b: int, c: int, **kw):
+    """The tetrahedral mesh behind beam(a, b, c, **kw): (tets (6abc, 4) int32,
+    rest shape X, initial positions x0, initial velocities v0), each 3 nv."""
+    L = lib()
+    p = BeamParams()
+    L.mprgp_beam_default(C.byref(p))
+    p.a, p.b, p.c = a, b, c
+    _set_fields(p, kw)
+    nv = (a + 1) * (b + 1) * (c + 1)
+    tets = np.zeros((6 * a * b * c, 4), np.int32)
+    X, x0, v0 = np.zeros(3 * nv), np.zeros(3 * nv), np.zeros(3 * nv)
+    _check(L.mprgp_beam_mesh(C.byref(p), _ptr(tets), _ptr(X), _ptr(x0), _ptr(v0)), "beam_mesh")
+    return tets, X, x0, v0
+
+
+class FemMesh:
+    """GPU assembly of A = M + h^2 K and b for a tetrahedral mesh (mprgp_fem_*)."""
+
+    def __init__(self, ctx, tets, X, young, poisson, rho):
+        self.ctx = ctx
+        tets = np.ascontiguousarray(tets, np.int32)
+        X = np.ascontiguousarray(X, np.float64)
+        self.nv = X.size // 3
+        self.h = C.c_void_p()
+        _check(lib().mprgp_fem_create(ctx.h, self.nv, tets.shape[0], _ptr(tets), _ptr(X), young,
+                                      poisson, rho, C.byref(self.h)), "fem_create")
+        n, nnzb = C.c_int(), C.c_int()
+        _check(lib().mprgp_fem_sizes(self.h, C.byref(n), C.byref(nnzb)), "fem_sizes")
+        self.nnzb = nnzb.value
+
+    def close(self):
+        if self.h:
+            lib().mprgp_fem_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def assemble(self, h, gravity, x, v=None, prob=None, precisions=1):
+        """A and b on the device; with `prob`, loaded into it."""
+        g = np.ascontiguousarray(gravity, np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        v = None if v is None else np.ascontiguousarray(v, np.float64)
+        _check(lib().mprgp_fem_assemble(self.h, h, _ptr(g), _ptr(x), _ptr(v), 0,
+                                        prob.h if prob is not None else None, precisions),
+               "fem_assemble")
+
+    def rhs(self, h, gravity, x, v=None, prob=None):
+        """b only (A unchanged), for a later timestep."""
+        g = np.ascontiguousarray(gravity, np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        v = None if v is None else np.ascontiguousarray(v, np.float64)
+        _check(lib().mprgp_fem_rhs(self.h, h, _ptr(g), _ptr(x), _ptr(v), 0,
+                                   prob.h if prob is not None else None), "fem_rhs")
+
+    def get(self):
+        """(row_ptr, cols, vals (nnzb, 9), b, mass) of the last assembly."""
+        rp = np.zeros(self.nv + 1, np.int32)
+        cols = np.zeros(self.nnzb, np.int32)
+        vals = np.zeros((self.nnzb, 9))
+        b = np.zeros(3 * self.nv)
+        mass = np.zeros(self.nv)
+        _check(lib().mprgp_fem_get(self.h, _ptr(rp), _ptr(cols), _ptr(vals), _ptr(b), _ptr(mass)),
+               "fem_get")
+        return rp, cols, vals, b, mass
 
 
 # ------------------------------------------------------------- contexts --

@@ -202,6 +202,33 @@ int mprgp_beam_sizes(const mprgp_beam_params *p, int *nv, int *nnzb, int *nplane
   return MPRGP_OK;
 }
 
+int mprgp_beam_mesh(const mprgp_beam_params *p, int *tets, double *X, double *x0, double *v0) {
+  if (!valid(p) || !tets || !X) return MPRGP_INVALID;
+  const Grid G(*p);
+  static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  long long t4 = 0;
+  for (int k = 0; k < p->c; ++k)
+    for (int j = 0; j < p->b; ++j)
+      for (int i = 0; i < p->a; ++i)
+        for (int t = 0; t < 6; ++t) {
+          int o[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {1, 1, 1}};
+          o[1][perm[t][0]] = 1;
+          o[2][perm[t][0]] = 1;
+          o[2][perm[t][1]] = 1;
+          for (int a = 0; a < 4; ++a) tets[t4++] = G.id(i + o[a][0], j + o[a][1], k + o[a][2]);
+        }
+  for (int v = 0; v < G.nv; ++v) {
+    const int i = v % G.nx, j = (v / G.nx) % G.ny, k = v / (G.nx * G.ny);
+    for (int d = 0; d < 3; ++d) {
+      const long long q = 3LL * v + d;
+      X[q] = (d == 0 ? i : d == 1 ? j : k) * p->edge;
+      if (x0) x0[q] = X[q] + (d == 1 ? -p->lift : 0.0);
+      if (v0) v0[q] = p->v0_sigma * gauss(p->seed, 7, (uint64_t)q);
+    }
+  }
+  return MPRGP_OK;
+}
+
 int mprgp_beam_build(const mprgp_beam_params *p, int *row_ptr, int *cols, double *vals,
                      double *b, double *x0, int *plane_ptr, double *planes) {
   if (!valid(p) || !row_ptr || !cols || !vals || !b || !x0) return MPRGP_INVALID;

@@ -100,3 +100,45 @@ def test_context_without_gpu_fails_loudly(lib_built):
     with pytest.raises(M.MPRGPError) as ei:
         M.Context(0)
     assert ei.value.code == M.NO_DEVICE
+
+
+def test_beam_mesh_and_numpy_fem_assembly():
+    """The exported mesh reproduces the generator's system: a numpy assembly
+    of A = M + h^2 K (linear material as FEMEnergy.cpp:657, Lame parameters
+    as FEMEnergy.cpp:383-384, lumped mass rho V / 4 as FEMMesh.cpp:501-511)
+    and b = M (x0 + h v0) + h^2 M g + h^2 K X from tets and X equals
+    mprgp_beam_build's."""
+    kw = dict(extra_planes_max=1, extra_planes_min=1, plane_mode=2, seed=17)
+    qp = M.beam(2, 3, 4, **kw)
+    tets, X, x0, v0 = M.beam_mesh(2, 3, 4, **kw)
+    p = qp.params
+    nv = qp.nv
+    assert tets.shape == (6 * 2 * 3 * 4, 4) and tets.min() >= 0 and tets.max() < nv
+    assert np.array_equal(x0, qp.x0)
+    E, nu, rho, h = p["young"], p["poisson"], p["rho"], p["dt"]
+    lam, mu = nu * E / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    K = np.zeros((3 * nv, 3 * nv))
+    mass = np.zeros(nv)
+    Xv = X.reshape(-1, 3)
+    for t in tets:
+        Dm = (Xv[t[1:]] - Xv[t[0]]).T
+        V = abs(np.linalg.det(Dm)) / 6.0
+        assert V > 0
+        inv = np.linalg.inv(Dm)
+        gN = np.vstack([-inv.sum(axis=0), inv])
+        for a in range(4):
+            mass[t[a]] += rho * V / 4
+            for b_ in range(4):
+                Kab = V * (lam * np.outer(gN[a], gN[b_]) + mu * np.outer(gN[b_], gN[a]) +
+                           mu * gN[a].dot(gN[b_]) * np.eye(3))
+                K[3 * t[a]:3 * t[a] + 3, 3 * t[b_]:3 * t[b_] + 3] += Kab
+    A = np.diag(np.repeat(mass, 3)) + h * h * K
+    g = np.tile([0.0, p["gravity"], 0.0], nv)
+    m3 = np.repeat(mass, 3)
+    b = m3 * (x0 + h * v0) + h * h * m3 * g + h * h * K.dot(X)
+    ptr, idx, val = M.bsr_to_csr(nv, qp.row_ptr, qp.cols, qp.vals)
+    Ad = np.zeros_like(A)
+    for r in range(3 * nv):
+        Ad[r, idx[ptr[r]:ptr[r + 1]]] = val[ptr[r]:ptr[r + 1]]
+    assert np.abs(Ad - A).max() <= 1e-12 * np.abs(A).max()
+    assert np.linalg.norm(b - qp.b) <= 1e-12 * np.linalg.norm(b)
