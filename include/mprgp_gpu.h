@@ -157,6 +157,10 @@ int mprgp_problem_get_x(mprgp_problem *prob, double *x, int on_device);
 /* face codes as the reference's projector.getFace(): one per constraint row
  * (planes, in plane_ptr order) or one per unknown (bounds). */
 int mprgp_problem_num_constraints(mprgp_problem *prob, int *m);
+int mprgp_problem_num_vertices(mprgp_problem *prob, int *nv);
+/* The plane constraints as set: plane_ptr[nv+1] and planes[4 m] in the
+ * (n, p) form (host arrays). */
+int mprgp_problem_get_planes(mprgp_problem *prob, int *plane_ptr, double *planes);
 int mprgp_problem_get_face(mprgp_problem *prob, unsigned char *face);
 /* Power-method reuse (on by default): a solve whose power method starts from
  * the seeded random vector (no stored start vector in use) reuses the result
@@ -296,6 +300,21 @@ int mprgp_beam_build(const mprgp_beam_params *p, int *row_ptr, int *cols, double
  * tets of each cube), rest shape X[3 nv], and optionally the initial
  * positions x0[3 nv] and velocities v0[3 nv] that mprgp_beam_build uses. */
 int mprgp_beam_mesh(const mprgp_beam_params *p, int *tets, double *X, double *x0, double *v0);
+
+/* ---- plane-constraint generation on the GPU ---------------------------- */
+/* The proximity query of LinearConCollider::handle(body, plane, delta)
+ * (LinearConCollider.cpp:140-161) for planes[4 nplanes] = (n, p), |n| = 1,
+ * in order: plane q becomes a constraint of vertex v when n.x_v + p - delta
+ * <= 0, unless v already holds a plane within 1e-4 of it in (n, p)
+ * (addConPlane, LinearConCollider.cpp:43-56); with decoupled = 1 only the
+ * first such plane of a vertex (LinearConCollider.cpp:153-158).  x: vertex
+ * positions (3 nv; host, or device with on_device = 1; NULL = the problem's
+ * current x).  The lists replace the problem's constraints
+ * (mprgp_problem_set_planes); a vertex that would need more than 3 planes
+ * is an MPRGP_INVALID error.  *num_constraints receives the total. */
+int mprgp_planes_collide(mprgp_context *ctx, mprgp_problem *prob, const double *x, int on_device,
+                         int nplanes, const double *planes, double delta, int decoupled,
+                         int *num_constraints);
 
 /* ---- FEM assembly on the GPU ------------------------------------------- */
 /* The system the reference's FEM driver builds before each solve

@@ -118,6 +118,9 @@ def _sig(lib):
     s("mprgp_server_result", C.c_int, _P, C.c_longlong, _P, _P, C.POINTER(Stats), _P, _IP)
     s("mprgp_server_info", C.c_int, _P, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), _IP)
     s("mprgp_beam_mesh", C.c_int, C.POINTER(BeamParams), _P, _P, _P, _P)
+    s("mprgp_problem_num_vertices", C.c_int, _P, _IP)
+    s("mprgp_problem_get_planes", C.c_int, _P, _P, _P)
+    s("mprgp_planes_collide", C.c_int, _P, _P, _P, C.c_int, C.c_int, _P, C.c_double, C.c_int, _IP)
     s("mprgp_fem_create", C.c_int, _P, C.c_int, C.c_int, _P, _P, C.c_double, C.c_double,
       C.c_double, C.POINTER(_P))
     s("mprgp_fem_destroy", C.c_int, _P)
@@ -426,6 +429,26 @@ class Problem:
         f = np.zeros(max(m.value, 1), np.uint8)
         _check(lib().mprgp_problem_get_face(self.h, _ptr(f)), "get_face")
         return f[:m.value]
+
+    def get_planes(self):
+        """(plane_ptr, planes (m, 4)) as set, in the (n, p) form."""
+        m = C.c_int()
+        _check(lib().mprgp_problem_num_constraints(self.h, C.byref(m)), "num_constraints")
+        ptr = np.zeros(self.nv + 1, np.int32)
+        planes = np.zeros((max(m.value, 1), 4))
+        _check(lib().mprgp_problem_get_planes(self.h, _ptr(ptr), _ptr(planes)), "get_planes")
+        return ptr, planes[:m.value]
+
+    def collide_planes(self, planes, delta, decoupled=False, x=None) -> int:
+        """Replaces the constraints by the planes (n, p) within `delta` of the
+        vertices at x (default: the problem's current x); returns their count."""
+        pl = np.ascontiguousarray(planes, np.float64).reshape(-1, 4)
+        xx = None if x is None else np.ascontiguousarray(x, np.float64)
+        m = C.c_int()
+        _check(lib().mprgp_planes_collide(self.ctx.h, self.h, _ptr(xx), 0, pl.shape[0], _ptr(pl),
+                                          delta, int(bool(decoupled)), C.byref(m)),
+               "planes_collide")
+        return m.value
 
     def set_power_cache(self, enable: bool):
         _check(lib().mprgp_problem_set_power_cache(self.h, int(bool(enable))), "set_power_cache")

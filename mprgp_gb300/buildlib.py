@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmprgp_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "server.cu", "fem.cu", "beam.cpp"]
+SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "server.cu", "fem.cu", "planes.cu", "beam.cpp"]
 
 
 def nvcc() -> str:

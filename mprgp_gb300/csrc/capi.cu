@@ -1026,6 +1026,23 @@ int mprgp_problem_get_x(mprgp_problem *p, double *x, int on_device) {
   return MPRGP_OK;
 }
 
+int mprgp_problem_num_vertices(mprgp_problem *p, int *nv) {
+  if (!p || !nv) return fail(MPRGP_INVALID, "num_vertices");
+  *nv = p->nv;
+  return MPRGP_OK;
+}
+
+int mprgp_problem_get_planes(mprgp_problem *p, int *plane_ptr, double *planes) {
+  if (!p || p->cons != 1) return fail(MPRGP_INVALID, "get_planes: no planes set");
+  if (plane_ptr) std::copy(p->h_plane_ptr.begin(), p->h_plane_ptr.end(), plane_ptr);
+  if (planes && p->m > 0) {
+    CK(cudaMemcpyAsync(planes, p->planes_raw, sizeof(double) * 4 * (size_t)p->m,
+                       cudaMemcpyDeviceToHost, p->ctx->stream));
+    CK(cudaStreamSynchronize(p->ctx->stream));
+  }
+  return MPRGP_OK;
+}
+
 int mprgp_problem_num_constraints(mprgp_problem *p, int *m) {
   if (!p || !m) return fail(MPRGP_INVALID, "num_constraints");
   *m = p->face_len;

@@ -200,3 +200,41 @@ def oracle_get_trace() -> np.ndarray:
     out = np.zeros((max(n, 1), 4))
     O.oracle_get_trace(ptr(out), n)
     return out[:n]
+
+
+def collide_planes(x, planes, delta, decoupled=False):
+    """CPU restatement of LinearConCollider::handle(body, plane, delta)
+    (LinearConCollider.cpp:140-161) over a list of planes, with
+    GeomConCache::addConPlane's 1e-4 duplicate test (:43-56) and the
+    decoupled one-plane-per-vertex rule (:153-158).  Expressions are
+    evaluated left to right in plain FP64.  Returns (plane_ptr, planes)."""
+    import math
+    nv = len(x) // 3
+    ptr, out = [0], []
+    for v in range(nv):
+        xv = [float(x[3 * v]), float(x[3 * v + 1]), float(x[3 * v + 2])]
+        mine = []
+        for pl in planes:
+            pl = [float(t) for t in pl]
+            s = pl[0] * xv[0]
+            s = s + pl[1] * xv[1]
+            s = s + pl[2] * xv[2]
+            s = s + pl[3]
+            s = s - delta
+            if not s <= 0.0:
+                continue
+            dup = False
+            for q in mine:
+                acc = 0.0
+                for k in range(4):
+                    d = q[k] - pl[k]
+                    acc = acc + d * d
+                dup = dup or math.sqrt(acc) <= 1e-4
+            if dup:
+                continue
+            mine.append(pl)
+            if decoupled:
+                break
+        out.extend(mine)
+        ptr.append(len(out))
+    return np.asarray(ptr, np.int32), np.asarray(out, np.float64).reshape(-1, 4)
