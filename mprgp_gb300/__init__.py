@@ -287,6 +287,12 @@ class FemMesh:
         _check(lib().mprgp_fem_rhs(self.h, h, _ptr(g), _ptr(x), _ptr(v), 0,
                                    prob.h if prob is not None else None), "fem_rhs")
 
+    def get_b(self):
+        """The right-hand side of the last assembly or rhs call (host copy)."""
+        b = np.zeros(3 * self.nv)
+        _check(lib().mprgp_fem_get(self.h, None, None, None, _ptr(b), None), "fem_get")
+        return b
+
     def get(self):
         """(row_ptr, cols, vals (nnzb, 9), b, mass) of the last assembly."""
         rp = np.zeros(self.nv + 1, np.int32)
