@@ -136,6 +136,10 @@ int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
  * power of two, 16 by default where the device allows it); 0 sends every
  * instance to the engine. */
 int mprgp_context_set_cluster(mprgp_context *ctx, int cluster);
+/* Instances larger than the largest cluster also take the cluster solver
+ * when each CTA of that cluster covers at most `items` items (1..4; default
+ * 1, the others then go to the persistent engine). */
+int mprgp_context_set_cluster_items(mprgp_context *ctx, int items);
 
 /* ---- problem: one QP instance resident in device memory ----------------- */
 /* Replaces the reference's FixedSparseMatrix<T> + projector objects

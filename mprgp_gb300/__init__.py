@@ -83,6 +83,7 @@ def _sig(lib):
     s("mprgp_context_info", C.c_int, _P, _IP, _IP)
     s("mprgp_context_set_tuning", C.c_int, _P, C.c_int, C.c_int)
     s("mprgp_context_set_cluster", C.c_int, _P, C.c_int)
+    s("mprgp_context_set_cluster_items", C.c_int, _P, C.c_int)
     s("mprgp_problem_create", C.c_int, _P, C.c_int, C.POINTER(_P))
     s("mprgp_problem_destroy", C.c_int, _P)
     s("mprgp_problem_set_matrix", C.c_int, _P, C.c_int, _P, _P, _P, C.c_int, C.c_int)
@@ -334,6 +335,10 @@ class Context:
     def set_cluster(self, cluster: int = 8):
         """CTAs per cluster of the small-instance solver (0 = engine only)."""
         _check(lib().mprgp_context_set_cluster(self.h, cluster), "set_cluster")
+
+    def set_cluster_items(self, items: int = 1):
+        """Items per CTA allowed in the largest cluster (1..4)."""
+        _check(lib().mprgp_context_set_cluster_items(self.h, items), "set_cluster_items")
 
     def set_tuning(self, stage: int = 0, ctas_per_sm: int = 0):
         _check(lib().mprgp_context_set_tuning(self.h, stage, ctas_per_sm), "set_tuning")

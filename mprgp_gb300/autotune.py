@@ -7,6 +7,8 @@ the tuner checks that for the setting it picks.
 
   cluster      largest cluster of the small-instance solver (CTAs of 256
                vertex rows; instances up to that many items take it)
+  cluster_items  items per CTA allowed in the largest cluster (larger
+               instances then also run as independent clusters)
   power        the power method's loop: a CUDA-graph WHILE loop of the power
                kernel, plain stream launches of it, or phases of the
                persistent engine
@@ -32,9 +34,11 @@ import numpy as np
 
 from . import KIND_PLANES, PREC_MIXED, Context, default_options, load_beam
 
-DEFAULT = {"cluster": 16, "power": "graph", "power_regs": 40, "ctas_per_sm": 0, "stage": 0}
+DEFAULT = {"cluster": 16, "cluster_items": 1, "power": "graph", "power_regs": 40,
+           "ctas_per_sm": 0, "stage": 0}
 SPACE = {
     "cluster": [16, 8, 4, 0],
+    "cluster_items": [1, 2, 4],
     "power": ["graph", "stream", "engine"],
     "power_regs": [40, 64],
     "ctas_per_sm": [0, 3, 2],
@@ -62,6 +66,7 @@ def apply(ctx: Context, cfg: dict) -> None:
                 raise
             cl //= 2
             cl = cl if cl >= 2 else 0
+    ctx.set_cluster_items(cfg.get("cluster_items", 1))
     bits = _POWER_BITS[cfg["power"]] | (1 if cfg["stage"] else 0)
     bits |= 8 if cfg.get("power_regs", 40) == 64 else 0
     ctx.set_tuning(bits, cfg["ctas_per_sm"])
@@ -134,6 +139,7 @@ def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5
         # coordinate descent; the power form and the power kernel's register
         # budget interact, so they are searched together
         steps = [[{"cluster": v} for v in SPACE["cluster"]],
+                 [{"cluster_items": v} for v in SPACE["cluster_items"]],
                  [{"power": f, "power_regs": r} for f in SPACE["power"]
                   for r in (SPACE["power_regs"] if f != "engine" else [40])],
                  [{"ctas_per_sm": v} for v in SPACE["ctas_per_sm"]],

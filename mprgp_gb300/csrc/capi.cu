@@ -53,6 +53,7 @@ struct mprgp_context {
   int power_variant = 0; // power kernel with 40 registers (0, 6 CTAs/SM) or 64 (1, 4 CTAs/SM)
   int bps_power_v[2] = {0, 0};
   int cluster = 16;      // largest cluster of the small-instance solver (0 = off)
+  int cluster_items = 1; // items per CTA allowed in the largest cluster (1..kClusterItems)
   int cluster_ok[kClusterClasses] = {0, 0, 0, 0, 0};  // cluster sizes 1, 2, 4, 8, 16 usable
   cudaStream_t side[kClusterClasses] = {};  // one per cluster size (run concurrently)
   cudaEvent_t fork_ev = nullptr, join_ev[kClusterClasses] = {};
@@ -386,11 +387,15 @@ void fill_stats(const InstState &s, double ms, mprgp_stats *out) {
 // Cluster-size class (log2 of the cluster size) of an instance of `items`
 // items on the cluster solver, or -1 for the persistent engine.
 int cluster_class(const mprgp_context *c, int items) {
+  int largest = -1;
   for (int q = 0; q < kClusterClasses; ++q) {
     const int cs = 1 << q;
     if (cs > c->cluster) break;
-    if (c->cluster_ok[q] && items <= cs * kClusterItems) return q;
+    if (!c->cluster_ok[q]) continue;
+    if (items <= cs) return q;  // one item per CTA
+    largest = q;
   }
+  if (largest >= 0 && items <= (1 << largest) * c->cluster_items) return largest;
   return -1;
 }
 
@@ -828,6 +833,13 @@ int mprgp_context_set_cluster(mprgp_context *c, int cluster) {
     if (!c->cluster_ok[q]) return fail(MPRGP_INVALID, "set_cluster: size not available");
   }
   c->cluster = cluster;
+  return MPRGP_OK;
+}
+
+int mprgp_context_set_cluster_items(mprgp_context *c, int items) {
+  if (!c || items < 1 || items > kClusterItems)
+    return fail(MPRGP_INVALID, "set_cluster_items: 1..4");
+  c->cluster_items = items;
   return MPRGP_OK;
 }
 

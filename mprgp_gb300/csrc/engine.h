@@ -140,8 +140,9 @@ constexpr int kPowerUnroll = 8;  // power launches per evaluation of the loop co
 // Small instances run on the cluster solver: one thread-block cluster per
 // instance, CTA r covering items r, r + cluster, ... (at most kClusterItems
 // of them); the host picks the smallest cluster size (a power of two up to
-// kClusterMax) that gives every CTA one item.
-constexpr int kClusterItems = 1;
+// kClusterMax) that gives every CTA one item, or else the largest size with
+// up to the context's items-per-CTA limit (at most kClusterItems).
+constexpr int kClusterItems = 4;
 constexpr int kClusterMax = 16;
 constexpr int kClusterClasses = 5;  // cluster sizes 1, 2, 4, 8, 16
 

@@ -385,3 +385,26 @@ def test_relayout_when_planes_change(ctx):
     A, _, _, _ = H.qp_from_beam(corner)
     assert rel(yd.cpu().numpy(), A.matvec(xd.cpu().numpy())) < 1e-14
     fresh.close()
+
+
+@pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
+def test_multi_item_clusters_equal_engine(precision):
+    """With several items per CTA, instances beyond the largest cluster also
+    run on the cluster solver (a 47-item and a 34-item beam on 16 CTAs), and
+    still give bitwise the engine's results."""
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(16, 16, 40, 2, 61), (20, 12, 30, 1, 62), (8, 8, 20, 1, 63)]]
+    c = M.Context(0)
+    try:
+        c.set_cluster(0)
+        ref = _solve_all(c, qps, precision)
+        c.set_cluster(16)
+        for items in (2, 4):
+            c.set_cluster_items(items)
+            got = _solve_all(c, qps, precision)
+            for (xe, fe, se), (xc, fc, sc) in zip(ref, got):
+                assert se.code == 0 and sc.code == 0
+                assert np.array_equal(xe, xc) and np.array_equal(fe, fc)
+                assert (se.iterations, se.phases) == (sc.iterations, sc.phases)
+    finally:
+        c.close()
