@@ -126,7 +126,10 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * issues the power kernel's launches from the host stream instead of a
  * CUDA-graph WHILE loop; bit 3 = 1 uses the power kernel built for 64
  * registers per thread (4 CTAs per SM) instead of 40 (6 CTAs per SM);
- * ctas_per_sm caps the persistent grid (0 = every resident CTA). */
+ * bit 4 = 1 runs the large instances' phases as a CUDA-graph loop of
+ * ordinary launches (one phase per launch) instead of the persistent
+ * cooperative engine; ctas_per_sm caps the persistent grid (0 = every
+ * resident CTA). */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
 /* Small instances -- up to `cluster` items of 256 vertices -- are solved by
  * one thread-block cluster each, one CTA per item (state in shared memory,

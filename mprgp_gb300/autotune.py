@@ -14,6 +14,8 @@ the tuner checks that for the setting it picks.
                persistent engine
   power_regs   the power kernel's register budget: 40 (6 CTAs per SM) or
                64 (4 CTAs per SM, more loads in flight per thread)
+  engine       the large instances' MPRGP phases: the persistent cooperative
+               engine, or a CUDA-graph loop of one launch per phase
   ctas_per_sm  resident CTAs per SM of the persistent engine (0 = all)
   stage        FP32 matrix slices staged in shared memory by bulk copies
 
@@ -35,12 +37,13 @@ import numpy as np
 from . import KIND_PLANES, PREC_MIXED, Context, default_options, load_beam
 
 DEFAULT = {"cluster": 16, "cluster_items": 1, "power": "graph", "power_regs": 40,
-           "ctas_per_sm": 0, "stage": 0}
+           "engine": "persistent", "ctas_per_sm": 0, "stage": 0}
 SPACE = {
     "cluster": [16, 8, 4, 0],
     "cluster_items": [1, 2, 4],
     "power": ["graph", "stream", "engine"],
     "power_regs": [40, 64],
+    "engine": ["persistent", "graph"],
     "ctas_per_sm": [0, 3, 2],
     "stage": [0, 1],
 }
@@ -69,6 +72,7 @@ def apply(ctx: Context, cfg: dict) -> None:
     ctx.set_cluster_items(cfg.get("cluster_items", 1))
     bits = _POWER_BITS[cfg["power"]] | (1 if cfg["stage"] else 0)
     bits |= 8 if cfg.get("power_regs", 40) == 64 else 0
+    bits |= 16 if cfg.get("engine", "persistent") == "graph" else 0
     ctx.set_tuning(bits, cfg["ctas_per_sm"])
 
 
@@ -142,6 +146,7 @@ def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5
                  [{"cluster_items": v} for v in SPACE["cluster_items"]],
                  [{"power": f, "power_regs": r} for f in SPACE["power"]
                   for r in (SPACE["power_regs"] if f != "engine" else [40])],
+                 [{"engine": v} for v in SPACE["engine"]],
                  [{"ctas_per_sm": v} for v in SPACE["ctas_per_sm"]],
                  [{"stage": v} for v in SPACE["stage"]]]
         for step in steps:

@@ -51,7 +51,9 @@ struct mprgp_context {
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
   int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
   int power_variant = 0; // power kernel with 40 registers (0, 6 CTAs/SM) or 64 (1, 4 CTAs/SM)
-  int bps_power_v[2] = {0, 0};
+  int bps_power_v[3] = {0, 0, 0};  // per power-kernel variant (2: all phases)
+  int engine_graph = 0;  // large instances' phases as a graph loop of the phase kernel (1)
+                         // or the persistent cooperative engine (0)
   int cluster = 16;      // largest cluster of the small-instance solver (0 = off)
   int cluster_items = 1; // items per CTA allowed in the largest cluster (1..kClusterItems)
   int cluster_ok[kClusterClasses] = {0, 0, 0, 0, 0};  // cluster sizes 1, 2, 4, 8, 16 usable
@@ -64,7 +66,7 @@ struct mprgp_context {
   // power-method graphs (one per grid size) and their device-side inputs
   int bps_power = 0;
   EngineArgs *d_args = nullptr;
-  PowCtl *d_pc = nullptr;
+  PowCtl *d_pc = nullptr, *d_pc2 = nullptr;  // power loop, engine loop
   std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> power_graphs;
   long long launches = 0;  // kernels launched (each power-loop iteration counts)
   double solver_ms = 0.0;  // device time of engine runs (power loop + engine)
@@ -402,20 +404,21 @@ int cluster_class(const mprgp_context *c, int items) {
 // Grid of the power kernel over `items` items: every resident CTA, or the
 // items rounded up to a multiple of 32 when that is fewer (few distinct sizes,
 // so few cached graph instantiations).
-int power_grid(mprgp_context *c, int items) {
-  const int cap = std::max(1, c->nsm * c->bps_power);
+int power_grid(mprgp_context *c, int items, int variant) {
+  const int cap = std::max(1, c->nsm * c->bps_power_v[variant]);
   return std::min(cap, (items + 31) / 32 * 32);
 }
 
-// The instantiated power-method graph for `grid` CTAs of the context's
-// power-kernel variant.
-int power_graph(mprgp_context *c, int grid, cudaGraphExec_t *exec) {
-  const int key = grid * 2 + c->power_variant;
+// The instantiated loop graph for `grid` CTAs of a phase-kernel variant
+// (0, 1: the power loop with its control block d_pc; 2: the all-phase loop
+// with d_pc2).
+int power_graph(mprgp_context *c, int grid, int variant, cudaGraphExec_t *exec) {
+  const int key = grid * 4 + variant;
   auto it = c->power_graphs.find(key);
   if (it == c->power_graphs.end()) {
     cudaGraph_t g;
     cudaGraphExec_t e;
-    CK(build_power_graph(grid, c->power_variant, c->d_args, c->d_pc, &g, &e));
+    CK(build_power_graph(grid, variant, c->d_args, variant == 2 ? c->d_pc2 : c->d_pc, &g, &e));
     it = c->power_graphs.emplace(key, std::make_pair(g, e)).first;
   }
   *exec = it->second.second;
@@ -560,16 +563,27 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   // the power kernel while any instance is in a power phase; then the engine.
   const bool power = c->power_kernel && in_power > 0 && power_launches > 0;
   cudaGraphExec_t pexec = nullptr;
-  const int pgrid = power_grid(c, prefix[n_large]);
+  const int pgrid = power_grid(c, prefix[n_large], c->power_variant);
   if (power) {
     if (c->power_graph) {
-      rc = power_graph(c, pgrid, &pexec);
+      rc = power_graph(c, pgrid, c->power_variant, &pexec);
       if (rc) return rc;
     }
     PowCtl pc0 = {in_power, 0u, 0u, 0u, (unsigned int)power_launches, 0u};
     CK(cudaMemcpyAsync(c->d_pc, &pc0, sizeof(PowCtl), cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(c->d_args, &args, sizeof(EngineArgs), cudaMemcpyHostToDevice, s));
   }
+  // The large instances' remaining phases: the persistent cooperative engine,
+  // or (engine_graph) the same phases as a graph loop of the all-phase kernel.
+  const bool egraph = c->engine_graph && n_large > 0;
+  cudaGraphExec_t eexec = nullptr;
+  if (egraph) {
+    rc = power_graph(c, power_grid(c, prefix[n_large], 2), 2, &eexec);
+    if (rc) return rc;
+    PowCtl pc0 = {(unsigned int)n_large, 0u, 0u, 0u, (unsigned int)args.max_phases, 0u};
+    CK(cudaMemcpyAsync(c->d_pc2, &pc0, sizeof(PowCtl), cudaMemcpyHostToDevice, s));
+  }
+  if (power || egraph)
+    CK(cudaMemcpyAsync(c->d_args, &args, sizeof(EngineArgs), cudaMemcpyHostToDevice, s));
   CK(cudaEventRecord(c->e0, s));
   // The cluster-size classes run on side streams, concurrently with each
   // other and with the power loop; the engine (a cooperative launch, whose
@@ -593,10 +607,12 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   CK(cudaEventRecord(c->e_pow, s));  // the main stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
     if (class_n[q]) CK(cudaStreamWaitEvent(s, c->join_ev[q], 0));
-  if (n_large > 0) CK(launch_engine(args, grid, s));
+  if (egraph) CK(cudaGraphLaunch(eexec, s));
+  else if (n_large > 0) CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(c->e1, s));
-  PowCtl pc1 = {0u, 0u, 0u, 0u, 0u, 0u};
+  PowCtl pc1 = {0u, 0u, 0u, 0u, 0u, 0u}, pc2 = {0u, 0u, 0u, 0u, 0u, 0u};
   if (power) CK(cudaMemcpyAsync(&pc1, c->d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
+  if (egraph) CK(cudaMemcpyAsync(&pc2, c->d_pc2, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   Ctl ctl1;
   CK(cudaMemcpyAsync(&ctl1, c->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   for (int i = 0; i < n; ++i)
@@ -613,7 +629,10 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   else if (power)
     c->launches += power_launches;
   for (int q = 0; q < kClusterClasses; ++q) c->launches += class_n[q] ? 1 : 0;
-  c->launches += n_large > 0 ? 1 : 0;
+  if (egraph)
+    c->launches += (long long)kPowerUnroll * ((pc2.launches + kPowerUnroll - 1) / kPowerUnroll);
+  else
+    c->launches += n_large > 0 ? 1 : 0;
   c->solver_ms += ms;
   int worst = MPRGP_OK;
   for (int i = 0; i < n; ++i) {
@@ -742,6 +761,7 @@ int mprgp_context_create(int device, mprgp_context **out) {
   CK(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   CK(power_max_blocks_per_sm(0, &c->bps_power_v[0]));
   CK(power_max_blocks_per_sm(1, &c->bps_power_v[1]));
+  CK(power_max_blocks_per_sm(2, &c->bps_power_v[2]));
   c->bps_power = c->bps_power_v[0];
   {
     int largest = 0;
@@ -759,6 +779,7 @@ int mprgp_context_create(int device, mprgp_context **out) {
   int rc = dalloc(c, &c->ctl, 1);
   if (!rc) rc = dalloc(c, &c->d_args, 1);
   if (!rc) rc = dalloc(c, &c->d_pc, 1);
+  if (!rc) rc = dalloc(c, &c->d_pc2, 1);
   if (rc) return rc;
   CK(cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -776,6 +797,7 @@ int mprgp_context_destroy(mprgp_context *c) {
   dfree(c, c->d_prefix);
   dfree(c, c->d_args);
   dfree(c, c->d_pc);
+  dfree(c, c->d_pc2);
   cudaStreamSynchronize(c->stream);
   for (int q = 0; q < kClusterClasses; ++q) {
     if (c->side[q]) cudaStreamDestroy(c->side[q]);
@@ -804,10 +826,11 @@ int mprgp_context_sync(mprgp_context *c) {
 }
 
 int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
-  if (!c || stage < 0 || stage > 15 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  if (!c || stage < 0 || stage > 31 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
   c->power_kernel = (stage & 2) ? 0 : 1;
   c->power_graph = (stage & 4) ? 0 : 1;
   c->power_variant = (stage & 8) ? 1 : 0;
+  c->engine_graph = (stage & 16) ? 1 : 0;
   c->bps_power = c->bps_power_v[c->power_variant];
   stage &= 1;
   c->stage = stage;

@@ -1787,11 +1787,15 @@ __device__ __forceinline__ bool power_phase(int ph) {
   return ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST;
 }
 
-__device__ __forceinline__ void power_item(const InstDesc *desc, const int *item_prefix,
+// One item of a phase launch.  kAll = false: power-method phases only (the
+// other instances' items return at once); kAll = true: whatever phase each
+// instance is in, with the same per-row work, reductions and transitions as
+// the persistent engine -- so any phase can run as a launch of a graph loop.
+template <bool kAll>
+__device__ __forceinline__ void phase_item(const InstDesc *desc, const int *item_prefix,
                                            int ninst, int item, PowCtl *pc,
                                            cudaGraphConditionalHandle h, int signal,
-                                           InstDesc &sD, InstState &sS,
-                                           RedBuf &red,
+                                           InstDesc &sD, InstState &sS, RedBuf &red,
                                            double (&sums)[kPart], int &s_last) {
   const int inst = find_instance(item_prefix, ninst, item);
   __syncthreads();  // the previous item's readers of sD/sS are done
@@ -1808,19 +1812,22 @@ __device__ __forceinline__ void power_item(const InstDesc *desc, const int *item
   }
   __syncthreads();
   const int phase = sS.phase;
-  if (!power_phase(phase)) return;
+  if (kAll ? phase == PH_DONE : !power_phase(phase)) return;
   const int local = item - sD.item_begin;
   const int slot = local * kThreads + threadIdx.x;
+  const bool wmin = kAll && phase == PH_PL_SPMV;
   double part[kPart];
 #pragma unroll
-  for (int k = 0; k < kPart; ++k) part[k] = 0.0;
+  for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
   if (slot < sD.nv) {
     const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
-    row_power(sD, sS, v, slot, part);
+    if (kAll) row_op(sD, sS, v, slot, part);
+    else row_power(sD, sS, v, slot, part);
   }
   const int ns = nslots(phase);
-  const double r = block_reduce(part, red, ns, false);
-  if (threadIdx.x < ns) sD.part[(size_t)local * kPart + threadIdx.x] = r;
+  const double r = block_reduce(part, red, ns, wmin);
+  if (threadIdx.x < ns || (wmin && threadIdx.x == kMinSlot))
+    sD.part[(size_t)local * kPart + threadIdx.x] = r;
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned int old = atom_add_acq_rel(sD.cnt, 1u);
@@ -1830,22 +1837,32 @@ __device__ __forceinline__ void power_item(const InstDesc *desc, const int *item
   if (!s_last) return;
   double acc[kPart];
 #pragma unroll
-  for (int k = 0; k < kPart; ++k) acc[k] = 0.0;
-  for (int it = threadIdx.x; it < sD.nitems; it += kThreads)
-    for (int k = 0; k < ns; ++k) acc[k] += sD.part[(size_t)it * kPart + k];
-  const double t = block_reduce(acc, red, ns, false);
-  if (threadIdx.x < ns) sums[threadIdx.x] = t;
+  for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+  for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
+#pragma unroll
+    for (int k = 0; k < kPart; ++k) {
+      if (k == kMinSlot ? !wmin : k >= ns) continue;
+      const double x = sD.part[(size_t)it * kPart + k];
+      acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+    }
+  }
+  const double t = block_reduce(acc, red, ns, wmin);
+  if (threadIdx.x < kPart) sums[threadIdx.x] = t;
   __syncthreads();
   if (threadIdx.x == 0) {
     InstState S = sS;
-    S.phases++;
-    advance_power(sD, S, sums);
+    if (kAll) {
+      advance(sD, S, sums);
+    } else {
+      S.phases++;
+      advance_power(sD, S, sums);
+    }
     *sD.st = S;
     *sD.cnt = 0u;
     // `active` is read before this finalize is counted: only the last
     // finalize of the launch rewrites it, after every other one was counted.
     const unsigned int active = pc->active;
-    if (power_phase(S.phase)) atomicAdd(&pc->busy, 1u);
+    if (kAll ? S.phase != PH_DONE : power_phase(S.phase)) atomicAdd(&pc->busy, 1u);
     const unsigned int old = atom_add_acq_rel(&pc->fin, 1u);
     if (old == active - 1u) {
       const unsigned int busy = atomicAdd(&pc->busy, 0u);
@@ -1862,12 +1879,13 @@ __device__ __forceinline__ void power_item(const InstDesc *desc, const int *item
   }
 }
 
-// Two register budgets: 40 registers (6 CTAs per SM, for grids that fill
-// the SMs) or 64 (4 CTAs per SM, more loads in flight per thread); the
-// context's tuning picks one.
-template <int kMinBlocks>
+// The phase kernel: power-only with two register budgets -- 40 registers (6
+// CTAs per SM, for grids that fill the SMs) or 64 (4 CTAs per SM, more loads
+// in flight per thread) -- or every phase (kAll, 64 registers like the
+// persistent engine).  The context's tuning picks one.
+template <int kMinBlocks, bool kAll>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
-    power_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc, cudaGraphConditionalHandle h,
+    phase_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc, cudaGraphConditionalHandle h,
                  int signal) {
   __shared__ InstDesc sD;
   __shared__ InstState sS;
@@ -1880,7 +1898,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   const int *item_prefix = pargs->item_prefix;
   const int ninst = pargs->ninst, total = pargs->total_items;
   for (int item = blockIdx.x; item < total; item += gridDim.x)
-    power_item(desc, item_prefix, ninst, item, pc, h, signal, sD, sS, red, sums, s_last);
+    phase_item<kAll>(desc, item_prefix, ninst, item, pc, h, signal, sD, sS, red, sums, s_last);
 }
 
 // ---------------------------------------------------- cluster solver -----
@@ -2087,12 +2105,16 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, engine_kernel, kThreads, stage_bytes);
 }
-// A graph whose WHILE node runs power_kernel over `grid` CTAs until no
+// A graph whose WHILE node runs phase_kernel over `grid` CTAs until no
 // instance is left in a power phase or PowCtl::limit launches have run.  The
 // kernel reads its EngineArgs and PowCtl from device memory, so one
 // instantiation serves every later run with the same grid.
+// variant 0: power phases, 40 registers; 1: power phases, 64 registers;
+// 2: every phase (the graph form of the engine).
 const void *power_kernel_fn(int variant) {
-  return variant ? (const void *)power_kernel<4> : (const void *)power_kernel<6>;
+  return variant == 2 ? (const void *)phase_kernel<4, true>
+         : variant   ? (const void *)phase_kernel<4, false>
+                     : (const void *)phase_kernel<6, false>;
 }
 cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, PowCtl *d_pc,
                               cudaGraph_t *graph, cudaGraphExec_t *exec) {
@@ -2141,10 +2163,10 @@ cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, P
 cudaError_t launch_power_direct(int grid, int variant, int launches, const EngineArgs *d_args,
                                 PowCtl *d_pc, cudaStream_t stream) {
   for (int k = 0; k < launches; ++k) {
-    if (variant)
-      power_kernel<4><<<grid, kThreads, 0, stream>>>(d_args, d_pc, cudaGraphConditionalHandle(0), 0);
-    else
-      power_kernel<6><<<grid, kThreads, 0, stream>>>(d_args, d_pc, cudaGraphConditionalHandle(0), 0);
+    const cudaGraphConditionalHandle h0 = 0;
+    if (variant == 2) phase_kernel<4, true><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
+    else if (variant) phase_kernel<4, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
+    else phase_kernel<6, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

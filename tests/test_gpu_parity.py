@@ -408,3 +408,37 @@ def test_multi_item_clusters_equal_engine(precision):
                 assert (se.iterations, se.phases) == (sc.iterations, sc.phases)
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
+def test_engine_graph_loop_equals_persistent_engine(precision):
+    """The large instances' phases as a CUDA-graph loop of one launch per
+    phase give bitwise the persistent engine's results (one instance alone
+    and two in one batch)."""
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(16, 16, 40, 2, 71), (24, 20, 30, 1, 72)]]
+    c = M.Context(0)
+    try:
+        res = {}
+        for bits in (0, 16):
+            c.set_tuning(bits, 0)
+            single = _solve_all(c, qps, precision)
+            probs, opts = [], []
+            for qp in qps:
+                probs.append(M.load_beam(c, qp, precisions=3))
+                opts.append(M.default_options(tol=1e-10 * np.linalg.norm(qp.b), max_it=20000,
+                                              kind=M.KIND_PLANES, project_x0=1, seed=SEED,
+                                              precision=precision))
+            stats = c.solve_batch(probs, opts)
+            batch = [(pr.get_x(), st) for pr, st in zip(probs, stats)]
+            for pr in probs:
+                pr.close()
+            res[bits] = (single, batch)
+        for (xa, fa, sa), (xb, fb, sb) in zip(res[0][0], res[16][0]):
+            assert sa.code == 0 and sb.code == 0
+            assert np.array_equal(xa, xb) and np.array_equal(fa, fb)
+            assert (sa.iterations, sa.phases) == (sb.iterations, sb.phases)
+        for (xa, sa), (xb, sb) in zip(res[0][1], res[16][1]):
+            assert sa.code == 0 and sb.code == 0 and np.array_equal(xa, xb)
+    finally:
+        c.close()
