@@ -255,6 +255,12 @@ typedef struct mprgp_server_config {
   int power_launches; /* power-method loop iterations per step (0..1003) */
   int cluster_quantum; /* phases per step of the small instances (cluster
                           solver; 0 = run them to completion in the step) */
+  int lanes;          /* 0: each step runs every admitted request in one
+                         engine run and waits for it; 2: small requests
+                         (cluster solver) and large ones run on two
+                         asynchronous lanes -- a step retires the runs that
+                         finished, admits, starts a new run on every idle
+                         lane and returns without waiting for it */
 } mprgp_server_config;
 typedef struct mprgp_server mprgp_server;
 int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out);

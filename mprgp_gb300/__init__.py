@@ -46,7 +46,7 @@ class Stats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_slots", C.c_int), ("quantum_phases", C.c_int),
-                ("power_launches", C.c_int), ("cluster_quantum", C.c_int)]
+                ("power_launches", C.c_int), ("cluster_quantum", C.c_int), ("lanes", C.c_int)]
 
 
 class BeamParams(C.Structure):
@@ -506,9 +506,10 @@ class Server:
     """Continuous-batching QP server (mprgp_server_*)."""
 
     def __init__(self, ctx: Context, hbm_budget=0, max_slots=0, quantum_phases=0,
-                 power_launches=256, cluster_quantum=0):
+                 power_launches=256, cluster_quantum=0, lanes=0):
         self.ctx = ctx
-        cfg = ServerConfig(hbm_budget, max_slots, quantum_phases, power_launches, cluster_quantum)
+        cfg = ServerConfig(hbm_budget, max_slots, quantum_phases, power_launches, cluster_quantum,
+                           lanes)
         self.h = C.c_void_p()
         _check(lib().mprgp_server_create(ctx.h, C.byref(cfg), C.byref(self.h)), "server_create")
         self.nv = {}

@@ -36,16 +36,63 @@ void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const doubl
                         float *out32, double *dinv, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st);
+void launch_state_scatter(const InstDesc *desc, int n, const InstState *in, const int *fresh,
+                          cudaStream_t st);
+void launch_state_gather(const InstDesc *desc, int n, InstState *out, cudaStream_t st);
 void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
                  cudaStream_t st);
 }  // namespace mprgp
 
 using namespace mprgp;
 
+// Device and pinned-host resources of one engine lane, and the run in flight
+// on it.  Lane 0 runs on the context stream (the synchronous calls); the
+// server's asynchronous form runs the small instances on lane 1 and the large
+// ones on lane 2, each on a stream of its own, so one lane's run never waits
+// for the other's.
+struct LaneRun {
+  bool active = false;
+  int n = 0, n_large = 0, quantum = 0, cluster_quantum = 0, power_launches = 0;
+  bool power = false, power_graph = false, egraph = false;
+  int class_n[kClusterClasses] = {0, 0, 0, 0, 0};
+  std::vector<mprgp_problem *> probs;
+  std::vector<mprgp_options> opts;
+  std::vector<int> pos;
+};
+
+struct HostIO {  // pinned: the run's control blocks in and out
+  Ctl ctl_in, ctl_out;
+  PowCtl pc_in[2], pc_out[2];  // power loop, engine loop
+  EngineArgs args;
+};
+
+struct Lane {
+  bool ready = false, own_stream = false;
+  cudaStream_t stream = nullptr;
+  Ctl *ctl = nullptr;
+  EngineArgs *d_args = nullptr;
+  PowCtl *d_pc = nullptr, *d_pc2 = nullptr;  // power loop, engine loop
+  cudaStream_t side[kClusterClasses] = {};   // one per cluster size (run concurrently)
+  cudaEvent_t fork_ev = nullptr, join_ev[kClusterClasses] = {};
+  cudaEvent_t fence = nullptr;               // context-stream work the run depends on
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e_pow = nullptr, e_end = nullptr;
+  // loop graphs of the phase kernel, keyed grid * 4 + variant (they hold
+  // this lane's d_args / d_pc / d_pc2)
+  std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
+  // per-run arrays in desc order (grown on demand)
+  int cap = 0;
+  InstDesc *d_desc = nullptr, *h_desc = nullptr;
+  int *d_prefix = nullptr, *h_prefix = nullptr;
+  InstState *d_st = nullptr, *h_st_in = nullptr, *h_st_out = nullptr;
+  int *d_fresh = nullptr, *h_fresh = nullptr;
+  HostIO *io = nullptr;
+  LaneRun run;
+};
+constexpr int kLanes = 3;
+
 struct mprgp_context {
   int device = 0;
   cudaStream_t stream = nullptr;
-  Ctl *ctl = nullptr;
   int nsm = 0, bps = 0, bps_stage = 0;
   int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
@@ -57,25 +104,14 @@ struct mprgp_context {
   int cluster = 16;      // largest cluster of the small-instance solver (0 = off)
   int cluster_items = 1; // items per CTA allowed in the largest cluster (1..kClusterItems)
   int cluster_ok[kClusterClasses] = {0, 0, 0, 0, 0};  // cluster sizes 1, 2, 4, 8, 16 usable
-  cudaStream_t side[kClusterClasses] = {};  // one per cluster size (run concurrently)
-  cudaEvent_t fork_ev = nullptr, join_ev[kClusterClasses] = {};
   int ctas_per_sm = 0;   // persistent CTAs per SM (0 = all resident)
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaMemPool_t pool = nullptr;      // every device array of the context's problems
   mprgp_problem *scratch = nullptr;
-  // power-method graphs (one per grid size) and their device-side inputs
   int bps_power = 0;
-  EngineArgs *d_args = nullptr;
-  PowCtl *d_pc = nullptr, *d_pc2 = nullptr;  // power loop, engine loop
-  std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> power_graphs;
+  Lane lane[kLanes];
   long long launches = 0;  // kernels launched (each power-loop iteration counts)
-  double solver_ms = 0.0;  // device time of engine runs (power loop + engine)
+  double solver_ms = 0.0;  // device time of engine runs, summed over runs (lanes overlap)
   double power_ms = 0.0;   // device time of the power loop alone
-  cudaEvent_t e_pow = nullptr;  // reused by mprgp_solve_bsr
-  // per-launch arrays (grown on demand)
-  InstDesc *d_desc = nullptr;
-  int *d_prefix = nullptr;
-  int cap_inst = 0;
 };
 
 struct mprgp_problem {
@@ -409,91 +445,204 @@ int power_grid(mprgp_context *c, int items, int variant) {
   return std::min(cap, (items + 31) / 32 * 32);
 }
 
-// The instantiated loop graph for `grid` CTAs of a phase-kernel variant
-// (0, 1: the power loop with its control block d_pc; 2: the all-phase loop
-// with d_pc2).
-int power_graph(mprgp_context *c, int grid, int variant, cudaGraphExec_t *exec) {
+// The instantiated loop graph of a lane for `grid` CTAs of a phase-kernel
+// variant (0, 1: the power loop with the lane's d_pc; 2: the all-phase loop
+// with its d_pc2).
+int power_graph(Lane &L, int grid, int variant, cudaGraphExec_t *exec) {
   const int key = grid * 4 + variant;
-  auto it = c->power_graphs.find(key);
-  if (it == c->power_graphs.end()) {
+  auto it = L.graphs.find(key);
+  if (it == L.graphs.end()) {
     cudaGraph_t g;
     cudaGraphExec_t e;
-    CK(build_power_graph(grid, variant, c->d_args, variant == 2 ? c->d_pc2 : c->d_pc, &g, &e));
-    it = c->power_graphs.emplace(key, std::make_pair(g, e)).first;
+    CK(build_power_graph(grid, variant, L.d_args, variant == 2 ? L.d_pc2 : L.d_pc, &g, &e));
+    it = L.graphs.emplace(key, std::make_pair(g, e)).first;
   }
   *exec = it->second.second;
   return MPRGP_OK;
 }
 
-int ensure_launch_arrays(mprgp_context *c, int ninst) {
-  if (ninst <= c->cap_inst) return MPRGP_OK;
-  dfree(c, c->d_desc);
-  dfree(c, c->d_prefix);
-  int cap = std::max(ninst, 16);
-  int rc = dalloc(c, &c->d_desc, cap);
+// Creates a lane's streams, events and control blocks on first use.
+int lane_init(mprgp_context *c, int k) {
+  Lane &L = c->lane[k];
+  if (L.ready) return MPRGP_OK;
+  if (k == 0) {
+    L.stream = c->stream;
+  } else {
+    CK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+    L.own_stream = true;
+  }
+  for (int q = 0; q < kClusterClasses; ++q) {
+    CK(cudaStreamCreateWithFlags(&L.side[q], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&L.join_ev[q], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&L.fork_ev, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&L.fence, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&L.e_end, cudaEventDisableTiming));
+  CK(cudaEventCreate(&L.e0));
+  CK(cudaEventCreate(&L.e1));
+  CK(cudaEventCreate(&L.e_pow));
+  CK(cudaMallocHost((void **)&L.io, sizeof(HostIO)));
+  std::memset(L.io, 0, sizeof(HostIO));
+  int rc = dalloc(c, &L.ctl, 1);
+  if (!rc) rc = dalloc(c, &L.d_args, 1);
+  if (!rc) rc = dalloc(c, &L.d_pc, 1);
+  if (!rc) rc = dalloc(c, &L.d_pc2, 1);
   if (rc) return rc;
-  rc = dalloc(c, &c->d_prefix, cap + 1);
-  if (rc) return rc;
-  c->cap_inst = cap;
+  CK(cudaMemsetAsync(L.ctl, 0, sizeof(Ctl), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  L.ready = true;
   return MPRGP_OK;
+}
+
+void lane_free(mprgp_context *c, Lane &L) {
+  if (!L.ready) return;
+  if (L.stream) cudaStreamSynchronize(L.stream);
+  for (int q = 0; q < kClusterClasses; ++q)
+    if (L.side[q]) cudaStreamSynchronize(L.side[q]);
+  dfree(c, L.ctl);
+  dfree(c, L.d_args);
+  dfree(c, L.d_pc);
+  dfree(c, L.d_pc2);
+  dfree(c, L.d_desc);
+  dfree(c, L.d_prefix);
+  dfree(c, L.d_st);
+  dfree(c, L.d_fresh);
+  cudaStreamSynchronize(c->stream);
+  cudaFreeHost(L.h_desc);
+  cudaFreeHost(L.h_prefix);
+  cudaFreeHost(L.h_st_in);
+  cudaFreeHost(L.h_st_out);
+  cudaFreeHost(L.h_fresh);
+  cudaFreeHost(L.io);
+  for (auto &kv : L.graphs) {
+    cudaGraphExecDestroy(kv.second.second);
+    cudaGraphDestroy(kv.second.first);
+  }
+  L.graphs.clear();
+  for (int q = 0; q < kClusterClasses; ++q) {
+    if (L.side[q]) cudaStreamDestroy(L.side[q]);
+    if (L.join_ev[q]) cudaEventDestroy(L.join_ev[q]);
+  }
+  cudaEventDestroy(L.fork_ev);
+  cudaEventDestroy(L.fence);
+  cudaEventDestroy(L.e_end);
+  cudaEventDestroy(L.e0);
+  cudaEventDestroy(L.e1);
+  cudaEventDestroy(L.e_pow);
+  if (L.own_stream) cudaStreamDestroy(L.stream);
+  L = Lane();
+}
+
+// Grows a lane's per-run arrays to `n` instances (the lane is idle).
+int lane_reserve(mprgp_context *c, Lane &L, int n) {
+  if (n <= L.cap) return MPRGP_OK;
+  const int cap = std::max(64, std::max(n, 2 * L.cap));
+  dfree(c, L.d_desc);
+  dfree(c, L.d_prefix);
+  dfree(c, L.d_st);
+  dfree(c, L.d_fresh);
+  cudaFreeHost(L.h_desc);
+  cudaFreeHost(L.h_prefix);
+  cudaFreeHost(L.h_st_in);
+  cudaFreeHost(L.h_st_out);
+  cudaFreeHost(L.h_fresh);
+  L.h_desc = nullptr;
+  L.h_prefix = L.h_fresh = nullptr;
+  L.h_st_in = L.h_st_out = nullptr;
+  L.cap = 0;
+  int rc = dalloc(c, &L.d_desc, cap);
+  if (!rc) rc = dalloc(c, &L.d_prefix, cap + 1);
+  if (!rc) rc = dalloc(c, &L.d_st, cap);
+  if (!rc) rc = dalloc(c, &L.d_fresh, cap);
+  if (rc) return rc;
+  CK(cudaMallocHost((void **)&L.h_desc, sizeof(InstDesc) * cap));
+  CK(cudaMallocHost((void **)&L.h_prefix, sizeof(int) * (cap + 1)));
+  CK(cudaMallocHost((void **)&L.h_st_in, sizeof(InstState) * cap));
+  CK(cudaMallocHost((void **)&L.h_st_out, sizeof(InstState) * cap));
+  CK(cudaMallocHost((void **)&L.h_fresh, sizeof(int) * cap));
+  L.cap = cap;
+  return MPRGP_OK;
+}
+
+bool other_lanes_active(const mprgp_context *c, int k) {
+  for (int j = 0; j < kLanes; ++j)
+    if (j != k && c->lane[j].run.active) return true;
+  return false;
 }
 
 }  // namespace
 
 namespace mprgp {
 
-// One engine run over `n` problems.  Instances with fresh[i] != 0 start a
-// solve (their initial state is uploaded); the others resume from the state
-// left in device memory by the previous run.  The run advances the large
-// instances by at most `quantum` engine macro-phases (0: until all are done)
-// after up to `power_launches` launches of the power kernel, and the small
-// ones (cluster solver) by at most `cluster_quantum` phases (0: until done).
-// done[i] reports instances that finished (or failed); stats are filled for
-// every instance.
-int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
-               const int *fresh, int quantum, int power_launches, int cluster_quantum,
-               mprgp_stats *stats, int *done) {
-  int rc = ensure_launch_arrays(c, n);
+// Lane (1: small, 2: large) that the server's asynchronous form gives an
+// instance of `nv` vertices: small ones are those of the cluster solver.
+int engine_lane_of(const mprgp_context *c, int nv) {
+  return cluster_class(c, nitems_of(nv)) >= 0 ? 1 : 2;
+}
+
+// Starts one engine run over `n` problems on lane `k` and returns without
+// waiting for it.  Instances with fresh[i] != 0 start a solve (their initial
+// state is uploaded); the others resume from the state left in device memory
+// by the previous run.  The run advances the large instances by at most
+// `quantum` macro-phases (0: until all are done) after up to `power_launches`
+// launches of the power kernel, and the small ones (cluster solver) by at
+// most `cluster_quantum` phases (0: until done).  The problems must stay
+// untouched until engine_end.
+int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
+                 const mprgp_options *opts, const int *fresh, int quantum, int power_launches,
+                 int cluster_quantum) {
+  if (k < 0 || k >= kLanes || n <= 0) return fail(MPRGP_INVALID, "engine_begin");
+  int rc = lane_init(c, k);
+  if (rc) return rc;
+  Lane &L = c->lane[k];
+  if (L.run.active) return fail(MPRGP_INVALID, "engine lane busy");
+  rc = lane_reserve(c, L, n);
   if (rc) return rc;
   // Small instances run on the cluster solver, one cluster each, grouped by
   // cluster size (the smallest usable size that gives every CTA its items);
-  // the others on the power loop and the persistent engine.  The desc array
-  // holds the large instances first, then each cluster-size class.
-  std::vector<int> pos(n), cls(n);
-  int n_large = 0, class_n[kClusterClasses] = {0, 0, 0, 0, 0};
+  // the others on the power loop and the engine.  The desc array holds the
+  // large instances first, then each cluster-size class.
+  LaneRun &R = L.run;
+  R.probs.assign(probs, probs + n);
+  R.opts.assign(opts, opts + n);
+  R.pos.assign(n, 0);
+  std::vector<int> cls(n);
+  int n_large = 0;
+  for (int q = 0; q < kClusterClasses; ++q) R.class_n[q] = 0;
   for (int i = 0; i < n; ++i) {
     mprgp_problem *p = probs[i];
     if (!p || p->ctx != c) return fail(MPRGP_INVALID, "problem/context mismatch");
     cls[i] = cluster_class(c, nitems_of(p->nv));
-    if (cls[i] < 0) pos[i] = n_large++;
-    else class_n[cls[i]]++;
+    if (cls[i] < 0) R.pos[i] = n_large++;
+    else R.class_n[cls[i]]++;
   }
   int class_off[kClusterClasses];
   {
-    int k = n_large;
+    int f = n_large;
     for (int q = 0; q < kClusterClasses; ++q) {
-      class_off[q] = k;
-      k += class_n[q];
+      class_off[q] = f;
+      f += R.class_n[q];
     }
     int fill[kClusterClasses];
     for (int q = 0; q < kClusterClasses; ++q) fill[q] = class_off[q];
     for (int i = 0; i < n; ++i)
-      if (cls[i] >= 0) pos[i] = fill[cls[i]]++;
+      if (cls[i] >= 0) R.pos[i] = fill[cls[i]]++;
   }
-  const int n_small = n - n_large;
-  std::vector<InstDesc> desc(n);
-  std::vector<InstState> st(n);
-  std::vector<int> prefix(n_large + 1, 0);
+  InstDesc *desc = L.h_desc;
+  InstState *st = L.h_st_in;  // desc order
+  int *prefix = L.h_prefix;
+  prefix[0] = 0;
   for (int i = 0; i < n; ++i)
-    if (pos[i] < n_large) prefix[pos[i] + 1] = nitems_of(probs[i]->nv);
+    if (R.pos[i] < n_large) prefix[R.pos[i] + 1] = nitems_of(probs[i]->nv);
   for (int j = 0; j < n_large; ++j) prefix[j + 1] += prefix[j];
   double wait_s = 0.0;
   long long phase_bound = 0;
   for (int i = 0; i < n; ++i) {
     mprgp_problem *p = probs[i];
-    const int j = pos[i];
-    rc = prepare(p, &opts[i], j < n_large ? prefix[j] : 0, &desc[j], &st[i]);
+    const int j = R.pos[i];
+    rc = prepare(p, &opts[i], j < n_large ? prefix[j] : 0, &desc[j], &st[j]);
     if (rc) return rc;
+    L.h_fresh[j] = fresh[i] ? 1 : 0;
     wait_s = std::max(wait_s, opts[i].wait_limit_s);
     // Each MPRGP iteration takes at most 4 phases (CG: spmv, candidate,
     // optional delta^T A delta and residual replacement; expansion 3;
@@ -501,14 +650,12 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
     phase_bound = std::max(phase_bound, 1100LL + 8LL * ((long long)opts[i].max_it + 2));
   }
   if (wait_s <= 0.0) wait_s = 5.0;
-  cudaStream_t s = c->stream;
-  for (int i = 0; i < n; ++i)
-    if (fresh[i]) probs[i]->phase_host = st[i].phase;
   for (int i = 0; i < n; ++i) {
     if (!fresh[i]) continue;
     mprgp_problem *p = probs[i];
-    InstState &S = st[i];
-    const InstDesc &D = desc[pos[i]];
+    InstState &S = st[R.pos[i]];
+    const InstDesc &D = desc[R.pos[i]];
+    p->phase_host = S.phase;
     p->run_random = S.phase == PH_POW_RAND;
     p->run_cached = 0;
     if (p->run_random && p->pcache_on && p->pcache.valid && p->pcache.seed == opts[i].seed &&
@@ -523,27 +670,32 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
       p->phase_host = S.phase;
     }
   }
-  for (int i = 0; i < n; ++i) {
-    if (!fresh[i]) continue;
-    CK(cudaMemcpyAsync(probs[i]->st, &st[i], sizeof(InstState), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(probs[i]->cnt, 0, sizeof(unsigned int), s));
-  }
   unsigned int in_power = 0;  // large instances in a power phase
   for (int i = 0; i < n; ++i) {
     const int ph = probs[i]->phase_host;
-    if (pos[i] < n_large)
+    if (R.pos[i] < n_large)
       in_power += (ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST) ? 1u : 0u;
   }
-  CK(cudaMemcpyAsync(c->d_desc, desc.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(c->d_prefix, prefix.data(), sizeof(int) * (n_large + 1), cudaMemcpyHostToDevice, s));
-  Ctl ctl0;
-  std::memset(&ctl0, 0, sizeof(ctl0));
-  ctl0.active = n_large;
-  ctl0.snap[0] = ctl0.snap[1] = n_large;
-  CK(cudaMemcpyAsync(c->ctl, &ctl0, sizeof(Ctl), cudaMemcpyHostToDevice, s));
-  EngineArgs args;
-  args.desc = c->d_desc;
-  args.item_prefix = c->d_prefix;
+  cudaStream_t s = L.stream;
+  if (s != c->stream) {  // the problems' uploads and setup kernels come first
+    CK(cudaEventRecord(L.fence, c->stream));
+    CK(cudaStreamWaitEvent(s, L.fence, 0));
+  }
+  CK(cudaMemcpyAsync(L.d_desc, desc, sizeof(InstDesc) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(L.d_prefix, prefix, sizeof(int) * (n_large + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(L.d_st, st, sizeof(InstState) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(L.d_fresh, L.h_fresh, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  launch_state_scatter(L.d_desc, n, L.d_st, L.d_fresh, s);
+  CK(cudaGetLastError());
+  HostIO &io = *L.io;
+  std::memset(&io.ctl_in, 0, sizeof(Ctl));
+  io.ctl_in.active = n_large;
+  io.ctl_in.snap[0] = io.ctl_in.snap[1] = n_large;
+  CK(cudaMemcpyAsync(L.ctl, &io.ctl_in, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  EngineArgs &args = io.args;
+  std::memset(&args, 0, sizeof(args));
+  args.desc = L.d_desc;
+  args.item_prefix = L.d_prefix;
   args.ninst = n_large;
   args.total_items = prefix[n_large];
   long long maxp = phase_bound;
@@ -553,7 +705,7 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   args.total_ns = (long long)(std::max(60.0, 20.0 * wait_s) * 1e9);
   const bool stage = c->stage && c->bps_stage > 0;
   args.stage_bytes = stage ? kStageBytes : 0;
-  args.ctl = c->ctl;
+  args.ctl = L.ctl;
   int per_sm = stage ? c->bps_stage : c->bps;
   if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
   const int grid = std::max(1, std::min(prefix[n_large], c->nsm * per_sm));
@@ -561,100 +713,132 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   // The power method first (at most 1003 phases: the seeded start, 1001
   // iterations, the last difference), as a device-driven loop of launches of
   // the power kernel while any instance is in a power phase; then the engine.
-  const bool power = c->power_kernel && in_power > 0 && power_launches > 0;
+  R.power = c->power_kernel && in_power > 0 && power_launches > 0;
   cudaGraphExec_t pexec = nullptr;
   const int pgrid = power_grid(c, prefix[n_large], c->power_variant);
-  if (power) {
+  if (R.power) {
     if (c->power_graph) {
-      rc = power_graph(c, pgrid, c->power_variant, &pexec);
+      rc = power_graph(L, pgrid, c->power_variant, &pexec);
       if (rc) return rc;
     }
-    PowCtl pc0 = {in_power, 0u, 0u, 0u, (unsigned int)power_launches, 0u};
-    CK(cudaMemcpyAsync(c->d_pc, &pc0, sizeof(PowCtl), cudaMemcpyHostToDevice, s));
+    io.pc_in[0] = {in_power, 0u, 0u, 0u, (unsigned int)power_launches, 0u};
+    CK(cudaMemcpyAsync(L.d_pc, &io.pc_in[0], sizeof(PowCtl), cudaMemcpyHostToDevice, s));
   }
+  R.power_graph = pexec != nullptr;
   // The large instances' remaining phases: the persistent cooperative engine,
-  // or (engine_graph) the same phases as a graph loop of the all-phase kernel.
-  const bool egraph = c->engine_graph && n_large > 0;
+  // or the same phases as a graph loop of the all-phase kernel -- always the
+  // latter while another lane has a run in flight, since a cooperative launch
+  // needs every one of its CTAs resident at once.
+  R.egraph = n_large > 0 && (c->engine_graph || k != 0 || other_lanes_active(c, k));
   cudaGraphExec_t eexec = nullptr;
-  if (egraph) {
-    rc = power_graph(c, power_grid(c, prefix[n_large], 2), 2, &eexec);
+  if (R.egraph) {
+    rc = power_graph(L, power_grid(c, prefix[n_large], 2), 2, &eexec);
     if (rc) return rc;
-    PowCtl pc0 = {(unsigned int)n_large, 0u, 0u, 0u, (unsigned int)args.max_phases, 0u};
-    CK(cudaMemcpyAsync(c->d_pc2, &pc0, sizeof(PowCtl), cudaMemcpyHostToDevice, s));
+    io.pc_in[1] = {(unsigned int)n_large, 0u, 0u, 0u, (unsigned int)args.max_phases, 0u};
+    CK(cudaMemcpyAsync(L.d_pc2, &io.pc_in[1], sizeof(PowCtl), cudaMemcpyHostToDevice, s));
   }
-  if (power || egraph)
-    CK(cudaMemcpyAsync(c->d_args, &args, sizeof(EngineArgs), cudaMemcpyHostToDevice, s));
-  CK(cudaEventRecord(c->e0, s));
+  if (R.power || R.egraph)
+    CK(cudaMemcpyAsync(L.d_args, &args, sizeof(EngineArgs), cudaMemcpyHostToDevice, s));
+  CK(cudaEventRecord(L.e0, s));
   // The cluster-size classes run on side streams, concurrently with each
-  // other and with the power loop; the engine (a cooperative launch, whose
-  // CTAs must all be resident) starts once they are done.
-  if (n_small > 0) CK(cudaEventRecord(c->fork_ev, s));
+  // other and with the power loop; the engine starts once they are done.
+  if (n - n_large > 0) CK(cudaEventRecord(L.fork_ev, s));
   for (int q = 0; q < kClusterClasses; ++q) {
-    if (!class_n[q]) continue;
+    if (!R.class_n[q]) continue;
     ClusterArgs cargs;
-    cargs.desc = c->d_desc + class_off[q];
-    cargs.ninst = class_n[q];
+    cargs.desc = L.d_desc + class_off[q];
+    cargs.ninst = R.class_n[q];
     cargs.max_phases = (int)std::min<long long>(
         cluster_quantum > 0 ? std::min<long long>(phase_bound, cluster_quantum) : phase_bound,
         INT_MAX);
-    CK(cudaStreamWaitEvent(c->side[q], c->fork_ev, 0));
-    CK(launch_cluster(cargs, 1 << q, c->side[q]));
-    CK(cudaEventRecord(c->join_ev[q], c->side[q]));
+    CK(cudaStreamWaitEvent(L.side[q], L.fork_ev, 0));
+    CK(launch_cluster(cargs, 1 << q, L.side[q]));
+    CK(cudaEventRecord(L.join_ev[q], L.side[q]));
   }
-  if (power && pexec) CK(cudaGraphLaunch(pexec, s));
-  if (power && !pexec)
-    CK(launch_power_direct(pgrid, c->power_variant, power_launches, c->d_args, c->d_pc, s));
-  CK(cudaEventRecord(c->e_pow, s));  // the main stream's power loop ends here
+  if (R.power && pexec) CK(cudaGraphLaunch(pexec, s));
+  if (R.power && !pexec)
+    CK(launch_power_direct(pgrid, c->power_variant, power_launches, L.d_args, L.d_pc, s));
+  CK(cudaEventRecord(L.e_pow, s));  // the lane stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
-    if (class_n[q]) CK(cudaStreamWaitEvent(s, c->join_ev[q], 0));
-  if (egraph) CK(cudaGraphLaunch(eexec, s));
+    if (R.class_n[q]) CK(cudaStreamWaitEvent(s, L.join_ev[q], 0));
+  if (R.egraph) CK(cudaGraphLaunch(eexec, s));
   else if (n_large > 0) CK(launch_engine(args, grid, s));
-  CK(cudaEventRecord(c->e1, s));
-  PowCtl pc1 = {0u, 0u, 0u, 0u, 0u, 0u}, pc2 = {0u, 0u, 0u, 0u, 0u, 0u};
-  if (power) CK(cudaMemcpyAsync(&pc1, c->d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
-  if (egraph) CK(cudaMemcpyAsync(&pc2, c->d_pc2, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
-  Ctl ctl1;
-  CK(cudaMemcpyAsync(&ctl1, c->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
-  for (int i = 0; i < n; ++i)
-    CK(cudaMemcpyAsync(&st[i], probs[i]->st, sizeof(InstState), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  CK(cudaEventRecord(L.e1, s));
+  if (R.power) CK(cudaMemcpyAsync(&io.pc_out[0], L.d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
+  if (R.egraph) CK(cudaMemcpyAsync(&io.pc_out[1], L.d_pc2, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&io.ctl_out, L.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+  launch_state_gather(L.d_desc, n, L.d_st, s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(L.h_st_out, L.d_st, sizeof(InstState) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaEventRecord(L.e_end, s));
+  R.n = n;
+  R.n_large = n_large;
+  R.quantum = quantum;
+  R.cluster_quantum = cluster_quantum;
+  R.power_launches = power_launches;
+  R.active = true;
+  return MPRGP_OK;
+}
+
+// Whether lane k's run has finished (1), is still in flight (0), or the lane
+// has no run (-1).
+int engine_ready(mprgp_context *c, int k) {
+  if (k < 0 || k >= kLanes || !c->lane[k].run.active) return -1;
+  const cudaError_t e = cudaEventQuery(c->lane[k].e_end);
+  if (e == cudaErrorNotReady) return 0;
+  return 1;  // finished, or failed: engine_end reports which
+}
+
+// Waits for lane k's run and takes its results: done[i] reports instances
+// that finished (or failed); stats are filled for every instance.
+int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
+  if (k < 0 || k >= kLanes || !c->lane[k].run.active) return fail(MPRGP_INVALID, "engine_end");
+  Lane &L = c->lane[k];
+  LaneRun &R = L.run;
+  R.active = false;
+  const int n = R.n, n_large = R.n_large;
+  CK(cudaEventSynchronize(L.e_end));
+  const HostIO &io = *L.io;
   float ms = 0.f, pms = 0.f;
-  CK(cudaEventElapsedTime(&ms, c->e0, c->e1));
-  if (power) CK(cudaEventElapsedTime(&pms, c->e0, c->e_pow));
+  CK(cudaEventElapsedTime(&ms, L.e0, L.e1));
+  if (R.power) CK(cudaEventElapsedTime(&pms, L.e0, L.e_pow));
   c->power_ms += pms;
-  // every body of the power loop issues kPowerUnroll launches, the stream form
+  // every body of a loop graph issues kPowerUnroll launches, the stream form
   // all `power_launches` (those after the last working one return at once)
-  if (power && pexec)
-    c->launches += (long long)kPowerUnroll * ((pc1.launches + kPowerUnroll - 1) / kPowerUnroll);
-  else if (power)
-    c->launches += power_launches;
-  for (int q = 0; q < kClusterClasses; ++q) c->launches += class_n[q] ? 1 : 0;
-  if (egraph)
-    c->launches += (long long)kPowerUnroll * ((pc2.launches + kPowerUnroll - 1) / kPowerUnroll);
+  if (R.power && R.power_graph)
+    c->launches += (long long)kPowerUnroll * ((io.pc_out[0].launches + kPowerUnroll - 1) / kPowerUnroll);
+  else if (R.power)
+    c->launches += R.power_launches;
+  for (int q = 0; q < kClusterClasses; ++q) c->launches += R.class_n[q] ? 1 : 0;
+  if (R.egraph)
+    c->launches += (long long)kPowerUnroll * ((io.pc_out[1].launches + kPowerUnroll - 1) / kPowerUnroll);
   else
     c->launches += n_large > 0 ? 1 : 0;
+  c->launches += 2;  // state scatter and gather
   c->solver_ms += ms;
+  const Ctl &ctl1 = io.ctl_out;
   int worst = MPRGP_OK;
   for (int i = 0; i < n; ++i) {
-    InstState &x = st[i];
-    probs[i]->phase_host = x.phase;
+    mprgp_problem *p = R.probs[i];
+    InstState x = L.h_st_out[R.pos[i]];
+    p->phase_host = x.phase;
     const bool finished = x.phase == PH_DONE;
-    const bool large = pos[i] < n_large;
+    const bool large = R.pos[i] < n_large;
     // an engine error concerns the engine's instances; an instance left
     // unfinished by a run that had no phase limit hit the hard phase bound
     const bool err = large && ctl1.err;
-    const bool unbounded = (large ? quantum : cluster_quantum) <= 0;
+    const bool unbounded = (large ? R.quantum : R.cluster_quantum) <= 0;
     if (err) x.code = ctl1.err;
     else if (!finished && unbounded) x.code = MPRGP_TIMEOUT;
-    probs[i]->xc = x.xc;
-    probs[i]->trace_n = x.trace_n;
-    if (finished && x.ev_upd && x.code > MPRGP_BREAKDOWN) probs[i]->ev_valid = 1;
-    if (finished && !err && probs[i]->run_random && !probs[i]->run_cached) {
-      auto &pc = probs[i]->pcache;
+    p->xc = x.xc;
+    p->trace_n = x.trace_n;
+    if (finished && x.ev_upd && x.code > MPRGP_BREAKDOWN) p->ev_valid = 1;
+    if (finished && !err && p->run_random && !p->run_cached) {
+      auto &pc = p->pcache;
       pc.valid = 1;
-      pc.seed = opts[i].seed;
-      pc.prec = desc[pos[i]].prec;
-      pc.gen = probs[i]->matrix_gen;
+      pc.seed = R.opts[i].seed;
+      pc.prec = L.h_desc[R.pos[i]].prec;
+      pc.gen = p->matrix_gen;
       pc.spec_rad = x.spec_rad;
       pc.power_iters = x.power_iters;
     }
@@ -664,6 +848,18 @@ int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp
   }
   if (ctl1.err) return fail(ctl1.err, "device wait limit reached");
   return worst < MPRGP_NOT_CONVERGED ? worst : MPRGP_OK;
+}
+
+// One engine run on lane 0 (the context stream), waited for.
+int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
+               const int *fresh, int quantum, int power_launches, int cluster_quantum,
+               mprgp_stats *stats, int *done) {
+  int rc = engine_begin(c, 0, n, probs, opts, fresh, quantum, power_launches, cluster_quantum);
+  if (rc) {
+    c->lane[0].run.active = false;
+    return rc;
+  }
+  return engine_end(c, 0, stats, done);
 }
 
 }  // namespace mprgp
@@ -748,9 +944,6 @@ int mprgp_context_create(int device, mprgp_context **out) {
     return fail(MPRGP_NO_DEVICE, "engine kernel cannot be resident");
   }
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  CK(cudaEventCreate(&c->e0));
-  CK(cudaEventCreate(&c->e1));
-  CK(cudaEventCreate(&c->e_pow));
   cudaMemPoolProps props;
   std::memset(&props, 0, sizeof(props));
   props.allocType = cudaMemAllocationTypePinned;
@@ -770,19 +963,11 @@ int mprgp_context_create(int device, mprgp_context **out) {
       c->cluster_ok[q] = cluster_max_active(1 << q, &nc) == cudaSuccess && nc >= 1;
       cudaGetLastError();
       if (c->cluster_ok[q]) largest = 1 << q;
-      CK(cudaStreamCreateWithFlags(&c->side[q], cudaStreamNonBlocking));
-      CK(cudaEventCreateWithFlags(&c->join_ev[q], cudaEventDisableTiming));
     }
-    CK(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
     c->cluster = std::min(c->cluster, largest);
   }
-  int rc = dalloc(c, &c->ctl, 1);
-  if (!rc) rc = dalloc(c, &c->d_args, 1);
-  if (!rc) rc = dalloc(c, &c->d_pc, 1);
-  if (!rc) rc = dalloc(c, &c->d_pc2, 1);
+  int rc = lane_init(c, 0);
   if (rc) return rc;
-  CK(cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream));
-  CK(cudaStreamSynchronize(c->stream));
   *out = c;
   return MPRGP_OK;
 }
@@ -792,25 +977,8 @@ int mprgp_context_destroy(mprgp_context *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   if (c->scratch) mprgp_problem_destroy(c->scratch);
-  dfree(c, c->ctl);
-  dfree(c, c->d_desc);
-  dfree(c, c->d_prefix);
-  dfree(c, c->d_args);
-  dfree(c, c->d_pc);
-  dfree(c, c->d_pc2);
+  for (int k = kLanes - 1; k >= 0; --k) lane_free(c, c->lane[k]);
   cudaStreamSynchronize(c->stream);
-  for (int q = 0; q < kClusterClasses; ++q) {
-    if (c->side[q]) cudaStreamDestroy(c->side[q]);
-    if (c->join_ev[q]) cudaEventDestroy(c->join_ev[q]);
-  }
-  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
-  for (auto &kv : c->power_graphs) {
-    cudaGraphExecDestroy(kv.second.second);
-    cudaGraphDestroy(kv.second.first);
-  }
-  cudaEventDestroy(c->e0);
-  cudaEventDestroy(c->e1);
-  cudaEventDestroy(c->e_pow);
   cudaStreamDestroy(c->stream);
   if (c->pool) cudaMemPoolDestroy(c->pool);
   delete c;
@@ -822,6 +990,8 @@ void *mprgp_context_stream(mprgp_context *c) { return c ? (void *)c->stream : nu
 int mprgp_context_sync(mprgp_context *c) {
   if (!c) return fail(MPRGP_INVALID, "ctx");
   CK(cudaStreamSynchronize(c->stream));
+  for (int k = 1; k < kLanes; ++k)
+    if (c->lane[k].ready) CK(cudaStreamSynchronize(c->lane[k].stream));
   return MPRGP_OK;
 }
 

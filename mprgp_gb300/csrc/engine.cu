@@ -2092,7 +2092,40 @@ __global__ void __launch_bounds__(256) spmv_kernel(SellMatrix A, const VT *__res
   st3(y, v, o);
 }
 
+// An engine run's instance states move between host and device as one array
+// in desc order: the fresh instances' initial states are scattered to their
+// state blocks (with their phase-item counters cleared) before the run, and
+// every instance's state is gathered back after it.  One CTA per instance.
+static_assert(sizeof(InstState) % 8 == 0, "InstState is copied as 8-byte words");
+constexpr int kStateWords = (int)(sizeof(InstState) / 8);
+
+__global__ void state_scatter_kernel(const InstDesc *__restrict__ desc, int n,
+                                     const InstState *__restrict__ in,
+                                     const int *__restrict__ fresh) {
+  const int j = blockIdx.x;
+  if (j >= n || !fresh[j]) return;
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(in + j);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(desc[j].st);
+  for (int w = threadIdx.x; w < kStateWords; w += blockDim.x) dst[w] = src[w];
+  if (threadIdx.x == 0) *desc[j].cnt = 0u;
+}
+
+__global__ void state_gather_kernel(const InstDesc *__restrict__ desc, int n, InstState *out) {
+  const int j = blockIdx.x;
+  if (j >= n) return;
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(desc[j].st);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(out + j);
+  for (int w = threadIdx.x; w < kStateWords; w += blockDim.x) dst[w] = src[w];
+}
+
 // Host-side launch helpers (declared in capi.cu).
+void launch_state_scatter(const InstDesc *desc, int n, const InstState *in, const int *fresh,
+                          cudaStream_t st) {
+  if (n > 0) state_scatter_kernel<<<n, 64, 0, st>>>(desc, n, in, fresh);
+}
+void launch_state_gather(const InstDesc *desc, int n, InstState *out, cudaStream_t st) {
+  if (n > 0) state_gather_kernel<<<n, 64, 0, st>>>(desc, n, out);
+}
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream) {
   void *params[] = {(void *)&args};
   return cudaLaunchCooperativeKernel((const void *)engine_kernel, dim3(grid), dim3(kThreads),

@@ -9,8 +9,13 @@
 // used first), then advances every admitted request -- small ones on the
 // cluster solver to completion (or by cluster_quantum phases), large ones by
 // one engine quantum, all in the same run, so their work overlaps on the
-// device -- and retires the ones that finished.  A request's result does not depend on
-// what else is in flight: each instance's reductions run in a fixed order.
+// device -- and retires the ones that finished.  In the asynchronous form
+// (two lanes) small and large requests run on separate engine lanes, each on
+// its own stream: a step retires the lane runs that finished, admits, starts
+// a run on every idle lane and returns without waiting, so a small request
+// that arrives while the large ones are mid-solve starts at once.  A
+// request's result does not depend on what else is in flight or on the form:
+// each instance's reductions run in a fixed order.
 #include <algorithm>
 #include <chrono>
 #include <deque>
@@ -27,6 +32,12 @@ namespace mprgp {
 int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
                const int *fresh, int quantum, int power_launches, int cluster_quantum,
                mprgp_stats *stats, int *done);
+int engine_begin(mprgp_context *c, int lane, int n, mprgp_problem *const *probs,
+                 const mprgp_options *opts, const int *fresh, int quantum, int power_launches,
+                 int cluster_quantum);
+int engine_ready(mprgp_context *c, int lane);
+int engine_end(mprgp_context *c, int lane, mprgp_stats *stats, int *done);
+int engine_lane_of(const mprgp_context *c, int nv);
 void set_last_error(const char *what);
 }  // namespace mprgp
 
@@ -46,6 +57,8 @@ struct Request {
   const double *p_vals = nullptr, *p_b = nullptr, *p_planes = nullptr, *p_x0 = nullptr;
   mprgp_options opt{};
   int state = 0;  // 0 queued, 1 running, 2 done
+  int lane = 0;   // asynchronous form: 0 small, 1 large
+  bool fresh = true;  // the next run starts its solve
   int code = 0;
   std::vector<double> x;
   std::vector<unsigned char> face;
@@ -85,6 +98,13 @@ struct mprgp_server {
   std::vector<long long> running;
   std::vector<char> fresh_flag;  // parallel to running
   std::deque<long long> completed;  // finished, not yet polled
+  // asynchronous form: per lane (small, large) the admitted requests waiting
+  // for its next run and those in its run in flight
+  int lanes = 0;
+  struct LaneQ {
+    std::vector<long long> pending, in_run;
+    bool active = false;
+  } lane[2];
 };
 
 namespace {
@@ -158,6 +178,195 @@ int admit(mprgp_server *s, Request &r) {
 
 }  // namespace
 
+namespace {
+
+int in_flight(const mprgp_server *s) {
+  if (!s->lanes) return (int)s->running.size();
+  int k = 0;
+  for (const auto &q : s->lane) k += (int)(q.pending.size() + q.in_run.size());
+  return k;
+}
+
+// Admission: FIFO, skipping requests that do not fit yet.
+void admit_queued(mprgp_server *s) {
+  for (auto it = s->queue.begin(); it != s->queue.end();) {
+    if (in_flight(s) >= s->max_slots) break;
+    Request &r = s->reqs[*it];
+    bool ok = true;
+    if (r.followup) {
+      auto sc = s->scenes.find(r.scene);
+      if (sc == s->scenes.end()) {  // evicted meanwhile: cannot warm start
+        r.state = 2;
+        r.code = MPRGP_INVALID;
+        s->completed.push_back(r.ticket);
+        it = s->queue.erase(it);
+        continue;
+      }
+      ok = !sc->second.busy;
+    } else {
+      const int prec = r.opt.precision == MPRGP_PREC_MIXED ? 3 : 1;
+      const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, r.m, prec);
+      auto sc = s->scenes.find(r.scene);
+      ok = (sc == s->scenes.end() || !sc->second.busy) && make_room(s, bytes);
+    }
+    if (!ok) {
+      ++it;
+      continue;
+    }
+    const int rc = admit(s, r);
+    if (rc) {
+      r.state = 2;
+      r.code = rc;
+      s->completed.push_back(r.ticket);
+      it = s->queue.erase(it);
+      continue;
+    }
+    r.state = 1;
+    r.t_admit = now_s();
+    r.fresh = true;
+    if (s->lanes) {
+      r.lane = mprgp::engine_lane_of(s->ctx, r.nv) == 1 ? 0 : 1;
+      s->lane[r.lane].pending.push_back(r.ticket);
+    } else {
+      s->running.push_back(r.ticket);
+      s->fresh_flag.push_back(1);
+    }
+    it = s->queue.erase(it);
+  }
+}
+
+// A finished request: its solution and face are read back, its scene freed
+// for the next request.
+void retire(mprgp_server *s, Request &r, const mprgp_stats &st) {
+  Scene &sc = s->scenes[r.scene];
+  r.stats = st;
+  r.code = st.code;
+  mprgp_problem_get_x(sc.prob, r.x.data(), 0);
+  if (sc.m > 0) mprgp_problem_get_face(sc.prob, r.face.data());
+  sc.busy = false;
+  r.state = 2;
+  r.t_done = now_s();
+  s->completed.push_back(r.ticket);
+}
+
+// The synchronous form: one engine run over every admitted request.
+int step_sync(mprgp_server *s, int *ncomp) {
+  const int n = (int)s->running.size();
+  if (n == 0) return MPRGP_OK;
+  std::vector<mprgp_problem *> probs(n);
+  std::vector<mprgp_options> opts(n);
+  std::vector<int> fresh(n), done(n, 0);
+  std::vector<mprgp_stats> st(n);
+  for (int i = 0; i < n; ++i) {
+    Request &r = s->reqs[s->running[i]];
+    probs[i] = s->scenes[r.scene].prob;
+    opts[i] = r.opt;
+    fresh[i] = s->fresh_flag[i];
+  }
+  const int rc = mprgp::engine_run(s->ctx, n, probs.data(), opts.data(), fresh.data(),
+                                   s->quantum, s->power_launches, s->cluster_quantum,
+                                   st.data(), done.data());
+  if (rc < MPRGP_NOT_CONVERGED) return rc;
+  std::vector<long long> still;
+  std::vector<char> still_fresh;
+  for (int i = 0; i < n; ++i) {
+    Request &r = s->reqs[s->running[i]];
+    if (!done[i]) {
+      still.push_back(r.ticket);
+      still_fresh.push_back(0);
+      continue;
+    }
+    retire(s, r, st[i]);
+    ++*ncomp;
+  }
+  s->running.swap(still);
+  s->fresh_flag.swap(still_fresh);
+  return MPRGP_OK;
+}
+
+// Takes the results of lane l's run if it has finished.
+int finish_lane(mprgp_server *s, int l, int *ncomp) {
+  auto &q = s->lane[l];
+  if (!q.active || mprgp::engine_ready(s->ctx, 1 + l) == 0) return MPRGP_OK;
+  const int n = (int)q.in_run.size();
+  std::vector<mprgp_stats> st(n);
+  std::vector<int> done(n, 0);
+  q.active = false;
+  const int rc = mprgp::engine_end(s->ctx, 1 + l, st.data(), done.data());
+  if (rc < MPRGP_NOT_CONVERGED) return rc;
+  std::vector<long long> keep;
+  for (int i = 0; i < n; ++i) {
+    Request &r = s->reqs[q.in_run[i]];
+    if (!done[i]) {
+      r.fresh = false;
+      keep.push_back(r.ticket);
+      continue;
+    }
+    retire(s, r, st[i]);
+    ++*ncomp;
+  }
+  q.in_run.clear();
+  // unfinished requests lead the lane's next run
+  q.pending.insert(q.pending.begin(), keep.begin(), keep.end());
+  return MPRGP_OK;
+}
+
+// Starts a run on lane l over its pending requests if the lane is idle.
+int start_lane(mprgp_server *s, int l) {
+  auto &q = s->lane[l];
+  if (q.active || q.pending.empty()) return MPRGP_OK;
+  q.in_run.swap(q.pending);
+  q.pending.clear();
+  const int n = (int)q.in_run.size();
+  std::vector<mprgp_problem *> probs(n);
+  std::vector<mprgp_options> opts(n);
+  std::vector<int> fresh(n);
+  for (int i = 0; i < n; ++i) {
+    Request &r = s->reqs[q.in_run[i]];
+    probs[i] = s->scenes[r.scene].prob;
+    opts[i] = r.opt;
+    fresh[i] = r.fresh ? 1 : 0;
+  }
+  const int rc = mprgp::engine_begin(s->ctx, 1 + l, n, probs.data(), opts.data(), fresh.data(),
+                                     s->quantum, s->power_launches, s->cluster_quantum);
+  if (rc) return rc;
+  q.active = true;
+  return MPRGP_OK;
+}
+
+// The asynchronous form: retire what the lanes finished, admit, start every
+// idle lane; when none of that happened, wait a little for a lane to finish
+// (the caller may have requests to submit meanwhile).
+int step_async(mprgp_server *s, int *ncomp) {
+  for (int l = 0; l < 2; ++l) {
+    const int rc = finish_lane(s, l, ncomp);
+    if (rc) return rc;
+  }
+  const size_t queued = s->queue.size();
+  admit_queued(s);
+  bool started = false;
+  for (int l = 0; l < 2; ++l) {
+    const bool idle = !s->lane[l].active;
+    const int rc = start_lane(s, l);
+    if (rc) return rc;
+    started |= idle && s->lane[l].active;
+  }
+  if (*ncomp || started || s->queue.size() != queued) return MPRGP_OK;
+  const double until = now_s() + 5e-4;
+  while (now_s() < until) {
+    bool any = false, ready = false;
+    for (int l = 0; l < 2; ++l) {
+      if (!s->lane[l].active) continue;
+      any = true;
+      ready |= mprgp::engine_ready(s->ctx, 1 + l) != 0;
+    }
+    if (!any || ready) break;
+  }
+  return MPRGP_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out) {
@@ -172,12 +381,19 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
   if (cfg && cfg->quantum_phases < 0) s->quantum = 0;  // each step runs to completion
   if (cfg && cfg->cluster_quantum > 0) s->cluster_quantum = cfg->cluster_quantum;
   if (cfg && cfg->power_launches >= 0) s->power_launches = std::min(cfg->power_launches, 1003);
+  if (cfg && cfg->lanes != 0 && cfg->lanes != 2) {
+    delete s;
+    return err(MPRGP_INVALID, "server_create: lanes must be 0 or 2");
+  }
+  s->lanes = cfg ? cfg->lanes : 0;
   *out = s;
   return MPRGP_OK;
 }
 
 int mprgp_server_destroy(mprgp_server *s) {
   if (!s) return MPRGP_OK;
+  for (int l = 0; l < 2; ++l)  // runs in flight end before their problems go
+    if (s->lane[l].active) mprgp::engine_end(s->ctx, 1 + l, nullptr, nullptr);
   for (auto &kv : s->scenes) mprgp_problem_destroy(kv.second.prob);
   delete s;
   return MPRGP_OK;
@@ -246,86 +462,15 @@ int mprgp_server_submit(mprgp_server *s, int scene, int nv, int nnzb, const int 
 
 int mprgp_server_step(mprgp_server *s, int *running, int *queued, int *completed) {
   if (!s) return err(MPRGP_INVALID, "server_step");
-  // Admission: FIFO, skipping requests that do not fit yet.
-  for (auto it = s->queue.begin(); it != s->queue.end();) {
-    if ((int)s->running.size() >= s->max_slots) break;
-    Request &r = s->reqs[*it];
-    bool ok = true;
-    if (r.followup) {
-      auto sc = s->scenes.find(r.scene);
-      if (sc == s->scenes.end()) {  // evicted meanwhile: cannot warm start
-        r.state = 2;
-        r.code = MPRGP_INVALID;
-        s->completed.push_back(r.ticket);
-        it = s->queue.erase(it);
-        continue;
-      }
-      ok = !sc->second.busy;
-    } else {
-      const int prec = r.opt.precision == MPRGP_PREC_MIXED ? 3 : 1;
-      const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, r.m, prec);
-      auto sc = s->scenes.find(r.scene);
-      ok = (sc == s->scenes.end() || !sc->second.busy) && make_room(s, bytes);
-    }
-    if (!ok) {
-      ++it;
-      continue;
-    }
-    const int rc = admit(s, r);
-    if (rc) {
-      r.state = 2;
-      r.code = rc;
-      s->completed.push_back(r.ticket);
-      it = s->queue.erase(it);
-      continue;
-    }
-    r.state = 1;
-    r.t_admit = now_s();
-    s->running.push_back(r.ticket);
-    s->fresh_flag.push_back(1);
-    it = s->queue.erase(it);
+  int ncomp = 0, rc;
+  if (s->lanes) {
+    rc = step_async(s, &ncomp);
+  } else {
+    admit_queued(s);
+    rc = step_sync(s, &ncomp);
   }
-  int ncomp = 0;
-  const int n = (int)s->running.size();
-  if (n > 0) {
-    std::vector<mprgp_problem *> probs(n);
-    std::vector<mprgp_options> opts(n);
-    std::vector<int> fresh(n), done(n, 0);
-    std::vector<mprgp_stats> st(n);
-    for (int i = 0; i < n; ++i) {
-      Request &r = s->reqs[s->running[i]];
-      probs[i] = s->scenes[r.scene].prob;
-      opts[i] = r.opt;
-      fresh[i] = s->fresh_flag[i];
-    }
-    const int rc = mprgp::engine_run(s->ctx, n, probs.data(), opts.data(), fresh.data(),
-                                     s->quantum, s->power_launches, s->cluster_quantum,
-                                     st.data(), done.data());
-    if (rc < MPRGP_NOT_CONVERGED) return rc;
-    std::vector<long long> still;
-    std::vector<char> still_fresh;
-    for (int i = 0; i < n; ++i) {
-      Request &r = s->reqs[s->running[i]];
-      if (!done[i]) {
-        still.push_back(r.ticket);
-        still_fresh.push_back(0);
-        continue;
-      }
-      Scene &sc = s->scenes[r.scene];
-      r.stats = st[i];
-      r.code = st[i].code;
-      mprgp_problem_get_x(sc.prob, r.x.data(), 0);
-      if (sc.m > 0) mprgp_problem_get_face(sc.prob, r.face.data());
-      sc.busy = false;
-      r.state = 2;
-      r.t_done = now_s();
-      s->completed.push_back(r.ticket);
-      ++ncomp;
-    }
-    s->running.swap(still);
-    s->fresh_flag.swap(still_fresh);
-  }
-  if (running) *running = (int)s->running.size();
+  if (rc) return rc;
+  if (running) *running = in_flight(s);
   if (queued) *queued = (int)s->queue.size();
   if (completed) *completed = ncomp;
   return MPRGP_OK;

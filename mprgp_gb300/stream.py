@@ -96,8 +96,8 @@ class StreamPlayer:
                                seed=self.seed, precision=precision, use_ev=self.use_ev)
 
     def play(self, rate_hz: float, precision=PREC_FP64, mode="device", max_slots=128,
-             quantum=256, power_launches=256, cluster_quantum=0, keep_x=False, stream=None,
-             flush=None) -> PlayResult:
+             quantum=256, power_launches=256, cluster_quantum=0, lanes=0, keep_x=False,
+             stream=None, flush=None) -> PlayResult:
         torch = self.torch
         reqs = self.win.reqs
         arrive = self.win.arrivals(rate_hz)
@@ -105,7 +105,7 @@ class StreamPlayer:
         if not record and len(self.fb) != sum(r.followup for r in reqs):
             raise RuntimeError("play in host mode first to record the follow-up right-hand sides")
         srv = Server(self.ctx, max_slots=max_slots, quantum_phases=quantum,
-                     power_launches=power_launches, cluster_quantum=cluster_quantum)
+                     power_launches=power_launches, cluster_quantum=cluster_quantum, lanes=lanes)
         # client-side scene state of the recording play (next_step_rhs)
         phys = {}
         pending = deque(range(len(reqs)))

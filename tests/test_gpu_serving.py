@@ -4,7 +4,9 @@
   served mix, where requests arrive while others are on the GPU;
 * follow-up timesteps warm-start from the resident scene and converge to the
   same solution as a cold solve of the same QP;
-* admission respects the HBM budget (scenes are evicted, never overcommitted).
+* admission respects the HBM budget (scenes are evicted, never overcommitted);
+* all of the above hold for both server forms: one synchronous run per step,
+  and two asynchronous lanes (small and large requests on separate streams).
 Tolerance: the stopping test 1e-8 ||b||; x compared to 1e-12 relative
 (in practice bitwise: each instance reduces in a fixed order).
 """
@@ -29,13 +31,18 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+@pytest.mark.parametrize("lanes", [0, 2])
 @pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
-def test_same_alone_and_in_the_mix(ctx, precision):
-    dims = [(4, 4, 6), (9, 5, 12), (3, 3, 4), (6, 8, 10), (5, 5, 5), (12, 6, 9)]
+def test_same_alone_and_in_the_mix(ctx, precision, lanes):
+    # sizes on both sides of the cluster solver's limit (16 items of 256
+    # vertices): the last two run on the engine
+    dims = [(4, 4, 6), (9, 5, 12), (3, 3, 4), (6, 8, 10), (5, 5, 5), (12, 6, 9), (14, 8, 30),
+            (16, 8, 32)]
     qps = [M.beam(*d, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=10 + i)
-           for i, (d, e) in enumerate(zip(dims, [0, 2, 1, 2, 0, 1]))]
+           for i, (d, e) in enumerate(zip(dims, [0, 2, 1, 2, 0, 1, 2, 1]))]
+    assert qps[-1].nv > 16 * 256 and qps[-2].nv > 16 * 256
     alone = [ctx.solve_bsr(q, opts_for(q, precision), q.x0) for q in qps]
-    srv = M.Server(ctx, quantum_phases=64, power_launches=128, max_slots=4)
+    srv = M.Server(ctx, quantum_phases=64, power_launches=128, max_slots=4, lanes=lanes)
     tickets, done = {}, {}
     # staggered arrivals: two at a time while earlier ones are in flight
     pending = list(range(len(qps)))
@@ -53,7 +60,7 @@ def test_same_alone_and_in_the_mix(ctx, precision):
                 assert st.code == 0
                 done[i] = (x, face, st)
                 del tickets[t]
-        assert steps < 10000
+        assert steps < 200000
     for i, (xa, fa, sa) in enumerate(alone):
         xs, fs, ss = done[i]
         assert rel(xs, xa) <= 1e-12, i
@@ -62,9 +69,10 @@ def test_same_alone_and_in_the_mix(ctx, precision):
     srv.close()
 
 
-def test_followup_warm_start(ctx):
+@pytest.mark.parametrize("lanes", [0, 2])
+def test_followup_warm_start(ctx, lanes):
     qp = M.beam(6, 5, 10, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=3)
-    srv = M.Server(ctx, quantum_phases=128, power_launches=256)
+    srv = M.Server(ctx, quantum_phases=128, power_launches=256, lanes=lanes)
     t = srv.submit(0, qp, opts_for(qp))
     while True:
         srv.step()
@@ -95,11 +103,13 @@ def test_followup_warm_start(ctx):
     srv.close()
 
 
-def test_admission_by_hbm_budget(ctx):
+@pytest.mark.parametrize("lanes", [0, 2])
+def test_admission_by_hbm_budget(ctx, lanes):
     qps = [M.beam(8, 8, 16, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=s)
            for s in range(4)]
     one = M.lib().mprgp_problem_bytes(qps[0].nv, qps[0].nnzb, len(qps[0].planes), 3)
-    srv = M.Server(ctx, hbm_budget=int(2.5 * one), quantum_phases=64, power_launches=64)
+    srv = M.Server(ctx, hbm_budget=int(2.5 * one), quantum_phases=64, power_launches=64,
+                   lanes=lanes)
     tickets = [srv.submit(i, q, opts_for(q)) for i, q in enumerate(qps)]
     max_running, finished = 0, 0
     for _ in range(100000):
