@@ -63,9 +63,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="c4: skip the arrival-rate sweep")
-    ap.add_argument("--lanes", type=int, default=SERVE_LANES, choices=[0, 2],
+    ap.add_argument("--lanes", type=int, default=SERVE_LANES, choices=[0, 2, 3],
                     help="c4: server form (0 one synchronous run per step, 2 asynchronous "
-                         "small/large lanes)")
+                         "small/large lanes, 3 plus a lane for the large ones' power method)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the launch-shape autotuner (mprgp_gb300.autotune) before warm-up")
     ap.add_argument("--tuning", type=int, default=None,
@@ -699,7 +699,7 @@ SERVE_SEED = 7
 SERVE_RATE = 5000.0        # headline arrival rate, req/s (saturates the server)
 SERVE_SWEEP = (100.0, 1000.0, 5000.0)
 SERVE_CPU_SAMPLE = 32      # new-scene requests per reference-arm step
-SERVE_LANES = 2            # server form: 0 synchronous steps, 2 asynchronous lanes
+SERVE_LANES = 3            # server form: 0 synchronous steps, 2 or 3 asynchronous lanes
 
 
 def serve_desc(win):
@@ -847,8 +847,10 @@ def run_serve(args):
                    "server": {"slots": served["max_slots"], "quantum_phases": served["quantum"],
                               "power_loop_per_step": served["power_launches"],
                               "small_instances": "cluster solver, to completion within a run",
-                              "lanes": ("two asynchronous lanes (small, large)" if args.lanes
-                                        else "one synchronous run per step")},
+                              "lanes": {0: "one synchronous run per step",
+                                        2: "two asynchronous lanes (small, large)",
+                                        3: "three asynchronous lanes (small, large, large "
+                                           "in the power method)"}[args.lanes]},
                    "inputs": "staged in device memory before the timed region (e2e: pinned host)",
                    "autotune": tuning,
                    "l2": "flushed before every window (256 MB device write)",

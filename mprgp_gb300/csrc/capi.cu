@@ -47,9 +47,10 @@ using namespace mprgp;
 
 // Device and pinned-host resources of one engine lane, and the run in flight
 // on it.  Lane 0 runs on the context stream (the synchronous calls); the
-// server's asynchronous form runs the small instances on lane 1 and the large
-// ones on lane 2, each on a stream of its own, so one lane's run never waits
-// for the other's.
+// server's asynchronous form runs the small instances on lane 1, the large
+// ones' MPRGP phases on lane 2 and (in its three-lane form) their power
+// method on lane 3, each on a stream of its own, so no lane's run waits for
+// another's.
 struct LaneRun {
   bool active = false;
   int n = 0, n_large = 0, quantum = 0, cluster_quantum = 0, power_launches = 0;
@@ -88,7 +89,7 @@ struct Lane {
   HostIO *io = nullptr;
   LaneRun run;
 };
-constexpr int kLanes = 3;
+constexpr int kLanes = 4;
 
 struct mprgp_context {
   int device = 0;
@@ -580,14 +581,33 @@ int engine_lane_of(const mprgp_context *c, int nv) {
   return cluster_class(c, nitems_of(nv)) >= 0 ? 1 : 2;
 }
 
+// Whether a solve of `p` started now with options `o` begins with the power
+// method (it does unless the exact power-method cache applies).
+int engine_needs_power(const mprgp_problem *p, const mprgp_options *o) {
+  if (o->use_ev && p->ev_valid) return 1;  // warm-started power method
+  int kind, alg, pre;
+  if (resolve_options(p, o, &kind, &alg, &pre)) return 1;
+  const int prec = (alg == ALG_MONOTONE) ? o->precision : PREC_FP64;
+  const bool cached = p->pcache_on && p->pcache.valid && p->pcache.seed == o->seed &&
+                      p->pcache.prec == prec && p->pcache.gen == p->matrix_gen;
+  return cached ? 0 : 1;
+}
+
+// Whether `p` was left in a power-method phase by its last engine run.
+int engine_in_power(const mprgp_problem *p) {
+  const int ph = p->phase_host;
+  return ph == PH_POW_RAND || ph == PH_POW || ph == PH_POW_LAST;
+}
+
 // Starts one engine run over `n` problems on lane `k` and returns without
 // waiting for it.  Instances with fresh[i] != 0 start a solve (their initial
 // state is uploaded); the others resume from the state left in device memory
 // by the previous run.  The run advances the large instances by at most
-// `quantum` macro-phases (0: until all are done) after up to `power_launches`
-// launches of the power kernel, and the small ones (cluster solver) by at
-// most `cluster_quantum` phases (0: until done).  The problems must stay
-// untouched until engine_end.
+// `quantum` macro-phases (0: until all are done; < 0: none, the run is the
+// power loop alone) after up to `power_launches` launches of the power
+// kernel, and the small ones (cluster solver) by at most `cluster_quantum`
+// phases (0: until done).  The problems must stay untouched until
+// engine_end.
 int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
                  const mprgp_options *opts, const int *fresh, int quantum, int power_launches,
                  int cluster_quantum) {
@@ -729,7 +749,8 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   // or the same phases as a graph loop of the all-phase kernel -- always the
   // latter while another lane has a run in flight, since a cooperative launch
   // needs every one of its CTAs resident at once.
-  R.egraph = n_large > 0 && (c->engine_graph || k != 0 || other_lanes_active(c, k));
+  R.egraph = n_large > 0 && quantum >= 0 &&
+             (c->engine_graph || k != 0 || other_lanes_active(c, k));
   cudaGraphExec_t eexec = nullptr;
   if (R.egraph) {
     rc = power_graph(L, power_grid(c, prefix[n_large], 2), 2, &eexec);
@@ -762,7 +783,7 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   for (int q = 0; q < kClusterClasses; ++q)
     if (R.class_n[q]) CK(cudaStreamWaitEvent(s, L.join_ev[q], 0));
   if (R.egraph) CK(cudaGraphLaunch(eexec, s));
-  else if (n_large > 0) CK(launch_engine(args, grid, s));
+  else if (n_large > 0 && quantum >= 0) CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(L.e1, s));
   if (R.power) CK(cudaMemcpyAsync(&io.pc_out[0], L.d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   if (R.egraph) CK(cudaMemcpyAsync(&io.pc_out[1], L.d_pc2, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
@@ -813,7 +834,7 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
   if (R.egraph)
     c->launches += (long long)kPowerUnroll * ((io.pc_out[1].launches + kPowerUnroll - 1) / kPowerUnroll);
   else
-    c->launches += n_large > 0 ? 1 : 0;
+    c->launches += (n_large > 0 && R.quantum >= 0) ? 1 : 0;
   c->launches += 2;  // state scatter and gather
   c->solver_ms += ms;
   const Ctl &ctl1 = io.ctl_out;
@@ -827,7 +848,7 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
     // an engine error concerns the engine's instances; an instance left
     // unfinished by a run that had no phase limit hit the hard phase bound
     const bool err = large && ctl1.err;
-    const bool unbounded = (large ? R.quantum : R.cluster_quantum) <= 0;
+    const bool unbounded = (large ? R.quantum : R.cluster_quantum) == 0;
     if (err) x.code = ctl1.err;
     else if (!finished && unbounded) x.code = MPRGP_TIMEOUT;
     p->xc = x.xc;

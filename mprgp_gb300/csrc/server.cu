@@ -38,6 +38,8 @@ int engine_begin(mprgp_context *c, int lane, int n, mprgp_problem *const *probs,
 int engine_ready(mprgp_context *c, int lane);
 int engine_end(mprgp_context *c, int lane, mprgp_stats *stats, int *done);
 int engine_lane_of(const mprgp_context *c, int nv);
+int engine_needs_power(const mprgp_problem *p, const mprgp_options *o);
+int engine_in_power(const mprgp_problem *p);
 void set_last_error(const char *what);
 }  // namespace mprgp
 
@@ -57,7 +59,7 @@ struct Request {
   const double *p_vals = nullptr, *p_b = nullptr, *p_planes = nullptr, *p_x0 = nullptr;
   mprgp_options opt{};
   int state = 0;  // 0 queued, 1 running, 2 done
-  int lane = 0;   // asynchronous form: 0 small, 1 large
+  int lane = 0;   // asynchronous form: 0 small, 1 large, 2 large in the power method
   bool fresh = true;  // the next run starts its solve
   int code = 0;
   std::vector<double> x;
@@ -98,13 +100,14 @@ struct mprgp_server {
   std::vector<long long> running;
   std::vector<char> fresh_flag;  // parallel to running
   std::deque<long long> completed;  // finished, not yet polled
-  // asynchronous form: per lane (small, large) the admitted requests waiting
-  // for its next run and those in its run in flight
+  // asynchronous form: per lane (small; large; large in the power method,
+  // three-lane form only) the admitted requests waiting for its next run and
+  // those in its run in flight.  Server lane l runs on engine lane l + 1.
   int lanes = 0;
   struct LaneQ {
     std::vector<long long> pending, in_run;
     bool active = false;
-  } lane[2];
+  } lane[3];
 };
 
 namespace {
@@ -226,6 +229,9 @@ void admit_queued(mprgp_server *s) {
     r.fresh = true;
     if (s->lanes) {
       r.lane = mprgp::engine_lane_of(s->ctx, r.nv) == 1 ? 0 : 1;
+      if (r.lane == 1 && s->lanes == 3 &&
+          mprgp::engine_needs_power(s->scenes[r.scene].prob, &r.opt))
+        r.lane = 2;
       s->lane[r.lane].pending.push_back(r.ticket);
     } else {
       s->running.push_back(r.ticket);
@@ -284,7 +290,9 @@ int step_sync(mprgp_server *s, int *ncomp) {
   return MPRGP_OK;
 }
 
-// Takes the results of lane l's run if it has finished.
+// Takes the results of lane l's run if it has finished.  Unfinished
+// requests lead the lane's next run, except that those of the power lane
+// that have left the power method move on to the large lane.
 int finish_lane(mprgp_server *s, int l, int *ncomp) {
   auto &q = s->lane[l];
   if (!q.active || mprgp::engine_ready(s->ctx, 1 + l) == 0) return MPRGP_OK;
@@ -299,14 +307,18 @@ int finish_lane(mprgp_server *s, int l, int *ncomp) {
     Request &r = s->reqs[q.in_run[i]];
     if (!done[i]) {
       r.fresh = false;
-      keep.push_back(r.ticket);
+      if (l == 2 && !mprgp::engine_in_power(s->scenes[r.scene].prob)) {
+        r.lane = 1;
+        s->lane[1].pending.push_back(r.ticket);
+      } else {
+        keep.push_back(r.ticket);
+      }
       continue;
     }
     retire(s, r, st[i]);
     ++*ncomp;
   }
   q.in_run.clear();
-  // unfinished requests lead the lane's next run
   q.pending.insert(q.pending.begin(), keep.begin(), keep.end());
   return MPRGP_OK;
 }
@@ -327,8 +339,12 @@ int start_lane(mprgp_server *s, int l) {
     opts[i] = r.opt;
     fresh[i] = r.fresh ? 1 : 0;
   }
+  // the power lane runs the power loop alone; with it, the large lane runs
+  // no power loop of its own
+  const int quantum = l == 2 ? -1 : s->quantum;
+  const int power = (l == 1 && s->lanes == 3) ? 0 : s->power_launches;
   const int rc = mprgp::engine_begin(s->ctx, 1 + l, n, probs.data(), opts.data(), fresh.data(),
-                                     s->quantum, s->power_launches, s->cluster_quantum);
+                                     quantum, power, s->cluster_quantum);
   if (rc) return rc;
   q.active = true;
   return MPRGP_OK;
@@ -338,14 +354,15 @@ int start_lane(mprgp_server *s, int l) {
 // idle lane; when none of that happened, wait a little for a lane to finish
 // (the caller may have requests to submit meanwhile).
 int step_async(mprgp_server *s, int *ncomp) {
-  for (int l = 0; l < 2; ++l) {
+  const int nl = s->lanes == 3 ? 3 : 2;
+  for (int l = nl - 1; l >= 0; --l) {  // the power lane first: it feeds the large lane
     const int rc = finish_lane(s, l, ncomp);
     if (rc) return rc;
   }
   const size_t queued = s->queue.size();
   admit_queued(s);
   bool started = false;
-  for (int l = 0; l < 2; ++l) {
+  for (int l = 0; l < nl; ++l) {
     const bool idle = !s->lane[l].active;
     const int rc = start_lane(s, l);
     if (rc) return rc;
@@ -355,7 +372,7 @@ int step_async(mprgp_server *s, int *ncomp) {
   const double until = now_s() + 5e-4;
   while (now_s() < until) {
     bool any = false, ready = false;
-    for (int l = 0; l < 2; ++l) {
+    for (int l = 0; l < nl; ++l) {
       if (!s->lane[l].active) continue;
       any = true;
       ready |= mprgp::engine_ready(s->ctx, 1 + l) != 0;
@@ -381,9 +398,9 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
   if (cfg && cfg->quantum_phases < 0) s->quantum = 0;  // each step runs to completion
   if (cfg && cfg->cluster_quantum > 0) s->cluster_quantum = cfg->cluster_quantum;
   if (cfg && cfg->power_launches >= 0) s->power_launches = std::min(cfg->power_launches, 1003);
-  if (cfg && cfg->lanes != 0 && cfg->lanes != 2) {
+  if (cfg && cfg->lanes != 0 && cfg->lanes != 2 && cfg->lanes != 3) {
     delete s;
-    return err(MPRGP_INVALID, "server_create: lanes must be 0 or 2");
+    return err(MPRGP_INVALID, "server_create: lanes must be 0, 2 or 3");
   }
   s->lanes = cfg ? cfg->lanes : 0;
   *out = s;
@@ -392,7 +409,7 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
 
 int mprgp_server_destroy(mprgp_server *s) {
   if (!s) return MPRGP_OK;
-  for (int l = 0; l < 2; ++l)  // runs in flight end before their problems go
+  for (int l = 0; l < 3; ++l)  // runs in flight end before their problems go
     if (s->lane[l].active) mprgp::engine_end(s->ctx, 1 + l, nullptr, nullptr);
   for (auto &kv : s->scenes) mprgp_problem_destroy(kv.second.prob);
   delete s;

@@ -31,7 +31,7 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("lanes", [0, 2])
+@pytest.mark.parametrize("lanes", [0, 2, 3])
 @pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
 def test_same_alone_and_in_the_mix(ctx, precision, lanes):
     # sizes on both sides of the cluster solver's limit (16 items of 256
@@ -69,7 +69,7 @@ def test_same_alone_and_in_the_mix(ctx, precision, lanes):
     srv.close()
 
 
-@pytest.mark.parametrize("lanes", [0, 2])
+@pytest.mark.parametrize("lanes", [0, 2, 3])
 def test_followup_warm_start(ctx, lanes):
     qp = M.beam(6, 5, 10, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=3)
     srv = M.Server(ctx, quantum_phases=128, power_launches=256, lanes=lanes)
@@ -103,7 +103,7 @@ def test_followup_warm_start(ctx, lanes):
     srv.close()
 
 
-@pytest.mark.parametrize("lanes", [0, 2])
+@pytest.mark.parametrize("lanes", [0, 2, 3])
 def test_admission_by_hbm_budget(ctx, lanes):
     qps = [M.beam(8, 8, 16, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=s)
            for s in range(4)]
