@@ -28,6 +28,9 @@ constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:
 #ifndef MPRGP_SPMV_CHUNK
 #define MPRGP_SPMV_CHUNK 4
 #endif
+#ifndef MPRGP_SPMV_MIN_BLOCKS  // resident CTAs per SM the standalone SpMV is compiled for
+#define MPRGP_SPMV_MIN_BLOCKS 4
+#endif
 #ifndef MPRGP_ENGINE_MIN_BLOCKS
 #define MPRGP_ENGINE_MIN_BLOCKS 4
 #endif
@@ -64,6 +67,46 @@ __device__ __forceinline__ void ld3(const double *b, int v, double o[3]) {
   o[1] = q[1];
   o[2] = q[2];
 }
+// SELL values of one 3x3 block (slot j of the matrix, lane l of its slice),
+// stored so that a lane reads its nine entries with vector loads that are
+// still coalesced across the warp.  Per slot, 288 values:
+//   FP32: m0..m3 as float4 at 4l, m4..m7 as float4 at 128 + 4l, m8 at 256 + l;
+//   FP64: (m0,m1), (m2,m3), (m4,m5), (m6,m7) as double2 at 64k + 2l, m8 at 256 + l.
+// Each slot starts on a 1152-byte (FP32) or 2304-byte (FP64) boundary.
+__host__ __device__ __forceinline__ size_t sell_index(size_t j, int e, int lane, float) {
+  const size_t b = j * (9 * kSlice);
+  return e < 4 ? b + 4 * lane + e : (e < 8 ? b + 128 + 4 * lane + (e - 4) : b + 256 + lane);
+}
+__host__ __device__ __forceinline__ size_t sell_index(size_t j, int e, int lane, double) {
+  const size_t b = j * (9 * kSlice);
+  return e < 8 ? b + 64 * (e >> 1) + 2 * lane + (e & 1) : b + 256 + lane;
+}
+__device__ __forceinline__ void ld_block(const float *vals, size_t j, int lane, float m[9]) {
+  const float *b = vals + j * (9 * kSlice);
+  float4 p, q;
+  asm("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w) : "l"(b + 4 * lane));
+  asm("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+      : "=f"(q.x), "=f"(q.y), "=f"(q.z), "=f"(q.w) : "l"(b + 128 + 4 * lane));
+  m[0] = p.x; m[1] = p.y; m[2] = p.z; m[3] = p.w;
+  m[4] = q.x; m[5] = q.y; m[6] = q.z; m[7] = q.w;
+  m[8] = ldro(b + 256 + lane);
+}
+__device__ __forceinline__ void ld_block(const double *vals, size_t j, int lane, double m[9]) {
+  const double *b = vals + j * (9 * kSlice);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    asm("ld.global.nc.v2.f64 {%0, %1}, [%2];"
+        : "=d"(m[2 * k]), "=d"(m[2 * k + 1]) : "l"(b + 64 * k + 2 * lane));
+  m[8] = ldro(b + 256 + lane);
+}
+// The same from a shared-memory copy of whole slots.
+template <typename VT>
+__device__ __forceinline__ void ld_block_smem(const VT *vals, size_t j, int lane, VT m[9]) {
+#pragma unroll
+  for (int e = 0; e < 9; ++e) m[e] = vals[sell_index(j, e, lane, VT())];
+}
+
 __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
   unsigned int v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -226,15 +269,13 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       if (cc[u] < 0) break;
-      const VT *q = vals + (size_t)(jb + u) * (9 * kSlice) + lane;
-      const VT m0 = ldro(q), m1 = ldro(q + 32), m2 = ldro(q + 64);
-      const VT m3 = ldro(q + 96), m4 = ldro(q + 128), m5 = ldro(q + 160);
-      const VT m6 = ldro(q + 192), m7 = ldro(q + 224), m8 = ldro(q + 256);
+      VT m[9];
+      ld_block(vals, (size_t)(jb + u), lane, m);
       VT xv[3];
       src(cc[u], xv);
-      a0 = fma(m0, xv[0], a0); a0 = fma(m1, xv[1], a0); a0 = fma(m2, xv[2], a0);
-      a1 = fma(m3, xv[0], a1); a1 = fma(m4, xv[1], a1); a1 = fma(m5, xv[2], a1);
-      a2 = fma(m6, xv[0], a2); a2 = fma(m7, xv[1], a2); a2 = fma(m8, xv[2], a2);
+      a0 = fma(m[0], xv[0], a0); a0 = fma(m[1], xv[1], a0); a0 = fma(m[2], xv[2], a0);
+      a1 = fma(m[3], xv[0], a1); a1 = fma(m[4], xv[1], a1); a1 = fma(m[5], xv[2], a1);
+      a2 = fma(m[6], xv[0], a2); a2 = fma(m[7], xv[1], a2); a2 = fma(m[8], xv[2], a2);
     }
   }
 #else
@@ -245,11 +286,7 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     for (int u = 0; u < K; ++u) c[u] = ldro(A.cols + (size_t)(jb + u) * kSlice + lane);
     VT m[K][9];
 #pragma unroll
-    for (int u = 0; u < K; ++u) {
-      const VT *q = vals + (size_t)(jb + u) * (9 * kSlice) + lane;
-#pragma unroll
-      for (int e = 0; e < 9; ++e) m[u][e] = ldro(q + 32 * e);
-    }
+    for (int u = 0; u < K; ++u) ld_block(vals, (size_t)(jb + u), lane, m[u]);
     VT xv[K][3];
 #pragma unroll
     for (int u = 0; u < K; ++u) src(c[u], xv[u]);
@@ -263,10 +300,8 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
   }
   for (; jb < j1; ++jb) {  // the last slots of the row
     const int c = ldro(A.cols + (size_t)jb * kSlice + lane);
-    const VT *q = vals + (size_t)jb * (9 * kSlice) + lane;
     VT m[9];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) m[e] = ldro(q + 32 * e);
+    ld_block(vals, (size_t)jb, lane, m);
     VT xv[3];
     src(c, xv);
     a0 = fma(m[0], xv[0], a0); a0 = fma(m[1], xv[1], a0); a0 = fma(m[2], xv[2], a0);
@@ -293,10 +328,8 @@ __device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (c[u] < 0) break;
-      const double *q = A.v64 + (size_t)(jb + u) * (9 * kSlice) + lane;
       double m[9];
-#pragma unroll
-      for (int e = 0; e < 9; ++e) m[e] = ldro(q + 32 * e);
+      ld_block(A.v64, (size_t)(jb + u), lane, m);
       double x[3], y[3];
       s1(c[u], x);
       s2(c[u], y);
@@ -332,11 +365,12 @@ __device__ __forceinline__ void spmv_row_staged(const SellMatrix &A, int v, cons
       if (c[u] < 0) break;
       VT xv[3];
       src(c[u], xv);
-      const VT *q = vs + (size_t)(jb + u - base) * (9 * kSlice) + lane;
+      VT m[9];
+      ld_block_smem(vs, (size_t)(jb + u - base), lane, m);
       const VT x0 = xv[0], x1 = xv[1], x2 = xv[2];
-      a0 = fma(q[0], x0, a0); a0 = fma(q[32], x1, a0); a0 = fma(q[64], x2, a0);
-      a1 = fma(q[96], x0, a1); a1 = fma(q[128], x1, a1); a1 = fma(q[160], x2, a1);
-      a2 = fma(q[192], x0, a2); a2 = fma(q[224], x1, a2); a2 = fma(q[256], x2, a2);
+      a0 = fma(m[0], x0, a0); a0 = fma(m[1], x1, a0); a0 = fma(m[2], x2, a0);
+      a1 = fma(m[3], x0, a1); a1 = fma(m[4], x1, a1); a1 = fma(m[5], x2, a1);
+      a2 = fma(m[6], x0, a2); a2 = fma(m[7], x1, a2); a2 = fma(m[8], x2, a2);
     }
   }
   out[0] = (OT)a0;
@@ -2048,8 +2082,8 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
     }
     out_cols[slot * kSlice + lane] = c;
     for (int e = 0; e < 9; ++e) {
-      if (out64) out64[(slot * 9 + e) * kSlice + lane] = m[e];
-      if (out32) out32[(slot * 9 + e) * kSlice + lane] = (float)m[e];
+      if (out64) out64[sell_index(slot, e, lane, double())] = m[e];
+      if (out32) out32[sell_index(slot, e, lane, float())] = (float)m[e];
     }
   }
   if (q < nv)
@@ -2080,7 +2114,7 @@ __global__ void planes_setup_kernel(int nv, const int *__restrict__ plane_ptr,
 
 // Standalone y = A x (FixedSparseMatrix::multiply, MPRGPSolver.h:469-473).
 template <typename VT>
-__global__ void __launch_bounds__(256) spmv_kernel(SellMatrix A, const VT *__restrict__ vals,
+__global__ void __launch_bounds__(256, MPRGP_SPMV_MIN_BLOCKS) spmv_kernel(SellMatrix A, const VT *__restrict__ vals,
                                                    int nv, const double *__restrict__ x,
                                                    double *__restrict__ y) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
