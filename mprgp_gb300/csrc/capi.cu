@@ -36,9 +36,9 @@ void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const doubl
                         float *out32, double *dinv, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st);
-void launch_state_scatter(const InstDesc *desc, int n, const InstState *in, const int *fresh,
-                          cudaStream_t st);
-void launch_state_gather(const InstDesc *desc, int n, InstState *out, cudaStream_t st);
+void launch_state_scatter(const InstDesc *desc, int n, InstState *states, InstState *const *home,
+                          const int *fresh, cudaStream_t st);
+void launch_state_gather(int n, const InstState *states, InstState *const *home, cudaStream_t st);
 void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
                  cudaStream_t st);
 }  // namespace mprgp
@@ -80,12 +80,15 @@ struct Lane {
   // loop graphs of the phase kernel, keyed grid * 4 + variant (they hold
   // this lane's d_args / d_pc / d_pc2)
   std::map<int, std::pair<cudaGraph_t, cudaGraphExec_t>> graphs;
-  // per-run arrays in desc order (grown on demand)
-  int cap = 0;
+  // per-run arrays in desc order (grown on demand); d_st holds the run's
+  // instance states, home their problems' own state blocks
+  int cap = 0, icap = 0;
   InstDesc *d_desc = nullptr, *h_desc = nullptr;
   int *d_prefix = nullptr, *h_prefix = nullptr;
   InstState *d_st = nullptr, *h_st_in = nullptr, *h_st_out = nullptr;
+  InstState **d_home = nullptr, **h_home = nullptr;
   int *d_fresh = nullptr, *h_fresh = nullptr;
+  int *d_item_inst = nullptr, *h_item_inst = nullptr;  // items of the large instances
   HostIO *io = nullptr;
   LaneRun run;
 };
@@ -508,12 +511,16 @@ void lane_free(mprgp_context *c, Lane &L) {
   dfree(c, L.d_prefix);
   dfree(c, L.d_st);
   dfree(c, L.d_fresh);
+  dfree(c, L.d_home);
+  dfree(c, L.d_item_inst);
   cudaStreamSynchronize(c->stream);
   cudaFreeHost(L.h_desc);
   cudaFreeHost(L.h_prefix);
   cudaFreeHost(L.h_st_in);
   cudaFreeHost(L.h_st_out);
   cudaFreeHost(L.h_fresh);
+  cudaFreeHost(L.h_home);
+  cudaFreeHost(L.h_item_inst);
   cudaFreeHost(L.io);
   for (auto &kv : L.graphs) {
     cudaGraphExecDestroy(kv.second.second);
@@ -534,33 +541,50 @@ void lane_free(mprgp_context *c, Lane &L) {
   L = Lane();
 }
 
-// Grows a lane's per-run arrays to `n` instances (the lane is idle).
-int lane_reserve(mprgp_context *c, Lane &L, int n) {
+// Grows a lane's per-run arrays to `n` instances and `items` items of large
+// instances (the lane is idle).
+int lane_reserve(mprgp_context *c, Lane &L, int n, int items) {
+  if (items > L.icap) {
+    const int icap = std::max(1024, std::max(items, 2 * L.icap));
+    dfree(c, L.d_item_inst);
+    cudaFreeHost(L.h_item_inst);
+    L.h_item_inst = nullptr;
+    L.icap = 0;
+    int rc = dalloc(c, &L.d_item_inst, icap);
+    if (rc) return rc;
+    CK(cudaMallocHost((void **)&L.h_item_inst, sizeof(int) * icap));
+    L.icap = icap;
+  }
   if (n <= L.cap) return MPRGP_OK;
   const int cap = std::max(64, std::max(n, 2 * L.cap));
   dfree(c, L.d_desc);
   dfree(c, L.d_prefix);
   dfree(c, L.d_st);
   dfree(c, L.d_fresh);
+  dfree(c, L.d_home);
   cudaFreeHost(L.h_desc);
   cudaFreeHost(L.h_prefix);
   cudaFreeHost(L.h_st_in);
   cudaFreeHost(L.h_st_out);
   cudaFreeHost(L.h_fresh);
+  cudaFreeHost(L.h_home);
   L.h_desc = nullptr;
   L.h_prefix = L.h_fresh = nullptr;
   L.h_st_in = L.h_st_out = nullptr;
+  L.h_home = nullptr;
   L.cap = 0;
   int rc = dalloc(c, &L.d_desc, cap);
   if (!rc) rc = dalloc(c, &L.d_prefix, cap + 1);
   if (!rc) rc = dalloc(c, &L.d_st, cap);
   if (!rc) rc = dalloc(c, &L.d_fresh, cap);
+  if (!rc) rc = dalloc(c, &L.d_home, cap);
   if (rc) return rc;
   CK(cudaMallocHost((void **)&L.h_desc, sizeof(InstDesc) * cap));
   CK(cudaMallocHost((void **)&L.h_prefix, sizeof(int) * (cap + 1)));
   CK(cudaMallocHost((void **)&L.h_st_in, sizeof(InstState) * cap));
   CK(cudaMallocHost((void **)&L.h_st_out, sizeof(InstState) * cap));
   CK(cudaMallocHost((void **)&L.h_fresh, sizeof(int) * cap));
+  CK(cudaMallocHost((void **)&L.h_home, sizeof(InstState *) * cap));
   L.cap = cap;
   return MPRGP_OK;
 }
@@ -616,8 +640,6 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   if (rc) return rc;
   Lane &L = c->lane[k];
   if (L.run.active) return fail(MPRGP_INVALID, "engine lane busy");
-  rc = lane_reserve(c, L, n);
-  if (rc) return rc;
   // Small instances run on the cluster solver, one cluster each, grouped by
   // cluster size (the smallest usable size that gives every CTA its items);
   // the others on the power loop and the engine.  The desc array holds the
@@ -627,15 +649,21 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   R.opts.assign(opts, opts + n);
   R.pos.assign(n, 0);
   std::vector<int> cls(n);
-  int n_large = 0;
+  int n_large = 0, large_items = 0;
   for (int q = 0; q < kClusterClasses; ++q) R.class_n[q] = 0;
   for (int i = 0; i < n; ++i) {
     mprgp_problem *p = probs[i];
     if (!p || p->ctx != c) return fail(MPRGP_INVALID, "problem/context mismatch");
     cls[i] = cluster_class(c, nitems_of(p->nv));
-    if (cls[i] < 0) R.pos[i] = n_large++;
-    else R.class_n[cls[i]]++;
+    if (cls[i] < 0) {
+      R.pos[i] = n_large++;
+      large_items += nitems_of(p->nv);
+    } else {
+      R.class_n[cls[i]]++;
+    }
   }
+  rc = lane_reserve(c, L, n, large_items);
+  if (rc) return rc;
   int class_off[kClusterClasses];
   {
     int f = n_large;
@@ -662,6 +690,8 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
     const int j = R.pos[i];
     rc = prepare(p, &opts[i], j < n_large ? prefix[j] : 0, &desc[j], &st[j]);
     if (rc) return rc;
+    desc[j].st = L.d_st + j;  // the run's state array
+    L.h_home[j] = p->st;
     L.h_fresh[j] = fresh[i] ? 1 : 0;
     wait_s = std::max(wait_s, opts[i].wait_limit_s);
     // Each MPRGP iteration takes at most 4 phases (CG: spmv, candidate,
@@ -705,7 +735,13 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   CK(cudaMemcpyAsync(L.d_prefix, prefix, sizeof(int) * (n_large + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(L.d_st, st, sizeof(InstState) * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(L.d_fresh, L.h_fresh, sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  launch_state_scatter(L.d_desc, n, L.d_st, L.d_fresh, s);
+  CK(cudaMemcpyAsync(L.d_home, L.h_home, sizeof(InstState *) * n, cudaMemcpyHostToDevice, s));
+  for (int j = 0; j < n_large; ++j)
+    for (int t = prefix[j]; t < prefix[j + 1]; ++t) L.h_item_inst[t] = j;
+  if (large_items > 0)
+    CK(cudaMemcpyAsync(L.d_item_inst, L.h_item_inst, sizeof(int) * large_items,
+                       cudaMemcpyHostToDevice, s));
+  launch_state_scatter(L.d_desc, n, L.d_st, L.d_home, L.d_fresh, s);
   CK(cudaGetLastError());
   HostIO &io = *L.io;
   std::memset(&io.ctl_in, 0, sizeof(Ctl));
@@ -716,6 +752,8 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   std::memset(&args, 0, sizeof(args));
   args.desc = L.d_desc;
   args.item_prefix = L.d_prefix;
+  args.item_inst = L.d_item_inst;
+  args.states = L.d_st;
   args.ninst = n_large;
   args.total_items = prefix[n_large];
   long long maxp = phase_bound;
@@ -788,7 +826,7 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   if (R.power) CK(cudaMemcpyAsync(&io.pc_out[0], L.d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   if (R.egraph) CK(cudaMemcpyAsync(&io.pc_out[1], L.d_pc2, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&io.ctl_out, L.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
-  launch_state_gather(L.d_desc, n, L.d_st, s);
+  launch_state_gather(n, L.d_st, L.d_home, s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(L.h_st_out, L.d_st, sizeof(InstState) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(L.e_end, s));

@@ -1675,6 +1675,12 @@ __device__ __forceinline__ int find_instance(const int *prefix, int n, int item)
   }
   return lo;
 }
+// The instance of an item: one load from the run's item map, or a search of
+// the item prefix when the run has no map.
+__device__ __forceinline__ int instance_of(const int *item_inst, const int *prefix, int n,
+                                           int item) {
+  return item_inst ? ldro(item_inst + item) : find_instance(prefix, n, item);
+}
 
 __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kernel(EngineArgs args) {
   __shared__ InstDesc sD;
@@ -1695,7 +1701,7 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kern
   unsigned int stage_parity = 0;
   for (int ph = 0; ph < args.max_phases; ++ph) {
     for (int item = blockIdx.x; item < args.total_items; item += gridDim.x) {
-      const int inst = find_instance(args.item_prefix, args.ninst, item);
+      const int inst = instance_of(args.item_inst, args.item_prefix, args.ninst, item);
       if (inst != s_cache_inst || ph != s_cache_ph) {
         const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
         int *dstd = reinterpret_cast<int *>(&sD);
@@ -1826,25 +1832,31 @@ __device__ __forceinline__ bool power_phase(int ph) {
 // instance is in, with the same per-row work, reductions and transitions as
 // the persistent engine -- so any phase can run as a launch of a graph loop.
 template <bool kAll>
-__device__ __forceinline__ void phase_item(const InstDesc *desc, const int *item_prefix,
-                                           int ninst, int item, PowCtl *pc,
+__device__ __forceinline__ void phase_item(const EngineArgs &args, int item, PowCtl *pc,
                                            cudaGraphConditionalHandle h, int signal,
                                            InstDesc &sD, InstState &sS, RedBuf &red,
                                            double (&sums)[kPart], int &s_last) {
-  const int inst = find_instance(item_prefix, ninst, item);
+  const int inst = instance_of(args.item_inst, args.item_prefix, args.ninst, item);
   __syncthreads();  // the previous item's readers of sD/sS are done
+  // desc and state in one round of loads when the run's states are an array
+  // (desc order), else the state after the desc that points at it
   {
-    const int *srcd = reinterpret_cast<const int *>(desc + inst);
+    const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
     int *dstd = reinterpret_cast<int *>(&sD);
     for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads) dstd[w] = ldro(srcd + w);
   }
-  __syncthreads();
-  {
+  if (args.states) {
+    const int *srcs = reinterpret_cast<const int *>(args.states + inst);
+    int *dsts = reinterpret_cast<int *>(&sS);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads) dsts[w] = srcs[w];
+    __syncthreads();
+  } else {
+    __syncthreads();
     const int *srcs = reinterpret_cast<const int *>(sD.st);
     int *dsts = reinterpret_cast<int *>(&sS);
     for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads) dsts[w] = srcs[w];
+    __syncthreads();
   }
-  __syncthreads();
   const int phase = sS.phase;
   if (kAll ? phase == PH_DONE : !power_phase(phase)) return;
   const int local = item - sD.item_begin;
@@ -1928,11 +1940,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   __shared__ int s_last;
   if (*(volatile unsigned int *)&pc->stop) return;  // written by an earlier launch
   if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
-  const InstDesc *desc = pargs->desc;
-  const int *item_prefix = pargs->item_prefix;
-  const int ninst = pargs->ninst, total = pargs->total_items;
-  for (int item = blockIdx.x; item < total; item += gridDim.x)
-    phase_item<kAll>(desc, item_prefix, ninst, item, pc, h, signal, sD, sS, red, sums, s_last);
+  const EngineArgs args = *pargs;
+  for (int item = blockIdx.x; item < args.total_items; item += gridDim.x)
+    phase_item<kAll>(args, item, pc, h, signal, sD, sS, red, sums, s_last);
 }
 
 // ---------------------------------------------------- cluster solver -----
@@ -2126,39 +2136,47 @@ __global__ void __launch_bounds__(256, MPRGP_SPMV_MIN_BLOCKS) spmv_kernel(SellMa
   st3(y, v, o);
 }
 
-// An engine run's instance states move between host and device as one array
-// in desc order: the fresh instances' initial states are scattered to their
-// state blocks (with their phase-item counters cleared) before the run, and
-// every instance's state is gathered back after it.  One CTA per instance.
+// During an engine run the instance states live in one array in desc order
+// (the run's desc entries point into it), so a launch can fetch an item's
+// desc and state in one round of loads.  Between runs each state lives with
+// its problem (`home`).  Before a run the fresh instances' initial states are
+// already in the array (uploaded from the host) and their phase-item counters
+// are cleared, the others' states are copied in from home; after it every
+// state is copied back home (the array then also goes to the host).  One CTA
+// per instance.
 static_assert(sizeof(InstState) % 8 == 0, "InstState is copied as 8-byte words");
 constexpr int kStateWords = (int)(sizeof(InstState) / 8);
 
-__global__ void state_scatter_kernel(const InstDesc *__restrict__ desc, int n,
-                                     const InstState *__restrict__ in,
+__global__ void state_scatter_kernel(const InstDesc *__restrict__ desc, int n, InstState *states,
+                                     InstState *const *__restrict__ home,
                                      const int *__restrict__ fresh) {
   const int j = blockIdx.x;
-  if (j >= n || !fresh[j]) return;
-  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(in + j);
-  unsigned long long *dst = reinterpret_cast<unsigned long long *>(desc[j].st);
+  if (j >= n) return;
+  if (fresh[j]) {
+    if (threadIdx.x == 0) *desc[j].cnt = 0u;
+    return;
+  }
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(home[j]);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(states + j);
   for (int w = threadIdx.x; w < kStateWords; w += blockDim.x) dst[w] = src[w];
-  if (threadIdx.x == 0) *desc[j].cnt = 0u;
 }
 
-__global__ void state_gather_kernel(const InstDesc *__restrict__ desc, int n, InstState *out) {
+__global__ void state_gather_kernel(int n, const InstState *states,
+                                    InstState *const *__restrict__ home) {
   const int j = blockIdx.x;
   if (j >= n) return;
-  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(desc[j].st);
-  unsigned long long *dst = reinterpret_cast<unsigned long long *>(out + j);
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(states + j);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(home[j]);
   for (int w = threadIdx.x; w < kStateWords; w += blockDim.x) dst[w] = src[w];
 }
 
 // Host-side launch helpers (declared in capi.cu).
-void launch_state_scatter(const InstDesc *desc, int n, const InstState *in, const int *fresh,
-                          cudaStream_t st) {
-  if (n > 0) state_scatter_kernel<<<n, 64, 0, st>>>(desc, n, in, fresh);
+void launch_state_scatter(const InstDesc *desc, int n, InstState *states, InstState *const *home,
+                          const int *fresh, cudaStream_t st) {
+  if (n > 0) state_scatter_kernel<<<n, 64, 0, st>>>(desc, n, states, home, fresh);
 }
-void launch_state_gather(const InstDesc *desc, int n, InstState *out, cudaStream_t st) {
-  if (n > 0) state_gather_kernel<<<n, 64, 0, st>>>(desc, n, out);
+void launch_state_gather(int n, const InstState *states, InstState *const *home, cudaStream_t st) {
+  if (n > 0) state_gather_kernel<<<n, 64, 0, st>>>(n, states, home);
 }
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream) {
   void *params[] = {(void *)&args};

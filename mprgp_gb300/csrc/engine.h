@@ -155,6 +155,8 @@ struct ClusterArgs {
 struct EngineArgs {
   const InstDesc *desc;
   const int *item_prefix;  // ninst + 1
+  const int *item_inst;    // total_items: the instance of each item (nullptr: search item_prefix)
+  const InstState *states; // the run's instance states, desc order (== desc[i].st), or nullptr
   int ninst, total_items;
   int max_phases;          // quantum / hard bound on macro-phases
   long long wait_ns;       // bound on a barrier wait

@@ -282,6 +282,8 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   EngineArgs args;
   args.desc = d_desc;
   args.item_prefix = d_pref;
+  args.item_inst = nullptr;  // one instance
+  args.states = nullptr;
   args.ninst = 1;
   args.total_items = nitems;
   args.max_phases = (int)std::min<long long>(1100LL + 8LL * ((long long)opt->max_it + 2), INT_MAX);
