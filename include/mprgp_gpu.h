@@ -226,6 +226,32 @@ int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *row_ptr, cons
                         const double *planes, const mprgp_options *opt, double *x,
                         unsigned char *face, mprgp_stats *stats);
 
+/* ---- ICA: the reference's comparison contact solver ---------------------- */
+/* Replaces ICASolver (src/MPRGPSolver/ICASolver.h:287-463): ICASolver(max_it,
+ * tol, gs_max_it, gs_tol); reset(A, r); solve(J, p, x) -> bool;
+ * getIterations(), getResidual(), getLambda().  Solves
+ *   A x = r + J^T lambda,  0 <= lambda _|_ J x - p >= 0
+ * with A as 3x3-block CSR (host arrays, 9 values per block, row-major; every
+ * row holds its diagonal block) and J as per-vertex planes (n, q) with
+ * p = -q (0..3 planes a vertex; the reference's defaults are gs_max_it = 20,
+ * gs_tol = 1e-3).  x: initial guess in, solution out (3 nv); lambda: one
+ * multiplier per plane, in plane order.  Returns MPRGP_OK when the residual
+ * ||A x - r - J^T lambda|| reached tol (the reference's true), else
+ * MPRGP_NOT_CONVERGED; MPRGP_BUSY while the context's server has
+ * asynchronous runs in flight. */
+typedef struct mprgp_ica_stats {
+  int iterations;       /* the reference's getIterations() */
+  int converged;        /* 1: residual <= tol */
+  double residual;      /* getResidual() */
+  long long pgs_sweeps; /* projected Gauss-Seidel sweeps, all iterations */
+  int levels;           /* dependency levels of the 3x3-block sweep */
+  double device_ms;     /* device time of the solve */
+} mprgp_ica_stats;
+int mprgp_ica_solve(mprgp_context *ctx, int nv, int nnzb, const int *row_ptr, const int *cols,
+                    const double *vals, const double *r, const int *plane_ptr,
+                    const double *planes, double *x, double *lambda, int max_it, double tol,
+                    int gs_max_it, double gs_tol, mprgp_ica_stats *stats);
+
 /* ---- batched: many instances advance in one persistent launch ----------- */
 int mprgp_solve_batch(mprgp_context *ctx, int count, mprgp_problem *const *probs,
                       const mprgp_options *opts, mprgp_stats *stats);

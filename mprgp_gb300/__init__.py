@@ -31,6 +31,11 @@ class Options(C.Structure):
                 ("wait_limit_s", C.c_double)]
 
 
+class IcaStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("residual", C.c_double),
+                ("pgs_sweeps", C.c_longlong), ("levels", C.c_int), ("device_ms", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [("code", C.c_int), ("iterations", C.c_int), ("num_cg", C.c_int),
                 ("num_exp", C.c_int), ("num_prop", C.c_int), ("power_iters", C.c_int),
@@ -108,6 +113,8 @@ def _sig(lib):
       C.POINTER(Stats))
     s("mprgp_solve_noalloc", C.c_int, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P,
       C.POINTER(Options), _P, _P, C.POINTER(Stats))
+    s("mprgp_ica_solve", C.c_int, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int,
+      C.c_double, C.c_int, C.c_double, C.POINTER(IcaStats))
     s("mprgp_server_create", C.c_int, _P, C.POINTER(ServerConfig), C.POINTER(_P))
     s("mprgp_server_destroy", C.c_int, _P)
     s("mprgp_server_submit", C.c_int, _P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P,
@@ -367,6 +374,22 @@ class Context:
             _ptr(face), _ptr(ev), C.byref(st))
         _check(rc, "solve_bsr")
         return x, (face[:m] if face is not None else None), st
+
+    def ica_solve(self, qp: BeamQP, x0, r=None, max_it=1000, tol=1e-4, gs_max_it=20,
+                  gs_tol=1e-3):
+        """The ICA contact solver (mprgp_ica_solve, the reference's ICASolver)
+        on a beam QP: A x = r + J^T lambda, 0 <= lambda _|_ J x - c >= 0 with
+        r = b by default.  Returns (x, lambda, IcaStats); a run that did not
+        reach tol returns normally with stats.converged == 0."""
+        x = np.ascontiguousarray(x0, np.float64).copy()
+        lam = np.zeros(max(len(qp.planes), 1))
+        rhs = np.ascontiguousarray(qp.b if r is None else r, np.float64)
+        st = IcaStats()
+        _check(lib().mprgp_ica_solve(self.h, qp.nv, qp.nnzb, _ptr(qp.row_ptr), _ptr(qp.cols),
+                                     _ptr(qp.vals), _ptr(rhs), _ptr(qp.plane_ptr), _ptr(qp.planes),
+                                     _ptr(x), _ptr(lam), max_it, tol, gs_max_it, gs_tol,
+                                     C.byref(st)), "ica_solve")
+        return x, lam[:len(qp.planes)], st
 
     def solve_batch(self, probs, opts):
         n = len(probs)

@@ -20,7 +20,11 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libmprgp_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "server.cu", "fem.cu", "planes.cu", "beam.cpp"]
+SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "server.cu", "fem.cu", "planes.cu", "ica.cu",
+           "beam.cpp"]
+# ica.cu reproduces a CPU restatement operation for operation: no contraction
+# of products and sums into fused multiply-adds there.
+FILE_FLAGS = {"ica.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -35,7 +39,7 @@ def _compile(src: str, ptxas_verbose: bool) -> str:
     cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj, "-std=c++17", "-O3",
            "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
     if src.endswith(".cu"):
-        cmd += ARCH + ["-lineinfo"]
+        cmd += ARCH + ["-lineinfo"] + FILE_FLAGS.get(src, [])
         cmd += os.environ.get("MPRGP_NVCC_FLAGS", "").split()
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]

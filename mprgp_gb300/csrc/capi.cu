@@ -599,6 +599,11 @@ bool other_lanes_active(const mprgp_context *c, int k) {
 
 namespace mprgp {
 
+// Whether any asynchronous lane of the context has a run in flight.
+int context_lanes_busy(const mprgp_context *c) {
+  return other_lanes_active(c, 0) ? 1 : 0;
+}
+
 // Lane (1: small, 2: large) that the server's asynchronous form gives an
 // instance of `nv` vertices: small ones are those of the cluster solver.
 int engine_lane_of(const mprgp_context *c, int nv) {

@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstring>
 
+#include "ica_oracle.h"
 #include "mprgp_oracle.h"
 
 using namespace oracle;
@@ -273,6 +274,23 @@ int oracle_get_trace(double *out, int cap) {
   for (int i = 0; i < n && i < cap; ++i)
     for (int k = 0; k < 4; ++k) out[4 * i + k] = g_trace_buf[i][k];
   return n;
+}
+
+// ICA (ICASolver.h:287-393) on a BSR matrix and per-vertex planes; see
+// ica_oracle.h.  stats (4 doubles): iterations, converged, residual, PGS sweeps.
+int oracle_ica_solve(int nv, const int *row_ptr, const int *cols, const double *vals,
+                     const double *r, const int *plane_ptr, const double *planes, double *x,
+                     double *lambda, int max_it, double tol, int gs_max_it, double gs_tol,
+                     double *stats) {
+  const IcaStats st = ica_solve(nv, row_ptr, cols, vals, r, plane_ptr, planes, x, lambda, max_it,
+                                tol, gs_max_it, gs_tol);
+  if (stats) {
+    stats[0] = st.iterations;
+    stats[1] = st.converged;
+    stats[2] = st.residual;
+    stats[3] = (double)st.pgs_sweeps;
+  }
+  return st.converged ? 0 : -1;
 }
 
 }  // extern "C"

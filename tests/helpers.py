@@ -45,6 +45,9 @@ def oracle():
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_seeded_uniform.restype = C.c_double
         L.oracle_seeded_uniform.argtypes = [C.c_uint64, C.c_uint64]
+        L.oracle_ica_solve.restype = C.c_int
+        L.oracle_ica_solve.argtypes = [C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int, C.c_double,
+                                       C.c_int, C.c_double, _P]
         _orc = L
     return _orc
 
@@ -238,3 +241,20 @@ def collide_planes(x, planes, delta, decoupled=False):
         out.extend(mine)
         ptr.append(len(out))
     return np.asarray(ptr, np.int32), np.asarray(out, np.float64).reshape(-1, 4)
+
+
+def oracle_ica(qp, x0, r=None, max_it=1000, tol=1e-4, gs_max_it=20, gs_tol=1e-3):
+    """The restated reference ICA solver (ICASolver.h:287-393) on a beam QP:
+    A x = r + J^T lambda, 0 <= lambda _|_ J x - c >= 0.  Returns
+    (x, lambda, stats dict)."""
+    O = oracle()
+    x = np.ascontiguousarray(x0, np.float64).copy()
+    lam = np.zeros(max(len(qp.planes), 1))
+    st = np.zeros(4)
+    rhs = np.ascontiguousarray(qp.b if r is None else r, np.float64)
+    code = O.oracle_ica_solve(qp.nv, ptr(qp.row_ptr), ptr(qp.cols), ptr(qp.vals), ptr(rhs),
+                              ptr(qp.plane_ptr), ptr(qp.planes), ptr(x), ptr(lam), max_it, tol,
+                              gs_max_it, gs_tol, ptr(st))
+    return x, lam[:len(qp.planes)], {"code": code, "iterations": int(st[0]),
+                                     "converged": int(st[1]), "residual": float(st[2]),
+                                     "pgs_sweeps": int(st[3])}
