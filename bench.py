@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="c4: skip the arrival-rate sweep")
+    ap.add_argument("--no-ica", action="store_true",
+                    help="c0/c1: skip the ICA comparison solve beside the line")
     ap.add_argument("--lanes", type=int, default=SERVE_LANES, choices=[0, 2, 3],
                     help="c4: server form (0 one synchronous run per step, 2 asynchronous "
                          "small/large lanes, 3 plus a lane for the large ones' power method)")
@@ -338,6 +340,8 @@ def run_gb300(args):
     }
     if not args.no_e2e:
         line["e2e"] = run_e2e(ctx, qp, opt, args, world, mixed)
+    if not args.no_ica and args.config in ("c0", "c1"):
+        line["ica_comparison"] = run_ica(ctx, qp, tol, prob)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, cst = cpu_baseline(qp, 1)
         line["cpu_baseline"] = {
@@ -351,6 +355,26 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(line))
+
+
+def run_ica(ctx, qp, tol, prob):
+    """The reference's comparison (test_case/MPRGP_ICA_Compare.cpp,
+    script/data/ica_mprgp.txt): its ICA contact solver on the same QP and
+    stopping scale, on the GPU (mprgp_ica_solve), from the same start x0,
+    with the reference's projected Gauss-Seidel defaults (20 sweeps,
+    1e-3).  Reported beside the MPRGP solve: device time, iterations and the
+    distance between the two solutions."""
+    x_m = prob.get_x()
+    ms = []
+    for _ in range(2):
+        x, lam, st = ctx.ica_solve(qp, qp.x0, max_it=100000, tol=tol)
+        ms.append(st.device_ms)
+    return {"solver": "ICA (ICASolver.h:287-463) on the GPU, exact level-scheduled "
+                      "block Gauss-Seidel + per-vertex projected Gauss-Seidel",
+            "converged": bool(st.converged), "iterations": st.iterations,
+            "pgs_sweeps": int(st.pgs_sweeps), "levels": st.levels,
+            "device_ms": round(min(ms), 3), "residual": st.residual, "tol": tol,
+            "rel_diff_to_mprgp_x": float(np.linalg.norm(x - x_m) / np.linalg.norm(x_m))}
 
 
 def run_e2e(ctx, qp, opt, args, world, mixed):

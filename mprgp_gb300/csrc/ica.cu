@@ -194,8 +194,11 @@ __device__ __forceinline__ void row_sum(const IcaArgs &a, int v, const double *x
 }
 
 __global__ void __launch_bounds__(kIcaThreads) ica_kernel(IcaArgs a) {
+  __shared__ double s_blk[kIcaThreads / 32][32][12];  // per warp: 32 blocks + their x
   const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const int gthreads = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gwarp = gtid >> 5, gwarps = gthreads >> 5;
   // reset (:296-350): Da^-1 per block row; B = J Da^-1 J^T per vertex.
   for (int v = gtid; v < a.nv; v += gthreads) {
     double *inv = a.inv + 9 * (size_t)v;
@@ -266,24 +269,46 @@ __global__ void __launch_bounds__(kIcaThreads) ica_kernel(IcaArgs a) {
       for (int k = 0; k < 3; ++k) a.rhs[3 * v + k] = (jl[k] - ua[k]) + a.r[3 * v + k];
     }
     if (!ica_barrier(a.ctl, a.wait_ns)) return;
-    // 3x3-block Gauss-Seidel sweep (:377-388), level by level
+    // 3x3-block Gauss-Seidel sweep (:377-388), level by level, one warp per
+    // block row: the lanes fetch the row's lower blocks and their x together
+    // (one round of loads); lane k (k < 3) then subtracts them from scalar
+    // row k in column order, and lane k forms component k of the new x.
     for (int lv = 0; lv < a.nlevels; ++lv) {
-      for (int t = a.lvl_ptr[lv] + gtid; t < a.lvl_ptr[lv + 1]; t += gthreads) {
+      for (int t = a.lvl_ptr[lv] + gwarp; t < a.lvl_ptr[lv + 1]; t += gwarps) {
         const int v = a.order[t];
-        double rv[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          double acc = a.rhs[3 * v + k];
-          for (int j = a.row_ptr[v]; j < a.row_ptr[v + 1]; ++j) {
-            const int u = a.cols[j];
-            if (u >= v) continue;
+        const int k0 = a.row_ptr[v], k1 = a.row_ptr[v + 1];
+        double acc = lane < 3 ? a.rhs[3 * v + lane] : 0.0;
+        for (int base = k0; base < k1; base += 32) {
+          const int j = base + lane;
+          const int u = j < k1 ? a.cols[j] : v;
+          const bool low = u < v;
+          if (low) {
             const double *blk = a.vals + 9 * (size_t)j;
             const double *xc = a.x + 3 * (size_t)u;
-            for (int b = 0; b < 3; ++b) acc -= blk[3 * k + b] * xc[b];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) s_blk[wid][lane][e] = blk[e];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) s_blk[wid][lane][9 + b] = xc[b];
           }
-          rv[k] = acc;
+          const unsigned int lower = __ballot_sync(0xffffffffu, low);
+          __syncwarp();
+          if (lane < 3) {
+            const int cnt = min(32, k1 - base);
+            for (int q = 0; q < cnt; ++q) {
+              if (!((lower >> q) & 1u)) continue;
+              const double *s = s_blk[wid][q];
+#pragma unroll
+              for (int b = 0; b < 3; ++b) acc -= s[3 * lane + b] * s[9 + b];
+            }
+          }
+          __syncwarp();
         }
-        mul3(a.inv + 9 * (size_t)v, rv, a.x + 3 * (size_t)v);
+        const double r0 = __shfl_sync(0xffffffffu, acc, 0), r1 = __shfl_sync(0xffffffffu, acc, 1),
+                     r2 = __shfl_sync(0xffffffffu, acc, 2);
+        if (lane < 3) {
+          const double *M = a.inv + 9 * (size_t)v + 3 * lane;
+          a.x[3 * (size_t)v + lane] = (M[0] * r0 + M[1] * r1) + M[2] * r2;
+        }
       }
       if (!ica_barrier(a.ctl, a.wait_ns)) return;
     }

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <random>
 
+#include "mprgp/ICASolver.h"
 #include "mprgp/MPRGPSolver.h"
 
 using namespace MATH;
@@ -95,6 +96,42 @@ int main() {
     std::printf("file-form solve: code %d\n", rc);
     CHECK(rc == 0 && (int)y.size() == n);
     std::remove(path.c_str());
+  }
+  {  // MPRGP vs ICA on one QP (test_case/MPRGP_ICA_Compare.cpp:12-83), n = 3 * 3
+    const int m3 = 9;
+    std::vector<double> Gd(m3 * m3), G(m3 * m3, 0.0), Jd(3 * m3, 0.0);
+    for (int i = 0; i < m3 * m3; ++i) Gd[i] = U(gen) + ((i % (m3 + 1)) == 0 ? 3.0 : 0.0);
+    for (int i = 0; i < m3; ++i)
+      for (int j = 0; j < m3; ++j)
+        for (int k = 0; k < m3; ++k) G[i * m3 + j] += Gd[k * m3 + i] * Gd[k * m3 + j];
+    for (int v = 0; v < 3; ++v) Jd[v * m3 + 3 * v + 1] = 1.0;  // y_v >= p_v
+    const SparseMatrix<double> A3 = from_dense(G, m3, m3), J3 = from_dense(Jd, 3, m3);
+    Vec<double> B3(m3), p3(3), x0(m3, 0.0);
+    for (int i = 0; i < m3; ++i) B3[i] = U(gen);
+    for (int v = 0; v < 3; ++v) p3[v] = 0.5 * U(gen);
+    Vec<double> xm = x0;
+    const int rc = MPRGPDecoupledCon<double>::solve<SparseMatrix<double>, true>(A3, B3, J3, p3, xm, 1e-12, 10000);
+    CHECK(rc == 0);
+    ICASolver ica(100000, 1e-12, 20, 1e-14);
+    ica.setName("ica with con");
+    ica.reset(A3, B3);
+    Vec<double> xi = x0;
+    CHECK(ica.solve(J3, p3, xi));
+    double d = 0.0, nx = 0.0, compl_ = 0.0;
+    for (int i = 0; i < m3; ++i) {
+      d += (xi[i] - xm[i]) * (xi[i] - xm[i]);
+      nx += xm[i] * xm[i];
+    }
+    for (int v = 0; v < 3; ++v) {
+      CHECK(ica.getLambda()[v] >= 0.0);
+      CHECK(xi[3 * v + 1] >= p3[v] - 1e-9);
+      compl_ += ica.getLambda()[v] * (xi[3 * v + 1] - p3[v]);
+    }
+    CHECK(std::sqrt(d) <= 1e-8 * std::sqrt(nx));
+    CHECK(std::fabs(compl_) <= 1e-9);
+    CHECK(ica.getResidual() <= 1e-12);
+    std::printf("ica: iterations %d residual %.3e |x_ica - x_mprgp| %.3e\n", ica.getIterations(),
+                ica.getResidual(), std::sqrt(d));
   }
   std::printf("%s (%d failures)\n", failures ? "FAILED" : "OK", failures);
   return failures ? 1 : 0;
