@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="c4: skip the arrival-rate sweep")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="c4: skip the plain FP64 one-at-a-time play (profiling runs)")
     ap.add_argument("--no-ica", action="store_true",
                     help="c0/c1: skip the ICA comparison solve beside the line")
     ap.add_argument("--lanes", type=int, default=SERVE_LANES, choices=[0, 2, 3],
@@ -823,14 +825,16 @@ def run_serve(args):
     total_ms = replicas.max_over_ranks(local_ms)
     lat = np.concatenate([r.latency_s for r in timed]) * 1e3
     # plain FP64, one request at a time, same stream and arrivals
-    base = check(pl.play(SERVE_RATE, M.PREC_FP64, "device", flush=flush, stream=stream,
-                         keep_x=True, **plain), "plain FP64")
-    # error of every served result against the plain FP64 GPU solve of the same QP
-    errs, same_face = [], 0
-    for i in range(n_req):
-        xs, xp = timed[0].xs[i], base.xs[i]
-        errs.append(float(np.linalg.norm(xs - xp) / max(np.linalg.norm(xp), 1e-300)))
-        same_face += int(np.array_equal(timed[0].faces[i], base.faces[i]))
+    base, errs, same_face = None, [float("nan")], 0
+    if not args.no_plain:
+        base = check(pl.play(SERVE_RATE, M.PREC_FP64, "device", flush=flush, stream=stream,
+                             keep_x=True, **plain), "plain FP64")
+        # error of every served result against the plain FP64 GPU solve of the same QP
+        errs = []
+        for i in range(n_req):
+            xs, xp = timed[0].xs[i], base.xs[i]
+            errs.append(float(np.linalg.norm(xs - xp) / max(np.linalg.norm(xp), 1e-300)))
+            same_face += int(np.array_equal(timed[0].faces[i], base.faces[i]))
     # arrival-rate sweep (one window each)
     sweep = []
     for rate in (() if args.no_sweep else SERVE_SWEEP):
@@ -881,7 +885,7 @@ def run_serve(args):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                        "p99": round(float(np.percentile(lat, 99)), 3)},
-        "plain_fp64_one_at_a_time": {
+        "plain_fp64_one_at_a_time": None if base is None else {
             "value": round(base.solves_per_s, 3), "unit": "solves/s",
             "p50_ms": round(float(np.percentile(base.latency_s, 50)) * 1e3, 3),
             "p99_ms": round(float(np.percentile(base.latency_s, 99)) * 1e3, 3),

@@ -124,7 +124,9 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * 0 reads it from global memory; bit 1 of stage = 1 runs the power method in
  * the persistent engine instead of the dedicated power kernel; bit 2 = 1
  * issues the power kernel's launches from the host stream instead of a
- * CUDA-graph WHILE loop; bit 3 = 1 uses the power kernel built for 64
+ * CUDA-graph WHILE loop (and likewise the graph loop of bit 4 when a run has
+ * a phase quantum: one launch per phase of it); bit 3 = 1 uses the power
+ * kernel built for 64
  * registers per thread (4 CTAs per SM) instead of 40 (6 CTAs per SM);
  * bit 4 = 1 runs the large instances' phases as a CUDA-graph loop of
  * ordinary launches (one phase per launch) instead of the persistent

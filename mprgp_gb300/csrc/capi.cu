@@ -55,6 +55,7 @@ struct LaneRun {
   bool active = false;
   int n = 0, n_large = 0, quantum = 0, cluster_quantum = 0, power_launches = 0;
   bool power = false, power_graph = false, egraph = false;
+  int egraph_stream = 0;  // > 0: the engine loop ran as this many stream launches
   int class_n[kClusterClasses] = {0, 0, 0, 0, 0};
   std::vector<mprgp_problem *> probs;
   std::vector<mprgp_options> opts;
@@ -795,9 +796,16 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   R.egraph = n_large > 0 && quantum >= 0 &&
              (c->engine_graph || k != 0 || other_lanes_active(c, k));
   cudaGraphExec_t eexec = nullptr;
-  if (R.egraph) {
-    rc = power_graph(L, power_grid(c, prefix[n_large], 2), 2, &eexec);
+  const int egrid = power_grid(c, prefix[n_large], 2);
+  // Stream form of that loop (with the power loop's stream form, for
+  // profilers that cannot see kernels inside conditional graphs): one launch
+  // per phase of the quantum, those after the last working one return at once.
+  R.egraph_stream = (R.egraph && !c->power_graph && quantum > 0) ? args.max_phases : 0;
+  if (R.egraph && !R.egraph_stream) {
+    rc = power_graph(L, egrid, 2, &eexec);
     if (rc) return rc;
+  }
+  if (R.egraph) {
     io.pc_in[1] = {(unsigned int)n_large, 0u, 0u, 0u, (unsigned int)args.max_phases, 0u};
     CK(cudaMemcpyAsync(L.d_pc2, &io.pc_in[1], sizeof(PowCtl), cudaMemcpyHostToDevice, s));
   }
@@ -825,7 +833,9 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   CK(cudaEventRecord(L.e_pow, s));  // the lane stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
     if (R.class_n[q]) CK(cudaStreamWaitEvent(s, L.join_ev[q], 0));
-  if (R.egraph) CK(cudaGraphLaunch(eexec, s));
+  if (R.egraph && R.egraph_stream)
+    CK(launch_power_direct(egrid, 2, R.egraph_stream, L.d_args, L.d_pc2, s));
+  else if (R.egraph) CK(cudaGraphLaunch(eexec, s));
   else if (n_large > 0 && quantum >= 0) CK(launch_engine(args, grid, s));
   CK(cudaEventRecord(L.e1, s));
   if (R.power) CK(cudaMemcpyAsync(&io.pc_out[0], L.d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
@@ -874,7 +884,9 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
   else if (R.power)
     c->launches += R.power_launches;
   for (int q = 0; q < kClusterClasses; ++q) c->launches += R.class_n[q] ? 1 : 0;
-  if (R.egraph)
+  if (R.egraph && R.egraph_stream)
+    c->launches += R.egraph_stream;
+  else if (R.egraph)
     c->launches += (long long)kPowerUnroll * ((io.pc_out[1].launches + kPowerUnroll - 1) / kPowerUnroll);
   else
     c->launches += (n_large > 0 && R.quantum >= 0) ? 1 : 0;
