@@ -130,8 +130,10 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * registers per thread (4 CTAs per SM) instead of 40 (6 CTAs per SM);
  * bit 4 = 1 runs the large instances' phases as a CUDA-graph loop of
  * ordinary launches (one phase per launch) instead of the persistent
- * cooperative engine; ctas_per_sm caps the persistent grid (0 = every
- * resident CTA). */
+ * cooperative engine; bit 5 = 1 runs the power method as one persistent
+ * cooperative launch (a grid barrier per phase, state kept on chip) in
+ * synchronous runs whose items fit four per resident CTA, the graph loop
+ * otherwise; ctas_per_sm caps the persistent grid (0 = every resident CTA). */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
 /* Small instances -- up to `cluster` items of 256 vertices -- are solved by
  * one thread-block cluster each, one CTA per item (state in shared memory,

@@ -10,8 +10,10 @@ the tuner checks that for the setting it picks.
   cluster_items  items per CTA allowed in the largest cluster (larger
                instances then also run as independent clusters)
   power        the power method's loop: a CUDA-graph WHILE loop of the power
-               kernel, plain stream launches of it, or phases of the
-               persistent engine
+               kernel, plain stream launches of it, phases of the persistent
+               engine, or one persistent cooperative launch of its own (grid
+               barrier per phase; synchronous runs whose items fit, else the
+               graph loop)
   power_regs   the power kernel's register budget: 40 (6 CTAs per SM) or
                64 (4 CTAs per SM, more loads in flight per thread)
   engine       the large instances' MPRGP phases: the persistent cooperative
@@ -41,13 +43,13 @@ DEFAULT = {"cluster": 16, "cluster_items": 1, "power": "graph", "power_regs": 40
 SPACE = {
     "cluster": [16, 8, 4, 0],
     "cluster_items": [1, 2, 4],
-    "power": ["graph", "stream", "engine"],
+    "power": ["graph", "stream", "engine", "persistent"],
     "power_regs": [40, 64],
     "engine": ["persistent", "graph"],
     "ctas_per_sm": [0, 3, 2],
     "stage": [0, 1],
 }
-_POWER_BITS = {"graph": 0, "engine": 2, "stream": 4}
+_POWER_BITS = {"graph": 0, "engine": 2, "stream": 4, "persistent": 32}
 
 
 def cache_path() -> str:
@@ -145,7 +147,7 @@ def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5
         steps = [[{"cluster": v} for v in SPACE["cluster"]],
                  [{"cluster_items": v} for v in SPACE["cluster_items"]],
                  [{"power": f, "power_regs": r} for f in SPACE["power"]
-                  for r in (SPACE["power_regs"] if f != "engine" else [40])],
+                  for r in (SPACE["power_regs"] if f in ("graph", "stream") else [40])],
                  [{"engine": v} for v in SPACE["engine"]],
                  [{"ctas_per_sm": v} for v in SPACE["ctas_per_sm"]],
                  [{"stage": v} for v in SPACE["stage"]]]

@@ -26,6 +26,9 @@ cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream)
 cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, PowCtl *d_pc,
                               cudaGraph_t *graph, cudaGraphExec_t *exec);
 cudaError_t power_max_blocks_per_sm(int variant, int *n);
+cudaError_t launch_power_persistent(const EngineArgs &args, PowCtl *d_pc, int limit, int grid,
+                                    cudaStream_t stream);
+cudaError_t power_persistent_max_blocks_per_sm(int *n);
 cudaError_t launch_cluster(const ClusterArgs &args, int csize, cudaStream_t stream);
 cudaError_t cluster_max_active(int csize, int *n);
 cudaError_t launch_power_direct(int grid, int variant, int launches, const EngineArgs *d_args,
@@ -54,7 +57,7 @@ using namespace mprgp;
 struct LaneRun {
   bool active = false;
   int n = 0, n_large = 0, quantum = 0, cluster_quantum = 0, power_launches = 0;
-  bool power = false, power_graph = false, egraph = false;
+  bool power = false, power_graph = false, power_persistent = false, egraph = false;
   int egraph_stream = 0;  // > 0: the engine loop ran as this many stream launches
   int class_n[kClusterClasses] = {0, 0, 0, 0, 0};
   std::vector<mprgp_problem *> probs;
@@ -104,6 +107,9 @@ struct mprgp_context {
   int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
   int power_variant = 0; // power kernel with 40 registers (0, 6 CTAs/SM) or 64 (1, 4 CTAs/SM)
   int bps_power_v[3] = {0, 0, 0};  // per power-kernel variant (2: all phases)
+  int power_persistent = 0;  // power loop as one persistent cooperative launch when the run
+                            // is synchronous and its items fit (1)
+  int bps_power_pp = 0;      // resident CTAs per SM of that kernel
   int engine_graph = 0;  // large instances' phases as a graph loop of the phase kernel (1)
                          // or the persistent cooperative engine (0)
   int cluster = 16;      // largest cluster of the small-instance solver (0 = off)
@@ -780,8 +786,15 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   R.power = c->power_kernel && in_power > 0 && power_launches > 0;
   cudaGraphExec_t pexec = nullptr;
   const int pgrid = power_grid(c, prefix[n_large], c->power_variant);
+  // ... or as one persistent cooperative launch: only on lane 0 with no other
+  // lane in flight (its CTAs must all be resident) and when every CTA holds
+  // at most kPowOwn items
+  const int pp_cap = c->nsm * c->bps_power_pp;
+  R.power_persistent = R.power && c->power_persistent && k == 0 && !other_lanes_active(c, k) &&
+                       pp_cap > 0 && prefix[n_large] <= pp_cap * kPowOwn;
+  const int pp_grid = std::max(1, std::min(prefix[n_large], pp_cap));
   if (R.power) {
-    if (c->power_graph) {
+    if (c->power_graph && !R.power_persistent) {
       rc = power_graph(L, pgrid, c->power_variant, &pexec);
       if (rc) return rc;
     }
@@ -827,8 +840,10 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
     CK(launch_cluster(cargs, 1 << q, L.side[q]));
     CK(cudaEventRecord(L.join_ev[q], L.side[q]));
   }
-  if (R.power && pexec) CK(cudaGraphLaunch(pexec, s));
-  if (R.power && !pexec)
+  if (R.power && R.power_persistent)
+    CK(launch_power_persistent(args, L.d_pc, power_launches, pp_grid, s));
+  else if (R.power && pexec) CK(cudaGraphLaunch(pexec, s));
+  else if (R.power)
     CK(launch_power_direct(pgrid, c->power_variant, power_launches, L.d_args, L.d_pc, s));
   CK(cudaEventRecord(L.e_pow, s));  // the lane stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
@@ -879,7 +894,9 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
   c->power_ms += pms;
   // every body of a loop graph issues kPowerUnroll launches, the stream form
   // all `power_launches` (those after the last working one return at once)
-  if (R.power && R.power_graph)
+  if (R.power && R.power_persistent)
+    c->launches += 1;
+  else if (R.power && R.power_graph)
     c->launches += (long long)kPowerUnroll * ((io.pc_out[0].launches + kPowerUnroll - 1) / kPowerUnroll);
   else if (R.power)
     c->launches += R.power_launches;
@@ -1031,6 +1048,7 @@ int mprgp_context_create(int device, mprgp_context **out) {
   CK(power_max_blocks_per_sm(0, &c->bps_power_v[0]));
   CK(power_max_blocks_per_sm(1, &c->bps_power_v[1]));
   CK(power_max_blocks_per_sm(2, &c->bps_power_v[2]));
+  CK(power_persistent_max_blocks_per_sm(&c->bps_power_pp));
   c->bps_power = c->bps_power_v[0];
   {
     int largest = 0;
@@ -1072,11 +1090,12 @@ int mprgp_context_sync(mprgp_context *c) {
 }
 
 int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
-  if (!c || stage < 0 || stage > 31 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  if (!c || stage < 0 || stage > 63 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
   c->power_kernel = (stage & 2) ? 0 : 1;
   c->power_graph = (stage & 4) ? 0 : 1;
   c->power_variant = (stage & 8) ? 1 : 0;
   c->engine_graph = (stage & 16) ? 1 : 0;
+  c->power_persistent = (stage & 32) ? 1 : 0;
   c->bps_power = c->bps_power_v[c->power_variant];
   stage &= 1;
   c->stage = stage;
@@ -1128,7 +1147,7 @@ size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {
   const size_t n = 3 * (size_t)nv;
   by += n * 8 * (kNumBuf + 3) + n * 4 * kNumBuf32;  // vectors, dinv, b, ev, FP32 shadows
   by += (size_t)nplanes * (8 * 4 * 2 + 8 * 2 + 1) + (size_t)(nv + 1) * 4 + n * 16 + n;
-  by += (size_t)nitems_of(nv) * kPart * 8 + sizeof(InstState) + 64;
+  by += (size_t)nitems_of(nv) * kPart * 8 * 2 + sizeof(InstState) + 64;
   by += (size_t)nnzb * (9 * 8 + 4) + (size_t)(nv + 1) * 4 + (size_t)nv * 4;  // BSR copy, rowmap
   return by;
 }
@@ -1146,7 +1165,7 @@ int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
   if ((rc = dalloc(p->ctx, &p->vec, n * kNumBuf)) || (rc = dalloc(p->ctx, &p->vec32, n * kNumBuf32)) ||
       (rc = dalloc(p->ctx, &p->ev, n)) ||
       (rc = dalloc(p->ctx, &p->b, n)) || (rc = dalloc(p->ctx, &p->dinv, n)) ||
-      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart)) || (rc = dalloc(p->ctx, &p->cnt, 1)) ||
+      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart * 2)) || (rc = dalloc(p->ctx, &p->cnt, 1)) ||
       (rc = dalloc(p->ctx, &p->st, 1)) || (rc = dalloc(p->ctx, &p->slice_off, p->nslices + 1))) {
     free_problem_arrays(p);
     delete p;

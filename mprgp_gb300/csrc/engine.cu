@@ -1945,6 +1945,108 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     phase_item<kAll>(args, item, pc, h, signal, sD, sS, red, sums, s_last);
 }
 
+// ------------------------------------------------ persistent power loop -----
+// Every power-method phase of a run's large instances in one cooperative
+// launch, a bounded grid barrier as the phase boundary.  Each CTA owns up to
+// kPowOwn items (grid-stride) and keeps their desc and state in shared
+// memory for the whole loop.  A phase: the owned items' rows and item
+// partials (double-buffered by phase parity in the instance's partial
+// array), the grid barrier, then every CTA reads all partials of each owned
+// item's instance, reduces them exactly as the launch form's finalize does
+// and advances its own copy of the state -- so every copy, and the result,
+// is bitwise that of the launch form.  The loop ends one phase after no
+// instance is left in a power phase (each CTA publishes the last phase at
+// which one of its instances was still busy, with atomicMax), or after
+// `limit` phases; then the CTA owning an instance's first item writes its
+// state back.
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    power_persistent_kernel(EngineArgs args, PowCtl *pc, int limit) {
+  __shared__ InstDesc sD[kPowOwn];
+  __shared__ InstState sS[kPowOwn];
+  __shared__ RedBuf red;
+  __shared__ double sums[kPart];
+  if (threadIdx.x == 0) g_staged = 0;
+  int own[kPowOwn];
+  int nown = 0;
+  for (int item = blockIdx.x; item < args.total_items && nown < kPowOwn; item += gridDim.x)
+    own[nown++] = item;
+  int inst_of[kPowOwn];
+  for (int o = 0; o < nown; ++o) {
+    inst_of[o] = instance_of(args.item_inst, args.item_prefix, args.ninst, own[o]);
+    const int *srcd = reinterpret_cast<const int *>(args.desc + inst_of[o]);
+    int *dstd = reinterpret_cast<int *>(&sD[o]);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads) dstd[w] = ldro(srcd + w);
+  }
+  __syncthreads();
+  for (int o = 0; o < nown; ++o) {
+    const int *srcs = reinterpret_cast<const int *>(args.states ? args.states + inst_of[o] : sD[o].st);
+    int *dsts = reinterpret_cast<int *>(&sS[o]);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads) dsts[w] = srcs[w];
+  }
+  __syncthreads();
+  int t = 0;
+  for (;; ++t) {
+    const int par = t & 1;
+    for (int o = 0; o < nown; ++o) {
+      const int phase = sS[o].phase;
+      if (!power_phase(phase)) continue;
+      const int local = own[o] - sD[o].item_begin;
+      const int slot = local * kThreads + threadIdx.x;
+      double part[kPart];
+#pragma unroll
+      for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+      if (slot < sD[o].nv) {
+        const int v = sD[o].A.rowmap ? ldro(sD[o].A.rowmap + slot) : slot;
+        row_power(sD[o], sS[o], v, slot, part);
+      }
+      const int ns = nslots(phase);
+      const double r = block_reduce(part, red, ns, false);
+      double *pp = sD[o].part + (size_t)par * sD[o].nitems * kPart;
+      if (threadIdx.x < ns) pp[(size_t)local * kPart + threadIdx.x] = r;
+    }
+    int unused;
+    if (!grid_barrier(args.ctl, args.wait_ns, unused)) return;
+    if (t > 0 && *(volatile unsigned int *)&pc->busy < (unsigned int)t) break;
+    bool busy = false;
+    for (int o = 0; o < nown; ++o) {
+      const int phase = sS[o].phase;
+      if (!power_phase(phase)) continue;
+      const int ns = nslots(phase);
+      const double *pp = sD[o].part + (size_t)par * sD[o].nitems * kPart;
+      double acc[kPart];
+#pragma unroll
+      for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+      for (int it = threadIdx.x; it < sD[o].nitems; it += kThreads) {
+#pragma unroll
+        for (int k = 0; k < kPart; ++k) {
+          if (k >= ns || k == kMinSlot) continue;
+          acc[k] += pp[(size_t)it * kPart + k];
+        }
+      }
+      const double tt = block_reduce(acc, red, ns, false);
+      if (threadIdx.x < kPart) sums[threadIdx.x] = tt;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        sS[o].phases++;
+        advance_power(sD[o], sS[o], sums);
+      }
+      __syncthreads();
+      busy |= power_phase(sS[o].phase);
+    }
+    if (busy && threadIdx.x == 0) atomicMax(&pc->busy, (unsigned int)(t + 1));
+    if (t + 1 >= limit) {
+      ++t;
+      break;
+    }
+  }
+  // the working phases run (the launch form's launch count)
+  if (blockIdx.x == 0 && threadIdx.x == 0) pc->launches = (unsigned int)t;
+  for (int o = 0; o < nown; ++o)
+    if (own[o] == sD[o].item_begin && threadIdx.x == 0) *sD[o].st = sS[o];
+}
+
 // ---------------------------------------------------- cluster solver -----
 // One thread-block cluster per small instance.  Every CTA of the cluster
 // holds the instance's desc and state in shared memory and advances its own
@@ -2291,6 +2393,15 @@ cudaError_t cluster_max_active(int csize, int *n) {
   cfg.attrs = at;
   cfg.numAttrs = 1;
   return cudaOccupancyMaxActiveClusters(n, cluster_kernel, &cfg);
+}
+cudaError_t launch_power_persistent(const EngineArgs &args, PowCtl *d_pc, int limit, int grid,
+                                    cudaStream_t stream) {
+  void *params[] = {(void *)&args, (void *)&d_pc, (void *)&limit};
+  return cudaLaunchCooperativeKernel((const void *)power_persistent_kernel<4>, dim3(grid),
+                                     dim3(kThreads), params, 0, stream);
+}
+cudaError_t power_persistent_max_blocks_per_sm(int *n) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_persistent_kernel<4>, kThreads, 0);
 }
 cudaError_t power_max_blocks_per_sm(int variant, int *n) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel_fn(variant), kThreads, 0);

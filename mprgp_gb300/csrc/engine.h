@@ -136,6 +136,7 @@ struct PowCtl {
   unsigned int stop;      // set when the loop is over: later launches return at once
 };
 constexpr int kPowerUnroll = 8;  // power launches per evaluation of the loop condition
+constexpr int kPowOwn = 4;       // items per CTA of the persistent power loop
 
 // Small instances run on the cluster solver: one thread-block cluster per
 // instance, CTA r covering items r, r + cluster, ... (at most kClusterItems
