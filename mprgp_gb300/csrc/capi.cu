@@ -36,12 +36,13 @@ cudaError_t launch_power_direct(int grid, int variant, int launches, const Engin
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, const int *rowmap, int *out_cols, double *out64,
-                        float *out32, double *dinv, cudaStream_t st);
+                        float *out32, double *dinv, int *bad, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st);
 void launch_state_scatter(const InstDesc *desc, int n, InstState *states, InstState *const *home,
                           const int *fresh, cudaStream_t st);
-void launch_state_gather(int n, const InstState *states, InstState *const *home, cudaStream_t st);
+void launch_state_gather(const InstDesc *desc, int n, InstState *states, InstState *const *home,
+                         cudaStream_t st);
 void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
                  cudaStream_t st);
 }  // namespace mprgp
@@ -143,6 +144,8 @@ struct mprgp_problem {
   double *vec = nullptr, *ev = nullptr, *part = nullptr;
   float *vec32 = nullptr;
   unsigned int *cnt = nullptr;
+  int *bad = nullptr;           // set on the device when A had a column outside 0..nv-1
+  int bad_host = -1;            // its value once read back (-1: not read since set_matrix)
   InstState *st = nullptr;
   double *trace = nullptr;
   int trace_cap = 0, trace_n = 0;
@@ -214,7 +217,7 @@ void free_problem_arrays(mprgp_problem *p) {
   dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
   dfree(p->ctx, p->dinv); dfree(p->ctx, p->b); dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw);
   dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
-  dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->st);
+  dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->bad); dfree(p->ctx, p->st);
   dfree(p->ctx, p->trace); dfree(p->ctx, p->stage_ptr); dfree(p->ctx, p->stage_cols); dfree(p->ctx, p->stage_vals);
   dfree(p->ctx, p->rowmap);
 }
@@ -299,10 +302,10 @@ int build_layout(mprgp_problem *p, unsigned long long key) {
   }
   c->launches++;
   launch_bsr_to_sell(nv, p->stage_ptr, p->stage_cols, p->stage_vals, p->slice_off, p->rowmap,
-                     p->cols, p->v64, p->v32, p->dinv, s);
+                     p->cols, p->v64, p->v32, p->dinv, p->bad, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
-  CK(cudaStreamSynchronize(s));  // `order` and `off` are released next
+  // `order` and `off` are pageable: cudaMemcpyAsync has staged them already
   p->layout = key;
   return MPRGP_OK;
 }
@@ -394,6 +397,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->ev = p->ev;
   d->part = p->part;
   d->cnt = p->cnt;
+  d->bad = p->bad;
   d->st = p->st;
   d->trace = p->trace;
   d->trace_cap = p->trace_cap;
@@ -856,7 +860,7 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   if (R.power) CK(cudaMemcpyAsync(&io.pc_out[0], L.d_pc, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   if (R.egraph) CK(cudaMemcpyAsync(&io.pc_out[1], L.d_pc2, sizeof(PowCtl), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&io.ctl_out, L.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
-  launch_state_gather(n, L.d_st, L.d_home, s);
+  launch_state_gather(L.d_desc, n, L.d_st, L.d_home, s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(L.h_st_out, L.d_st, sizeof(InstState) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaEventRecord(L.e_end, s));
@@ -1165,7 +1169,7 @@ int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
   if ((rc = dalloc(p->ctx, &p->vec, n * kNumBuf)) || (rc = dalloc(p->ctx, &p->vec32, n * kNumBuf32)) ||
       (rc = dalloc(p->ctx, &p->ev, n)) ||
       (rc = dalloc(p->ctx, &p->b, n)) || (rc = dalloc(p->ctx, &p->dinv, n)) ||
-      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart * 2)) || (rc = dalloc(p->ctx, &p->cnt, 1)) ||
+      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart * 2)) || (rc = dalloc(p->ctx, &p->cnt, 1)) || (rc = dalloc(p->ctx, &p->bad, 1)) ||
       (rc = dalloc(p->ctx, &p->st, 1)) || (rc = dalloc(p->ctx, &p->slice_off, p->nslices + 1))) {
     free_problem_arrays(p);
     delete p;
@@ -1200,9 +1204,9 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   if (h_ptr[0] != 0 || h_ptr[nv] != nnzb) return fail(MPRGP_INVALID, "row_ptr ends");
   for (int r = 0; r < nv; ++r)
     if (h_ptr[r + 1] < h_ptr[r]) return fail(MPRGP_INVALID, "row_ptr not monotone");
-  if (!on_device)
-    for (int q = 0; q < nnzb; ++q)
-      if (cols[q] < 0 || cols[q] >= nv) return fail(MPRGP_INVALID, "column out of range");
+  // Block columns are checked on the device as A is converted: a solve of an
+  // A that had one outside 0..nv-1 returns MPRGP_INVALID (the conversion
+  // keeps every index in range, so nothing reads out of bounds).
   // The BSR stays on the device (the SELL layout is rebuilt from it when the
   // constraint planes change which vertices have several planes).
   if (!p->stage_ptr) {
@@ -1220,6 +1224,8 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   CK(cudaMemcpyAsync(p->stage_ptr, row_ptr, sizeof(int) * (nv + 1), kind, s));
   CK(cudaMemcpyAsync(p->stage_cols, cols, sizeof(int) * nnzb, kind, s));
+  CK(cudaMemsetAsync(p->bad, 0, sizeof(int), s));
+  p->bad_host = -1;
   CK(cudaMemcpyAsync(p->stage_vals, vals, sizeof(double) * 9 * nnzb, kind, s));
   p->h_len.resize(nv);
   for (int r = 0; r < nv; ++r) p->h_len[r] = h_ptr[r + 1] - h_ptr[r];
@@ -1277,8 +1283,7 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
   p->face_len = m;
   p->cons = 1;
   p->planes_dirty = 1;
-  p->h_plane_ptr.swap(h);
-  CK(cudaStreamSynchronize(s));  // host staging vector `h` is released next
+  p->h_plane_ptr.swap(h);  // (the copy above was staged from h's buffer, now kept here)
   if (p->cols && p->stage_vals) {
     const unsigned long long key = layout_key(p);
     if (key != p->layout) return build_layout(p, key);
@@ -1421,6 +1426,13 @@ int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int
   if (!p || !x_dev || !y_dev || !p->cols) return fail(MPRGP_INVALID, "spmv");
   const bool f32 = precision == MPRGP_PREC_MIXED;
   if ((f32 && !p->has32) || (!f32 && !p->has64)) return fail(MPRGP_INVALID, "spmv precision");
+  if (p->bad_host < 0) {  // the device check of A's columns, read once per matrix
+    int b = 0;
+    CK(cudaMemcpyAsync(&b, p->bad, sizeof(int), cudaMemcpyDeviceToHost, p->ctx->stream));
+    CK(cudaStreamSynchronize(p->ctx->stream));
+    p->bad_host = b;
+  }
+  if (p->bad_host) return fail(MPRGP_INVALID, "spmv: A has a column outside 0..nv-1");
   SellMatrix A;
   A.nslices = p->nslices;
   A.slice_off = p->slice_off;

@@ -2166,7 +2166,7 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
                                    const int *__restrict__ cols, const double *__restrict__ vals,
                                    const int *__restrict__ slice_off,
                                    const int *__restrict__ rowmap, int *out_cols,
-                                   double *out64, float *out32, double *dinv) {
+                                   double *out64, float *out32, double *dinv, int *bad) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;  // SELL row (slot)
   const int s = q >> 5, lane = q & 31;
   const int nslices = (nv + kSlice - 1) / kSlice;
@@ -2183,7 +2183,11 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
     if (j < len) {
       c = cols[b + j];
       for (int e = 0; e < 9; ++e) m[e] = vals[9 * (size_t)(b + j) + e];
-      if (c == r) {
+      if (c < 0 || c >= nv) {  // invalid input: flag it, keep every index in range
+        if (bad) atomicOr(bad, 1);
+        c = r;
+        for (int e = 0; e < 9; ++e) m[e] = 0.0;
+      } else if (c == r) {
         dg[0] = m[0];
         dg[1] = m[4];
         dg[2] = m[8];
@@ -2263,10 +2267,14 @@ __global__ void state_scatter_kernel(const InstDesc *__restrict__ desc, int n, I
   for (int w = threadIdx.x; w < kStateWords; w += blockDim.x) dst[w] = src[w];
 }
 
-__global__ void state_gather_kernel(int n, const InstState *states,
+__global__ void state_gather_kernel(const InstDesc *__restrict__ desc, int n, InstState *states,
                                     InstState *const *__restrict__ home) {
   const int j = blockIdx.x;
   if (j >= n) return;
+  // An instance whose A had a block column outside 0..nv-1 (the conversion
+  // kept its indices in range) reports MPRGP_INVALID whatever it computed.
+  if (threadIdx.x == 0 && desc[j].bad && *desc[j].bad) states[j].code = kCodeInvalid;
+  __syncthreads();
   const unsigned long long *src = reinterpret_cast<const unsigned long long *>(states + j);
   unsigned long long *dst = reinterpret_cast<unsigned long long *>(home[j]);
   for (int w = threadIdx.x; w < kStateWords; w += blockDim.x) dst[w] = src[w];
@@ -2277,8 +2285,9 @@ void launch_state_scatter(const InstDesc *desc, int n, InstState *states, InstSt
                           const int *fresh, cudaStream_t st) {
   if (n > 0) state_scatter_kernel<<<n, 64, 0, st>>>(desc, n, states, home, fresh);
 }
-void launch_state_gather(int n, const InstState *states, InstState *const *home, cudaStream_t st) {
-  if (n > 0) state_gather_kernel<<<n, 64, 0, st>>>(n, states, home);
+void launch_state_gather(const InstDesc *desc, int n, InstState *states, InstState *const *home,
+                         cudaStream_t st) {
+  if (n > 0) state_gather_kernel<<<n, 64, 0, st>>>(desc, n, states, home);
 }
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream) {
   void *params[] = {(void *)&args};
@@ -2408,11 +2417,12 @@ cudaError_t power_max_blocks_per_sm(int variant, int *n) {
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, const int *rowmap, int *out_cols, double *out64,
-                        float *out32, double *dinv, cudaStream_t st) {
+                        float *out32, double *dinv, int *bad, cudaStream_t st) {
   const int nslices = (nv + kSlice - 1) / kSlice;
   const int threads = nslices * kSlice;
   bsr_to_sell_kernel<<<(threads + 255) / 256, 256, 0, st>>>(nv, row_ptr, cols, vals, slice_off,
-                                                            rowmap, out_cols, out64, out32, dinv);
+                                                            rowmap, out_cols, out64, out32, dinv,
+                                                            bad);
 }
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st) {

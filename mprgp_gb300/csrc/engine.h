@@ -111,6 +111,7 @@ struct InstDesc {
   double *ev;
   double *part;               // nitems * kPart
   unsigned int *cnt;          // items finished in the current phase
+  const int *bad;             // set when A held a block column outside 0..nv-1
   InstState *st;
   double *trace;              // optional step trace, 4 doubles per record
   int trace_cap, pad2;
@@ -137,6 +138,7 @@ struct PowCtl {
 };
 constexpr int kPowerUnroll = 8;  // power launches per evaluation of the loop condition
 constexpr int kPowOwn = 4;       // items per CTA of the persistent power loop
+constexpr int kCodeInvalid = -5;  // MPRGP_INVALID: the result code of an invalid instance
 
 // Small instances run on the cluster solver: one thread-block cluster per
 // instance, CTA r covering items r, r + cluster, ... (at most kClusterItems

@@ -41,8 +41,7 @@ cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream)
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, const int *rowmap, int *out_cols, double *out64,
-                        float *out32,
-                        double *dinv, cudaStream_t st);
+                        float *out32, double *dinv, int *bad, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, cudaStream_t st);
 void set_last_error(const char *what);
@@ -188,6 +187,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   Carve c;
   const size_t o_ctl = c.take<Ctl>(1), o_desc = c.take<InstDesc>(1), o_pref = c.take<int>(2);
   const size_t o_st = c.take<InstState>(1), o_cnt = c.take<unsigned int>(1);
+  const size_t o_bad = c.take<int>(1);
   const size_t o_soff = c.take<int>(nslices + 1), o_cols = c.take<int>(slots * kSlice);
   const size_t o_v64 = c.take<double>(slots * kSlice * 9);
   const size_t o_v32 = mixed ? c.take<float>(slots * kSlice * 9) : 0;
@@ -220,8 +220,17 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
 
   // A -> SELL-32 (+ D^-1), planes -> (n, c) rows, x -> X0; zero what counts.
   NCK(cudaMemcpyAsync(d_soff, off.data(), sizeof(int) * (nslices + 1), cudaMemcpyHostToDevice, s));
-  launch_bsr_to_sell(nv, row_ptr, cols, vals, d_soff, nullptr, d_cols, d_v64, d_v32, d_dinv, s);
+  int *d_bad = reinterpret_cast<int *>(base + o_bad);
+  NCK(cudaMemsetAsync(d_bad, 0, sizeof(int), s));
+  launch_bsr_to_sell(nv, row_ptr, cols, vals, d_soff, nullptr, d_cols, d_v64, d_v32, d_dinv, d_bad,
+                     s);
   NCK(cudaGetLastError());
+  {  // the conversion checks the block columns; no solve on an invalid A
+    int bad = 0;
+    NCK(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NCK(cudaStreamSynchronize(s));
+    if (bad) return err(MPRGP_INVALID, "solve_noalloc: A has a column outside 0..nv-1");
+  }
   if (m > 0) {
     launch_planes_setup(nv, plane_ptr, planes, d_pl, d_nn, d_indn, d_dinv, s);
     NCK(cudaGetLastError());

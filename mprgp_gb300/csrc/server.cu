@@ -255,6 +255,14 @@ void retire(mprgp_server *s, Request &r, const mprgp_stats &st) {
   s->completed.push_back(r.ticket);
 }
 
+// An engine run's return code that ends the step: a device or runtime
+// failure.  A request's own result code (breakdown, an invalid matrix) is
+// its result and leaves the others running.
+bool fatal(int rc) {
+  return rc == MPRGP_TIMEOUT || rc == MPRGP_CUDA_ERROR || rc == MPRGP_NO_DEVICE ||
+         rc == MPRGP_OOM;
+}
+
 // The synchronous form: one engine run over every admitted request.
 int step_sync(mprgp_server *s, int *ncomp) {
   const int n = (int)s->running.size();
@@ -272,7 +280,7 @@ int step_sync(mprgp_server *s, int *ncomp) {
   const int rc = mprgp::engine_run(s->ctx, n, probs.data(), opts.data(), fresh.data(),
                                    s->quantum, s->power_launches, s->cluster_quantum,
                                    st.data(), done.data());
-  if (rc < MPRGP_NOT_CONVERGED) return rc;
+  if (fatal(rc)) return rc;
   std::vector<long long> still;
   std::vector<char> still_fresh;
   for (int i = 0; i < n; ++i) {
@@ -301,7 +309,7 @@ int finish_lane(mprgp_server *s, int l, int *ncomp) {
   std::vector<int> done(n, 0);
   q.active = false;
   const int rc = mprgp::engine_end(s->ctx, 1 + l, st.data(), done.data());
-  if (rc < MPRGP_NOT_CONVERGED) return rc;
+  if (fatal(rc)) return rc;
   std::vector<long long> keep;
   for (int i = 0; i < n; ++i) {
     Request &r = s->reqs[q.in_run[i]];

@@ -482,3 +482,33 @@ def test_persistent_power_loop_equals_launch_loop(precision):
             assert sa.spec_rad == sb.spec_rad and sa.power_iters == sb.power_iters
     finally:
         c.close()
+
+
+def test_invalid_column_reports_invalid(ctx):
+    """A block column outside 0..nv-1 is caught on the device as A is
+    converted (the conversion keeps every index in range): the solve and the
+    standalone SpMV return MPRGP_INVALID, and a valid matrix loaded next into
+    the same context solves normally."""
+    torch = pytest.importorskip("torch")
+    qp = corner(4, 4, 8, seed=5)
+    cols = qp.cols.copy()
+    cols[len(cols) // 2] = qp.nv + 7
+    bad = M.BeamQP(qp.nv, qp.row_ptr, cols, qp.vals, qp.b, qp.x0, qp.plane_ptr, qp.planes, {})
+    opt = M.default_options(tol=1e-8 * np.linalg.norm(qp.b), max_it=200, kind=M.KIND_PLANES,
+                            project_x0=1, seed=SEED)
+    with pytest.raises(M.MPRGPError) as e:
+        ctx.solve_bsr(bad, opt, qp.x0)
+    assert e.value.code == M.INVALID
+    pr = M.Problem(ctx, qp.nv)
+    pr.set_matrix(bad.row_ptr, bad.cols, bad.vals, precisions=1)
+    xd = torch.zeros(qp.n, dtype=torch.float64, device="cuda")
+    yd = torch.zeros(qp.n, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    with pytest.raises(M.MPRGPError) as e:
+        pr.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_FP64)
+    assert e.value.code == M.INVALID
+    pr.set_matrix(qp.row_ptr, qp.cols, qp.vals, precisions=1)  # a valid A clears it
+    pr.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_FP64)
+    pr.close()
+    x, face, st = ctx.solve_bsr(qp, opt, qp.x0)
+    assert st.code == 0

@@ -127,3 +127,33 @@ def test_admission_by_hbm_budget(ctx, lanes):
             break
     assert finished == len(qps) and max_running <= 2
     srv.close()
+
+
+@pytest.mark.parametrize("lanes", [0, 3])
+def test_invalid_request_fails_alone(ctx, lanes):
+    """A request whose matrix has a column outside 0..nv-1 completes with
+    MPRGP_INVALID; the requests beside it are served normally."""
+    qps = [M.beam(5, 4, 6, extra_planes_max=1, extra_planes_min=1, plane_mode=2, seed=40 + i)
+           for i in range(3)]
+    cols = qps[1].cols.copy()
+    cols[3] = -2
+    q = qps[1]
+    qps[1] = M.BeamQP(q.nv, q.row_ptr, cols, q.vals, q.b, q.x0, q.plane_ptr, q.planes, {})
+    srv = M.Server(ctx, quantum_phases=128, power_launches=256, lanes=lanes)
+    tickets = [srv.submit(i, qp, opts_for(qp)) for i, qp in enumerate(qps)]
+    codes = {}
+    for _ in range(200000):
+        srv.step()
+        for i, t in enumerate(tickets):
+            if i in codes:
+                continue
+            try:
+                state, x, face, st, _ = srv.result(t)
+                if state == 2:
+                    codes[i] = st.code
+            except M.MPRGPError as e:  # a done ticket with an error code raises
+                codes[i] = e.code
+        if len(codes) == 3:
+            break
+    assert codes == {0: 0, 1: M.INVALID, 2: 0}
+    srv.close()
