@@ -67,7 +67,7 @@ def parse():
                     help="c4: skip the plain FP64 one-at-a-time play (profiling runs)")
     ap.add_argument("--no-ica", action="store_true",
                     help="c0/c1: skip the ICA comparison solve beside the line")
-    ap.add_argument("--lanes", type=int, default=SERVE_LANES, choices=[0, 2, 3],
+    ap.add_argument("--lanes", type=int, default=SERVE_LANES, choices=[0, 2, 3, 4, 5, 6],
                     help="c4: server form (0 one synchronous run per step, 2 asynchronous "
                          "small/large lanes, 3 plus a lane for the large ones' power method)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -876,9 +876,10 @@ def run_serve(args):
                               "power_loop_per_step": served["power_launches"],
                               "small_instances": "cluster solver, to completion within a run",
                               "lanes": {0: "one synchronous run per step",
-                                        2: "two asynchronous lanes (small, large)",
-                                        3: "three asynchronous lanes (small, large, large "
-                                           "in the power method)"}[args.lanes]},
+                                        2: "two asynchronous lanes (small, large)"}.get(
+                                  args.lanes, f"{args.lanes} asynchronous lanes (small, large, "
+                                              f"{args.lanes - 2} for the large requests' power "
+                                              f"method)")},
                    "inputs": "staged in device memory before the timed region (e2e: pinned host)",
                    "autotune": tuning,
                    "l2": "flushed before every window (256 MB device write)",

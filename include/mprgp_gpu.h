@@ -290,10 +290,10 @@ typedef struct mprgp_server_config {
                          (cluster solver) and large ones run on two
                          asynchronous lanes -- a step retires the runs that
                          finished, admits, starts a new run on every idle
-                         lane and returns without waiting for it; 3: as 2,
-                         plus a third lane that runs the large requests'
-                         power method (power_launches per run) before they
-                         join the large lane */
+                         lane and returns without waiting for it; 3..6: as
+                         2, plus lanes - 2 lanes that run the large requests'
+                         power method (power_launches per run; they share one
+                         queue) before they join the large lane */
 } mprgp_server_config;
 typedef struct mprgp_server mprgp_server;
 int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out);

@@ -97,7 +97,7 @@ struct Lane {
   HostIO *io = nullptr;
   LaneRun run;
 };
-constexpr int kLanes = 4;
+constexpr int kLanes = 7;  // 0: synchronous calls; 1..6: the server's asynchronous lanes
 
 struct mprgp_context {
   int device = 0;

@@ -68,6 +68,8 @@ struct Request {
   double t_submit = 0, t_admit = 0, t_done = 0;
 };
 
+constexpr int kMaxPowerLanes = 4;  // asynchronous power-method lanes at most
+
 struct Scene {
   mprgp_problem *prob = nullptr;
   size_t bytes = 0;
@@ -103,11 +105,11 @@ struct mprgp_server {
   // asynchronous form: per lane (small; large; large in the power method,
   // three-lane form only) the admitted requests waiting for its next run and
   // those in its run in flight.  Server lane l runs on engine lane l + 1.
-  int lanes = 0;
+  int lanes = 0, npow = 0;  // npow: power lanes (lanes - 2 when lanes >= 3)
   struct LaneQ {
     std::vector<long long> pending, in_run;
     bool active = false;
-  } lane[3];
+  } lane[2 + kMaxPowerLanes];  // the power lanes share lane[2].pending
 };
 
 namespace {
@@ -229,7 +231,7 @@ void admit_queued(mprgp_server *s) {
     r.fresh = true;
     if (s->lanes) {
       r.lane = mprgp::engine_lane_of(s->ctx, r.nv) == 1 ? 0 : 1;
-      if (r.lane == 1 && s->lanes == 3 &&
+      if (r.lane == 1 && s->npow > 0 &&
           mprgp::engine_needs_power(s->scenes[r.scene].prob, &r.opt))
         r.lane = 2;
       s->lane[r.lane].pending.push_back(r.ticket);
@@ -299,8 +301,9 @@ int step_sync(mprgp_server *s, int *ncomp) {
 }
 
 // Takes the results of lane l's run if it has finished.  Unfinished
-// requests lead the lane's next run, except that those of the power lane
-// that have left the power method move on to the large lane.
+// requests lead the lane's next run (a power lane's, the shared power
+// queue), except that those of a power lane that have left the power method
+// move on to the large lane.
 int finish_lane(mprgp_server *s, int l, int *ncomp) {
   auto &q = s->lane[l];
   if (!q.active || mprgp::engine_ready(s->ctx, 1 + l) == 0) return MPRGP_OK;
@@ -315,7 +318,7 @@ int finish_lane(mprgp_server *s, int l, int *ncomp) {
     Request &r = s->reqs[q.in_run[i]];
     if (!done[i]) {
       r.fresh = false;
-      if (l == 2 && !mprgp::engine_in_power(s->scenes[r.scene].prob)) {
+      if (l >= 2 && !mprgp::engine_in_power(s->scenes[r.scene].prob)) {
         r.lane = 1;
         s->lane[1].pending.push_back(r.ticket);
       } else {
@@ -327,16 +330,19 @@ int finish_lane(mprgp_server *s, int l, int *ncomp) {
     ++*ncomp;
   }
   q.in_run.clear();
-  q.pending.insert(q.pending.begin(), keep.begin(), keep.end());
+  auto &pend = l >= 2 ? s->lane[2].pending : q.pending;
+  pend.insert(pend.begin(), keep.begin(), keep.end());
   return MPRGP_OK;
 }
 
-// Starts a run on lane l over its pending requests if the lane is idle.
+// Starts a run on lane l over its pending requests (a power lane: the shared
+// power queue) if the lane is idle.
 int start_lane(mprgp_server *s, int l) {
   auto &q = s->lane[l];
-  if (q.active || q.pending.empty()) return MPRGP_OK;
-  q.in_run.swap(q.pending);
-  q.pending.clear();
+  auto &pend = l >= 2 ? s->lane[2].pending : q.pending;
+  if (q.active || pend.empty()) return MPRGP_OK;
+  q.in_run.swap(pend);
+  pend.clear();
   const int n = (int)q.in_run.size();
   std::vector<mprgp_problem *> probs(n);
   std::vector<mprgp_options> opts(n);
@@ -347,10 +353,10 @@ int start_lane(mprgp_server *s, int l) {
     opts[i] = r.opt;
     fresh[i] = r.fresh ? 1 : 0;
   }
-  // the power lane runs the power loop alone; with it, the large lane runs
-  // no power loop of its own
-  const int quantum = l == 2 ? -1 : s->quantum;
-  const int power = (l == 1 && s->lanes == 3) ? 0 : s->power_launches;
+  // a power lane runs the power loop alone; with power lanes, the large lane
+  // runs no power loop of its own
+  const int quantum = l >= 2 ? -1 : s->quantum;
+  const int power = (l == 1 && s->npow > 0) ? 0 : s->power_launches;
   const int rc = mprgp::engine_begin(s->ctx, 1 + l, n, probs.data(), opts.data(), fresh.data(),
                                      quantum, power, s->cluster_quantum);
   if (rc) return rc;
@@ -362,8 +368,8 @@ int start_lane(mprgp_server *s, int l) {
 // idle lane; when none of that happened, wait a little for a lane to finish
 // (the caller may have requests to submit meanwhile).
 int step_async(mprgp_server *s, int *ncomp) {
-  const int nl = s->lanes == 3 ? 3 : 2;
-  for (int l = nl - 1; l >= 0; --l) {  // the power lane first: it feeds the large lane
+  const int nl = 2 + s->npow;
+  for (int l = nl - 1; l >= 0; --l) {  // the power lanes first: they feed the large lane
     const int rc = finish_lane(s, l, ncomp);
     if (rc) return rc;
   }
@@ -406,18 +412,19 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
   if (cfg && cfg->quantum_phases < 0) s->quantum = 0;  // each step runs to completion
   if (cfg && cfg->cluster_quantum > 0) s->cluster_quantum = cfg->cluster_quantum;
   if (cfg && cfg->power_launches >= 0) s->power_launches = std::min(cfg->power_launches, 1003);
-  if (cfg && cfg->lanes != 0 && cfg->lanes != 2 && cfg->lanes != 3) {
+  if (cfg && (cfg->lanes == 1 || cfg->lanes < 0 || cfg->lanes > 2 + kMaxPowerLanes)) {
     delete s;
-    return err(MPRGP_INVALID, "server_create: lanes must be 0, 2 or 3");
+    return err(MPRGP_INVALID, "server_create: lanes must be 0 or 2..6");
   }
   s->lanes = cfg ? cfg->lanes : 0;
+  s->npow = s->lanes >= 3 ? s->lanes - 2 : 0;
   *out = s;
   return MPRGP_OK;
 }
 
 int mprgp_server_destroy(mprgp_server *s) {
   if (!s) return MPRGP_OK;
-  for (int l = 0; l < 3; ++l)  // runs in flight end before their problems go
+  for (int l = 0; l < 2 + kMaxPowerLanes; ++l)  // runs in flight end before their problems go
     if (s->lane[l].active) mprgp::engine_end(s->ctx, 1 + l, nullptr, nullptr);
   for (auto &kv : s->scenes) mprgp_problem_destroy(kv.second.prob);
   delete s;
