@@ -31,6 +31,12 @@ constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:
 #ifndef MPRGP_SPMV_MIN_BLOCKS  // resident CTAs per SM the standalone SpMV is compiled for
 #define MPRGP_SPMV_MIN_BLOCKS 4
 #endif
+#ifndef MPRGP_CLUSTER_MIN_BLOCKS  // resident CTAs per SM the cluster solver is compiled for
+#define MPRGP_CLUSTER_MIN_BLOCKS 6   // (its phases are latency-bound: more clusters in flight)
+#endif
+#ifndef MPRGP_ALLPHASE_MIN_BLOCKS  // ... and the all-phase kernel of the graph-loop engine
+#define MPRGP_ALLPHASE_MIN_BLOCKS 4
+#endif
 #ifndef MPRGP_ENGINE_MIN_BLOCKS
 #define MPRGP_ENGINE_MIN_BLOCKS 4
 #endif
@@ -2091,7 +2097,7 @@ __device__ __forceinline__ double ld_dsmem(unsigned int addr) {
   return v;
 }
 
-__global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) cluster_kernel(ClusterArgs args) {
+__global__ void __launch_bounds__(kThreads, MPRGP_CLUSTER_MIN_BLOCKS) cluster_kernel(ClusterArgs args) {
   __shared__ InstDesc sD;
   __shared__ InstState sS;
   __shared__ RedBuf red;
@@ -2308,7 +2314,7 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
 // variant 0: power phases, 40 registers; 1: power phases, 64 registers;
 // 2: every phase (the graph form of the engine).
 const void *power_kernel_fn(int variant) {
-  return variant == 2 ? (const void *)phase_kernel<4, true>
+  return variant == 2 ? (const void *)phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true>
          : variant   ? (const void *)phase_kernel<4, false>
                      : (const void *)phase_kernel<6, false>;
 }
@@ -2360,7 +2366,7 @@ cudaError_t launch_power_direct(int grid, int variant, int launches, const Engin
                                 PowCtl *d_pc, cudaStream_t stream) {
   for (int k = 0; k < launches; ++k) {
     const cudaGraphConditionalHandle h0 = 0;
-    if (variant == 2) phase_kernel<4, true><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
+    if (variant == 2) phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
     else if (variant) phase_kernel<4, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
     else phase_kernel<6, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
     cudaError_t e = cudaGetLastError();
