@@ -474,10 +474,30 @@ __device__ __forceinline__ int decide_face(const InstDesc &D, const VCons &C, co
   return cnt;
 }
 
-// Small SPD solve on the planes selected by `mask` (<= 3), Cramer's rule.
+// Whether the Gram matrix restricted to the planes in `mask` is exactly the
+// identity (mutually orthogonal unit normals, e.g. axis-aligned floor and
+// walls): the small QPs below then separate by plane.
+__device__ __forceinline__ bool unit_gram(const double G[3][3], int mask) {
+  bool id = true;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (((mask >> i) & 1) && ((mask >> j) & 1)) id &= (i == j) ? G[i][j] == 1.0 : G[i][j] == 0.0;
+  return id;
+}
+
+// Small SPD solve on the planes selected by `mask` (<= 3), Cramer's rule
+// (with G the identity on `mask`, Cramer's rule gives lam = q there).
 __device__ __forceinline__ bool solve_subset(const double G[3][3], const double q[3], int mask,
                                              double lam[3]) {
   lam[0] = lam[1] = lam[2] = 0.0;
+  if (unit_gram(G, mask)) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      if ((mask >> i) & 1) lam[i] = q[i];
+    return true;
+  }
   int idx[3], s = 0;
 #pragma unroll
   for (int i = 0; i < 3; ++i)
@@ -522,6 +542,14 @@ __device__ __forceinline__ void nonneg_qp3(const double G[3][3], const double q[
   for (int i = 0; i < 3; ++i)
     if (allow & (1 << i)) scale = fmax(scale, fabs(q[i]));
   const double tol = 1e-12 * scale;
+  if (unit_gram(G, allow)) {
+    // Separable: the enumeration below would stop at the support
+    // {i : q_i > tol} (smaller supports leave a q_i > tol unmet, larger ones
+    // come later), whose solution is lam_i = q_i there and 0 elsewhere.
+#pragma unroll
+    for (int i = 0; i < 3; ++i) lam[i] = (((allow >> i) & 1) && q[i] > tol) ? q[i] : 0.0;
+    return;
+  }
   double best_viol = DBL_MAX, best[3] = {0.0, 0.0, 0.0};
   // Supports are subsets of `allow`; visit them by popcount, then value.
   for (int size = 0; size <= 3; ++size) {
