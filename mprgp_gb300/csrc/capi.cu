@@ -38,7 +38,7 @@ void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const doubl
                         const int *slice_off, const int *rowmap, int *out_cols, double *out64,
                         float *out32, double *dinv, int *bad, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
-                         double *indn, const double *dinv, cudaStream_t st);
+                         double *indn, const double *dinv, unsigned char *unit, cudaStream_t st);
 void launch_state_scatter(const InstDesc *desc, int n, InstState *states, InstState *const *home,
                           const int *fresh, cudaStream_t st);
 void launch_state_gather(const InstDesc *desc, int n, InstState *states, InstState *const *home,
@@ -138,6 +138,7 @@ struct mprgp_problem {
   double *dinv = nullptr, *b = nullptr;
   int *plane_ptr = nullptr;
   double *planes_raw = nullptr, *planes = nullptr, *pl_nn = nullptr, *pl_indn = nullptr;
+  unsigned char *pl_unit = nullptr;  // per vertex: its planes are orthonormal
   double *L = nullptr, *U = nullptr;
   unsigned char *face = nullptr;
   int face_len = 0;
@@ -216,7 +217,7 @@ int nitems_of(int nv) { return (nv + kThreads - 1) / kThreads; }
 void free_problem_arrays(mprgp_problem *p) {
   dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
   dfree(p->ctx, p->dinv); dfree(p->ctx, p->b); dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw);
-  dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
+  dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->pl_unit); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
   dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->bad); dfree(p->ctx, p->st);
   dfree(p->ctx, p->trace); dfree(p->ctx, p->stage_ptr); dfree(p->ctx, p->stage_cols); dfree(p->ctx, p->stage_vals);
   dfree(p->ctx, p->rowmap);
@@ -360,7 +361,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   if (p->cons == 1 && p->planes_dirty) {
     p->ctx->launches++;
     launch_planes_setup(p->nv, p->plane_ptr, p->planes_raw, p->planes, p->pl_nn, p->pl_indn,
-                        p->dinv, st);
+                        p->dinv, p->pl_unit, st);
     CK(cudaGetLastError());
     p->planes_dirty = 0;
   }
@@ -388,6 +389,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->planes = p->planes;
   d->pl_nn = p->pl_nn;
   d->pl_indn = p->pl_indn;
+  d->pl_unit = p->pl_unit;
   d->L = p->L;
   d->U = p->U;
   d->face = p->face;
@@ -1271,6 +1273,7 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
     if (!rc) rc = dalloc(p->ctx, &p->planes, 4 * (size_t)std::max(m, 1));
     if (!rc) rc = dalloc(p->ctx, &p->pl_nn, (size_t)std::max(m, 1));
     if (!rc) rc = dalloc(p->ctx, &p->pl_indn, (size_t)std::max(m, 1));
+    if (!rc && !p->pl_unit) rc = dalloc(p->ctx, &p->pl_unit, (size_t)nv);
     if (!rc) rc = dalloc(p->ctx, &p->face, (size_t)std::max(m, 1));
     if (rc) return rc;
   }

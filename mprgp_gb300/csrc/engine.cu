@@ -397,16 +397,18 @@ __device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int slot,
 
 // --------------------------------------------------- vertex constraints --
 struct VCons {
-  int k, base;
+  int k, base, unit;  // unit: the planes' Gram matrix is the identity (k >= 2)
   double n[kMaxPlanes][3], c[kMaxPlanes], inn[kMaxPlanes], indn[kMaxPlanes];
   double lo[3], hi[3];
 };
 
 __device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
+  C.unit = 0;
   if (D.kind >= KIND_DECOUPLED) {
     const int b = ldro(D.plane_ptr + v), e = ldro(D.plane_ptr + v + 1);
     C.base = b;
     C.k = e - b;
+    if (D.pl_unit && C.k >= 2) C.unit = D.pl_unit[v];
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
       if (j < C.k) {
@@ -531,6 +533,18 @@ __device__ __forceinline__ bool solve_subset(const double G[3][3], const double 
   return true;
 }
 
+// nonneg_qp3 for G = I on `allow` (planes flagged orthonormal beforehand):
+// the same scale, tolerance and multipliers without forming G.
+__device__ __forceinline__ void unit_qp3(const double q[3], int allow, double lam[3]) {
+  double scale = 1e-300;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (allow & (1 << i)) scale = fmax(scale, fabs(q[i]));
+  const double tol = 1e-12 * scale;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) lam[i] = (((allow >> i) & 1) && q[i] > tol) ? q[i] : 0.0;
+}
+
 // min 0.5 l^T G l - q^T l, l >= 0 over the planes in `allow` (bit mask), by
 // enumerating supports in order of size, then mask value; the first support
 // that satisfies KKT wins.  Same procedure as the oracle's per-block solver
@@ -616,10 +630,13 @@ __device__ void project_v(const InstDesc &D, const VCons &C, const double x[3], 
       return;
     }
     double G[3][3], q[3], lam[3];
-    gram(C, G);
 #pragma unroll
     for (int j = 0; j < 3; ++j) q[j] = (j < C.k) ? C.c[j] - dot3(C.n[j], x) : 0.0;
-    nonneg_qp3(G, q, (1 << C.k) - 1, lam);
+    if (C.unit) unit_qp3(q, (1 << C.k) - 1, lam);  // what nonneg_qp3 returns for G = I
+    else {
+      gram(C, G);
+      nonneg_qp3(G, q, (1 << C.k) - 1, lam);
+    }
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       if (j < C.k)
@@ -658,10 +675,15 @@ __device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3
       return;
     }
     double G[3][3], q[3], lam[3];
-    gram(C, G);
 #pragma unroll
     for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? -dot3(C.n[j], g) : 0.0;
-    if (!solve_subset(G, q, act, lam)) return;
+    if (C.unit) {  // what solve_subset returns for G = I
+#pragma unroll
+      for (int j = 0; j < 3; ++j) lam[j] = (act & (1 << j)) ? q[j] : 0.0;
+    } else {
+      gram(C, G);
+      if (!solve_subset(G, q, act, lam)) return;
+    }
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       if (act & (1 << j))
@@ -705,10 +727,13 @@ __device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[
       return;
     }
     double G[3][3], q[3], lam[3];
-    gram(C, G);
 #pragma unroll
     for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? dot3(C.n[j], beta) : 0.0;
-    nonneg_qp3(G, q, act, lam);
+    if (C.unit) unit_qp3(q, act, lam);
+    else {
+      gram(C, G);
+      nonneg_qp3(G, q, act, lam);
+    }
     double gp[3] = {beta[0], beta[1], beta[2]};
 #pragma unroll
     for (int j = 0; j < 3; ++j)
@@ -2244,9 +2269,21 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
 // 1/diag(J J^T) and 1/diag(J D^-1 J^T) (MPRGPPrecondition.h:81-89).
 __global__ void planes_setup_kernel(int nv, const int *__restrict__ plane_ptr,
                                     const double *__restrict__ in, double *out, double *nn,
-                                    double *indn, const double *__restrict__ dinv) {
+                                    double *indn, const double *__restrict__ dinv,
+                                    unsigned char *unit) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
+  if (unit) {  // 2-3 planes with an identity Gram matrix (same products as gram())
+    const int b = plane_ptr[v], k = plane_ptr[v + 1] - b;
+    bool id = k >= 2 && k <= kMaxPlanes;
+    for (int i = 0; id && i < k; ++i)
+      for (int j = 0; j < k; ++j) {
+        const double *ni = in + 4 * (size_t)(b + i), *nj = in + 4 * (size_t)(b + j);
+        const double gij = dot3(ni, nj);
+        id &= (i == j) ? gij == 1.0 : gij == 0.0;
+      }
+    unit[v] = id ? 1 : 0;
+  }
   for (int q = plane_ptr[v]; q < plane_ptr[v + 1]; ++q) {
     const double n0 = in[4 * (size_t)q], n1 = in[4 * (size_t)q + 1], n2 = in[4 * (size_t)q + 2];
     out[4 * (size_t)q] = n0;
@@ -2459,8 +2496,9 @@ void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const doubl
                                                             bad);
 }
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
-                         double *indn, const double *dinv, cudaStream_t st) {
-  planes_setup_kernel<<<(nv + 255) / 256, 256, 0, st>>>(nv, plane_ptr, in, out, nn, indn, dinv);
+                         double *indn, const double *dinv, unsigned char *unit, cudaStream_t st) {
+  planes_setup_kernel<<<(nv + 255) / 256, 256, 0, st>>>(nv, plane_ptr, in, out, nn, indn, dinv,
+                                                        unit);
 }
 void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
                  cudaStream_t st) {

@@ -104,6 +104,7 @@ struct InstDesc {
   const double *planes;       // 4 per row: nx, ny, nz, c   (J x >= c)
   const double *pl_nn;        // 1 / |n|^2 = 1 / diag(J J^T)
   const double *pl_indn;      // 1 / (n . D^-1 n) = 1 / diag(J D^-1 J^T)
+  const unsigned char *pl_unit;  // per vertex: 2-3 planes whose Gram matrix is the identity
   const double *L, *U;        // bounds kinds
   unsigned char *face;        // one per constraint row / per unknown
   double *buf[kNumBuf];

@@ -43,7 +43,7 @@ void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const doubl
                         const int *slice_off, const int *rowmap, int *out_cols, double *out64,
                         float *out32, double *dinv, int *bad, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
-                         double *indn, const double *dinv, cudaStream_t st);
+                         double *indn, const double *dinv, unsigned char *unit, cudaStream_t st);
 void set_last_error(const char *what);
 }  // namespace mprgp
 
@@ -232,7 +232,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
     if (bad) return err(MPRGP_INVALID, "solve_noalloc: A has a column outside 0..nv-1");
   }
   if (m > 0) {
-    launch_planes_setup(nv, plane_ptr, planes, d_pl, d_nn, d_indn, d_dinv, s);
+    launch_planes_setup(nv, plane_ptr, planes, d_pl, d_nn, d_indn, d_dinv, nullptr, s);
     NCK(cudaGetLastError());
   }
   NCK(cudaMemsetAsync(d_face, 0, std::max(m, 1), s));
@@ -263,6 +263,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   D.planes = d_pl;
   D.pl_nn = d_nn;
   D.pl_indn = d_indn;
+  D.pl_unit = nullptr;  // the general per-vertex QPs throughout
   D.face = d_face;
   for (int i = 0; i < kNumBuf; ++i) D.buf[i] = d_vec + (size_t)i * n;
   for (int i = 0; i < kNumBuf32; ++i)
