@@ -34,6 +34,9 @@ constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:
 #ifndef MPRGP_CLUSTER_MIN_BLOCKS  // resident CTAs per SM the cluster solver is compiled for
 #define MPRGP_CLUSTER_MIN_BLOCKS 6   // (its phases are latency-bound: more clusters in flight)
 #endif
+#ifndef MPRGP_POWER_MIN_BLOCKS  // ... the smaller-register power kernel (tuning variant 0)
+#define MPRGP_POWER_MIN_BLOCKS 6
+#endif
 #ifndef MPRGP_ALLPHASE_MIN_BLOCKS  // ... and the all-phase kernel of the graph-loop engine
 #define MPRGP_ALLPHASE_MIN_BLOCKS 4
 #endif
@@ -2381,7 +2384,7 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
 const void *power_kernel_fn(int variant) {
   return variant == 2 ? (const void *)phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true>
          : variant   ? (const void *)phase_kernel<4, false>
-                     : (const void *)phase_kernel<6, false>;
+                     : (const void *)phase_kernel<MPRGP_POWER_MIN_BLOCKS, false>;
 }
 cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, PowCtl *d_pc,
                               cudaGraph_t *graph, cudaGraphExec_t *exec) {
@@ -2433,7 +2436,7 @@ cudaError_t launch_power_direct(int grid, int variant, int launches, const Engin
     const cudaGraphConditionalHandle h0 = 0;
     if (variant == 2) phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
     else if (variant) phase_kernel<4, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
-    else phase_kernel<6, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
+    else phase_kernel<MPRGP_POWER_MIN_BLOCKS, false><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

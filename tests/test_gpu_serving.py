@@ -5,8 +5,9 @@
 * follow-up timesteps warm-start from the resident scene and converge to the
   same solution as a cold solve of the same QP;
 * admission respects the HBM budget (scenes are evicted, never overcommitted);
-* all of the above hold for both server forms: one synchronous run per step,
-  and two asynchronous lanes (small and large requests on separate streams).
+* all of the above hold for every server form: one synchronous run per step,
+  two asynchronous lanes (small and large requests on separate streams), and
+  three or more (power-method lanes sharing one queue).
 Tolerance: the stopping test 1e-8 ||b||; x compared to 1e-12 relative
 (in practice bitwise: each instance reduces in a fixed order).
 """
@@ -31,7 +32,7 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("lanes", [0, 2, 3])
+@pytest.mark.parametrize("lanes", [0, 2, 3, 5])
 @pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
 def test_same_alone_and_in_the_mix(ctx, precision, lanes):
     # sizes on both sides of the cluster solver's limit (16 items of 256
