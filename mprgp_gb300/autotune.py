@@ -11,9 +11,11 @@ the tuner checks that for the setting it picks.
                instances then also run as independent clusters)
   power        the power method's loop: a CUDA-graph WHILE loop of the power
                kernel, plain stream launches of it, phases of the persistent
-               engine, or one persistent cooperative launch of its own (grid
+               engine, one persistent cooperative launch of its own (grid
                barrier per phase; synchronous runs whose items fit, else the
-               graph loop)
+               graph loop), or the power-step loop (each launch advances the
+               states the previous one left while its rows form their
+               products; graph or stream launches)
   power_regs   the power kernel's register budget: 40 (6 CTAs per SM) or
                64 (4 CTAs per SM, more loads in flight per thread)
   engine       the large instances' MPRGP phases: the persistent cooperative
@@ -43,13 +45,14 @@ DEFAULT = {"cluster": 16, "cluster_items": 1, "power": "graph", "power_regs": 40
 SPACE = {
     "cluster": [16, 8, 4, 0],
     "cluster_items": [1, 2, 4],
-    "power": ["graph", "stream", "engine", "persistent"],
+    "power": ["graph", "stream", "engine", "persistent", "step", "step-stream"],
     "power_regs": [40, 64],
     "engine": ["persistent", "graph"],
     "ctas_per_sm": [0, 3, 2],
     "stage": [0, 1],
 }
-_POWER_BITS = {"graph": 0, "engine": 2, "stream": 4, "persistent": 32}
+_POWER_BITS = {"graph": 0, "engine": 2, "stream": 4, "persistent": 32, "step": 64,
+               "step-stream": 64 | 4}
 
 
 def cache_path() -> str:

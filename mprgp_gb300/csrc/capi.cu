@@ -59,6 +59,7 @@ struct LaneRun {
   bool active = false;
   int n = 0, n_large = 0, quantum = 0, cluster_quantum = 0, power_launches = 0;
   bool power = false, power_graph = false, power_persistent = false, egraph = false;
+  int power_variant = 0;  // the power loop's kernel variant (3: the power-step loop)
   int egraph_stream = 0;  // > 0: the engine loop ran as this many stream launches
   int class_n[kClusterClasses] = {0, 0, 0, 0, 0};
   std::vector<mprgp_problem *> probs;
@@ -107,7 +108,9 @@ struct mprgp_context {
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
   int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
   int power_variant = 0; // power kernel with 40 registers (0, 6 CTAs/SM) or 64 (1, 4 CTAs/SM)
-  int bps_power_v[3] = {0, 0, 0};  // per power-kernel variant (2: all phases)
+  int bps_power_v[4] = {0, 0, 0, 0};  // per power-kernel variant (2: all phases, 3: power steps)
+  int power_step = 0;    // power loop as the power-step loop (1; deferred finalize) or the
+                         // phase kernel with a finalize per launch (0)
   int power_persistent = 0;  // power loop as one persistent cooperative launch when the run
                             // is synchronous and its items fit (1)
   int bps_power_pp = 0;      // resident CTAs per SM of that kernel
@@ -588,7 +591,8 @@ int lane_reserve(mprgp_context *c, Lane &L, int n, int items) {
   L.cap = 0;
   int rc = dalloc(c, &L.d_desc, cap);
   if (!rc) rc = dalloc(c, &L.d_prefix, cap + 1);
-  if (!rc) rc = dalloc(c, &L.d_st, cap);
+  // the run's states, then the power-step loop's two copies
+  if (!rc) rc = dalloc(c, &L.d_st, 3 * (size_t)cap);
   if (!rc) rc = dalloc(c, &L.d_fresh, cap);
   if (!rc) rc = dalloc(c, &L.d_home, cap);
   if (rc) return rc;
@@ -782,6 +786,8 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   const bool stage = c->stage && c->bps_stage > 0;
   args.stage_bytes = stage ? kStageBytes : 0;
   args.ctl = L.ctl;
+  args.pst[0] = L.d_st + L.cap;
+  args.pst[1] = L.d_st + 2 * (size_t)L.cap;
   int per_sm = stage ? c->bps_stage : c->bps;
   if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
   const int grid = std::max(1, std::min(prefix[n_large], c->nsm * per_sm));
@@ -791,7 +797,8 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   // the power kernel while any instance is in a power phase; then the engine.
   R.power = c->power_kernel && in_power > 0 && power_launches > 0;
   cudaGraphExec_t pexec = nullptr;
-  const int pgrid = power_grid(c, prefix[n_large], c->power_variant);
+  R.power_variant = c->power_step ? 3 : c->power_variant;
+  const int pgrid = power_grid(c, prefix[n_large], R.power_variant);
   // ... or as one persistent cooperative launch: only on lane 0 with no other
   // lane in flight (its CTAs must all be resident) and when every CTA holds
   // at most kPowOwn items
@@ -801,7 +808,7 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   const int pp_grid = std::max(1, std::min(prefix[n_large], pp_cap));
   if (R.power) {
     if (c->power_graph && !R.power_persistent) {
-      rc = power_graph(L, pgrid, c->power_variant, &pexec);
+      rc = power_graph(L, pgrid, R.power_variant, &pexec);
       if (rc) return rc;
     }
     io.pc_in[0] = {in_power, 0u, 0u, 0u, (unsigned int)power_launches, 0u};
@@ -850,7 +857,7 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
     CK(launch_power_persistent(args, L.d_pc, power_launches, pp_grid, s));
   else if (R.power && pexec) CK(cudaGraphLaunch(pexec, s));
   else if (R.power)
-    CK(launch_power_direct(pgrid, c->power_variant, power_launches, L.d_args, L.d_pc, s));
+    CK(launch_power_direct(pgrid, R.power_variant, power_launches, L.d_args, L.d_pc, s));
   CK(cudaEventRecord(L.e_pow, s));  // the lane stream's power loop ends here
   for (int q = 0; q < kClusterClasses; ++q)
     if (R.class_n[q]) CK(cudaStreamWaitEvent(s, L.join_ev[q], 0));
@@ -900,10 +907,14 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
   c->power_ms += pms;
   // every body of a loop graph issues kPowerUnroll launches, the stream form
   // all `power_launches` (those after the last working one return at once)
+  // (the power-step loop adds its settle kernel to every body)
+  const long long body = kPowerUnroll + (R.power_variant == 3 ? 1 : 0);
   if (R.power && R.power_persistent)
     c->launches += 1;
   else if (R.power && R.power_graph)
-    c->launches += (long long)kPowerUnroll * ((io.pc_out[0].launches + kPowerUnroll - 1) / kPowerUnroll);
+    c->launches += body * ((io.pc_out[0].launches + kPowerUnroll - 1) / kPowerUnroll);
+  else if (R.power && R.power_variant == 3)
+    c->launches += body * ((R.power_launches + kPowerUnroll - 1) / kPowerUnroll);
   else if (R.power)
     c->launches += R.power_launches;
   for (int q = 0; q < kClusterClasses; ++q) c->launches += R.class_n[q] ? 1 : 0;
@@ -1054,6 +1065,7 @@ int mprgp_context_create(int device, mprgp_context **out) {
   CK(power_max_blocks_per_sm(0, &c->bps_power_v[0]));
   CK(power_max_blocks_per_sm(1, &c->bps_power_v[1]));
   CK(power_max_blocks_per_sm(2, &c->bps_power_v[2]));
+  CK(power_max_blocks_per_sm(3, &c->bps_power_v[3]));
   CK(power_persistent_max_blocks_per_sm(&c->bps_power_pp));
   c->bps_power = c->bps_power_v[0];
   {
@@ -1096,12 +1108,13 @@ int mprgp_context_sync(mprgp_context *c) {
 }
 
 int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
-  if (!c || stage < 0 || stage > 63 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
+  if (!c || stage < 0 || stage > 127 || ctas_per_sm < 0) return fail(MPRGP_INVALID, "set_tuning");
   c->power_kernel = (stage & 2) ? 0 : 1;
   c->power_graph = (stage & 4) ? 0 : 1;
   c->power_variant = (stage & 8) ? 1 : 0;
   c->engine_graph = (stage & 16) ? 1 : 0;
   c->power_persistent = (stage & 32) ? 1 : 0;
+  c->power_step = (stage & 64) ? 1 : 0;
   c->bps_power = c->bps_power_v[c->power_variant];
   stage &= 1;
   c->stage = stage;

@@ -43,6 +43,9 @@ constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:
 #ifndef MPRGP_ENGINE_MIN_BLOCKS
 #define MPRGP_ENGINE_MIN_BLOCKS 4
 #endif
+#ifndef MPRGP_STEP_MIN_BLOCKS  // ... and the power-step kernel (288 threads: 56 registers)
+#define MPRGP_STEP_MIN_BLOCKS 4
+#endif
 
 // ------------------------------------------------------------ primitives --
 __device__ __forceinline__ long long gtimer() {
@@ -893,8 +896,28 @@ __device__ __forceinline__ void st3ff(float *b, int v, const float o[3]) {
   q[2] = o[2];
 }
 
-__device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, int v, int slot,
-                                         double *part) {
+// The matrix product of a power iteration's row before its scaling: A times
+// the stored source vector `src` (a buffer id, or < 0 for the stored start
+// vector ev) -- FP32 for the mixed form, FP64 otherwise.  It depends on the
+// source alone, so a row can form it before the phase's scale 1/||w|| is
+// known.
+__device__ __forceinline__ void pow_raw32(const InstDesc &D, int src, int slot, float w[3]) {
+  if (src < 0) {
+    spmv_row<float, SrcVtoF, float>(D.A, D.A.v32, slot, SrcVtoF{D.ev}, w);
+  } else {
+    const SrcF s{D.buf32[src == B_W ? F_W0 : F_W1]};
+    if (g_staged) spmv_row_staged<float, SrcF, float>(D.A, slot, s, w);
+    else spmv_row<float, SrcF, float>(D.A, D.A.v32, slot, s, w);
+  }
+}
+__device__ __forceinline__ void pow_raw64(const InstDesc &D, int src, int slot, double w[3]) {
+  spmv_any(D, false, slot, SrcV{src < 0 ? D.ev : B(D, src)}, SrcF{nullptr}, w);
+}
+
+// The rest of an FP32 power row given its raw product wr (unused in
+// PH_POW_LAST).
+__device__ __forceinline__ void row_power32_fin(const InstDesc &D, const InstState &S, int v,
+                                                const float wr[3], double *part) {
   const int k = S.pow_k;
   const float sc = (float)S.pow_scale;  // 1/||w|| (tmpOut /= norm)
   float u[3];
@@ -918,14 +941,7 @@ __device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, 
   }
   if (S.phase == PH_POW_LAST) return;
   st3ff(D.buf32[F_Z0 + (k & 1)], v, u);
-  float w[3];
-  if (S.pow_src < 0) {
-    spmv_row<float, SrcVtoF, float>(D.A, D.A.v32, slot, SrcVtoF{D.ev}, w);
-  } else {
-    const SrcF src{D.buf32[S.pow_src == B_W ? F_W0 : F_W1]};
-    if (g_staged) spmv_row_staged<float, SrcF, float>(D.A, slot, src, w);
-    else spmv_row<float, SrcF, float>(D.A, D.A.v32, slot, src, w);
-  }
+  float w[3] = {wr[0], wr[1], wr[2]};
   w[0] *= sc;
   w[1] *= sc;
   w[2] *= sc;
@@ -933,22 +949,28 @@ __device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, 
   part[1] += (double)fmaf(w[0], w[0], fmaf(w[1], w[1], w[2] * w[2]));
 }
 
-__device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, int v, int slot,
-                                       double *part) {
-  const bool f32 = D.prec == PREC_MIXED;
-  if (f32 && S.phase != PH_POW_RAND) {
-    row_power32(D, S, v, slot, part);
-    return;
-  }
-  if (S.phase == PH_POW_RAND) {
-    double t[3];
+__device__ __noinline__ void row_power32(const InstDesc &D, const InstState &S, int v, int slot,
+                                         double *part) {
+  float w[3] = {0.f, 0.f, 0.f};
+  if (S.phase != PH_POW_LAST) pow_raw32(D, S.pow_src, slot, w);
+  row_power32_fin(D, S, v, w, part);
+}
+
+// PH_POW_RAND's row: the seeded start vector (tmp.setRandom()).
+__device__ __forceinline__ void row_power_rand(const InstDesc &D, int v, double *part) {
+  double t[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) t[d] = seeded_uniform(D.seed, 3ull * v + d);
-    st3(B(D, B_W1), v, t);
-    if (f32) st3f(D.buf32[F_W1], v, t);
-    part[0] += dot3(t, t);
-    return;
-  }
+  for (int d = 0; d < 3; ++d) t[d] = seeded_uniform(D.seed, 3ull * v + d);
+  st3(B(D, B_W1), v, t);
+  if (D.prec == PREC_MIXED) st3f(D.buf32[F_W1], v, t);
+  part[0] += dot3(t, t);
+}
+
+// The rest of an FP64 power row given its raw product wr (unused in
+// PH_POW_LAST).
+__device__ __forceinline__ void row_power64_fin(const InstDesc &D, const InstState &S, int v,
+                                                const double wr[3], double *part) {
+  const bool f32 = D.prec == PREC_MIXED;
   const int k = S.pow_k;
   const double *src = S.pow_src < 0 ? D.ev : B(D, S.pow_src);
   double u[3];
@@ -964,18 +986,31 @@ __device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, in
   }
   if (S.phase == PH_POW_LAST) return;
   st3(B(D, B_T0 + (k & 1)), v, u);
-  double w[3];
-  // A (src / ||w||) = (A src) / ||w||; the FP32 pass reads src's FP32 shadow
-  // (the stored start vector ev has none and takes the FP64 pass).
-  const bool f32src = f32 && S.pow_src >= 0;
-  spmv_any(D, f32src, slot, SrcV{src},
-           SrcF{f32src ? D.buf32[S.pow_src == B_W ? F_W0 : F_W1] : nullptr}, w);
+  double w[3] = {wr[0], wr[1], wr[2]};
   w[0] *= S.pow_scale;
   w[1] *= S.pow_scale;
   w[2] *= S.pow_scale;
   st3(B(D, (k & 1) ? B_W1 : B_W), v, w);
   if (f32) st3f(D.buf32[(k & 1) ? F_W1 : F_W0], v, w);
   part[1] += dot3(w, w);
+}
+
+__device__ __noinline__ void row_power(const InstDesc &D, const InstState &S, int v, int slot,
+                                       double *part) {
+  const bool f32 = D.prec == PREC_MIXED;
+  if (f32 && S.phase != PH_POW_RAND) {
+    row_power32(D, S, v, slot, part);
+    return;
+  }
+  if (S.phase == PH_POW_RAND) {
+    row_power_rand(D, v, part);
+    return;
+  }
+  double w[3] = {0.0, 0.0, 0.0};
+  // A (src / ||w||) = (A src) / ||w||; the stored start vector ev and every
+  // source of the FP64 form take the FP64 pass
+  if (S.phase != PH_POW_LAST) pow_raw64(D, S.pow_src, slot, w);
+  row_power64_fin(D, S, v, w, part);
 }
 
 __device__ __noinline__ void row_init(const InstDesc &D, const InstState &S, int v, int slot,
@@ -2109,6 +2144,248 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     if (own[o] == sD[o].item_begin && threadIdx.x == 0) *sD[o].st = sS[o];
 }
 
+// ------------------------------------------------- power-step loop -----
+// The power method as a graph loop whose body is kPowerUnroll launches of
+// power_step_kernel and one of power_settle_kernel.  No launch finalizes its
+// own phase: launch j of a body reads the states launch j-1 left (launch 0:
+// the run's state array) and, for an instance whose rows ran there, the item
+// partials they wrote.  Every CTA reduces those partials in the launch
+// form's finalize order with one extra warp and advances its own copy of the
+// state from the sums, while its row warps already form their rows' products
+// with the source vector the advanced state will name (the previous phase's
+// output, which the state before the advance determines).  So a phase's
+// serial reduction and FP64 update overlap the next phase's matrix pass and
+// no launch waits on a last CTA.  The launches of even / odd position keep
+// their states and (two per item) partials in separate copies.  The settle
+// kernel applies the body's last partials, writes every state back to the
+// run's array and sets the loop condition.  Each copy of a state advances
+// from the same sums, summed in the same order, as the launch form's
+// finalize, so results are bitwise those of the launch form.
+constexpr int kStepThreads = kThreads + 32;  // the row warps + the reduction warp
+constexpr int kNoSrc = -1000;                 // no power product for the rows
+
+// Slots 0 and 1 of an instance's item partials (two per item) reduced by
+// one warp in the finalize's order: thread t of phase_item's finalize sums
+// items t, t + kThreads, ...; block_reduce's warp then adds the sums of
+// threads l, l + 32, ..., l + 224 and closes with warp_sum.  Lane l keeps
+// the sums of threads l + 32 i.  The partials come through shared memory,
+// kSumStage items at a time, by asynchronous 16-byte copies that are all in
+// flight together (plain loads would each wait for the previous add).
+constexpr int kSumStage = 6 * kThreads;  // items per staged round (24 KB)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void warp_item_sums(const double *pp, int nitems, int lane,
+                                               double2 *stage, double s[2]) {
+  double t0[kThreads / 32], t1[kThreads / 32];
+#pragma unroll
+  for (int i = 0; i < kThreads / 32; ++i) t0[i] = t1[i] = 0.0;
+  for (int base = 0; base < nitems; base += kSumStage) {
+    const int n = min(kSumStage, nitems - base);
+    __syncwarp();  // the previous round's readers are done
+    for (int j = lane; j < n; j += 32) cp_async16(stage + j, pp + 2 * (size_t)(base + j));
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < kThreads / 32; ++i)
+      for (int j = lane + 32 * i; j < n; j += kThreads) {  // base is a multiple of kThreads
+        const double2 q = stage[j];
+        t0[i] += q.x;
+        t1[i] += q.y;
+      }
+  }
+  double a0 = t0[0], a1 = t1[0];
+#pragma unroll
+  for (int i = 1; i < kThreads / 32; ++i) {
+    a0 = a0 + t0[i];
+    a1 = a1 + t1[i];
+  }
+  s[0] = warp_sum(a0);
+  s[1] = warp_sum(a1);
+}
+
+// block_reduce of slots 0 and 1 over the row threads of a kStepThreads
+// block (the same order); every thread takes part in the barriers.
+__device__ double block_reduce_rows(const double part[2], RedBuf &red, int ns) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < kThreads) {
+    red.v[0][threadIdx.x] = part[0];
+    if (ns > 1) red.v[1][threadIdx.x] = part[1];
+  }
+  __syncthreads();
+  if (warp < ns) {
+    const double *src = red.v[warp];
+    double acc = src[lane];
+#pragma unroll
+    for (int i = 1; i < kThreads / 32; ++i) acc = acc + src[lane + 32 * i];
+    acc = warp_sum(acc);
+    if (lane == 0) red.out[warp] = acc;
+  }
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < ns) r = red.out[threadIdx.x];
+  __syncthreads();
+  return r;
+}
+
+// Advances a copy of a power-phase state by the phase's sums (the launch
+// form's finalize).
+__device__ __forceinline__ void advance_power_sums(const InstDesc &D, InstState &S,
+                                                   const double s2[2]) {
+  double sums[kPart];
+#pragma unroll
+  for (int k = 0; k < kPart; ++k) sums[k] = k < 2 ? s2[k] : 0.0;
+  S.phases++;
+  advance_power(D, S, sums);
+}
+
+// The reduction warp's work for one instance: `out` = `in` advanced by the
+// partials pp (lane 0 writes it).  Not inlined, so that its FP64 state
+// update does not take registers from the row warps' matrix pass.
+__device__ __noinline__ void step_advance(const InstDesc &D, const InstState &in, InstState &out,
+                                          const double *pp, int lane, double2 *stage) {
+  double s2[2];
+  warp_item_sums(pp, D.nitems, lane, stage, s2);
+  if (lane == 0) {
+    InstState S = in;
+    advance_power_sums(D, S, s2);
+    out = S;
+  }
+}
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks)
+    power_step_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc, int node) {
+  __shared__ InstDesc sD;
+  __shared__ InstState sIn, sCur;
+  __shared__ RedBuf red;
+  __shared__ __align__(16) double2 sItems[kSumStage];
+  __shared__ int s_inst;
+  if (*(volatile unsigned int *)&pc->stop) return;  // the loop is over
+  if (threadIdx.x == 0) {
+    g_staged = 0;
+    s_inst = -1;
+  }
+  const EngineArgs args = *pargs;
+  const int par = node & 1;
+  const InstState *st_in = node == 0 ? args.states : args.pst[par ^ 1];
+  InstState *st_out = args.pst[par];
+  const int lane = threadIdx.x & 31;
+  for (int item = blockIdx.x; item < args.total_items; item += gridDim.x) {
+    const int inst = instance_of(args.item_inst, args.item_prefix, args.ninst, item);
+    __syncthreads();  // the previous item is done with the shared copies
+    // a CTA's consecutive items of one instance share its advanced state
+    const bool fresh = inst != s_inst;
+    if (fresh) {
+      const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
+      int *dstd = reinterpret_cast<int *>(&sD);
+      for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kStepThreads) dstd[w] = ldro(srcd + w);
+      const int *srcs = reinterpret_cast<const int *>(st_in + inst);
+      int *dsts = reinterpret_cast<int *>(&sIn);
+      for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kStepThreads) dsts[w] = srcs[w];
+      __syncthreads();
+    }
+    const int phase_in = fresh ? sIn.phase : sCur.phase;
+    const bool pend = fresh && node > 0 && power_phase(phase_in);
+    // the source vector of the product the rows will need
+    int src = kNoSrc;
+    if (pend) {
+      if (phase_in == PH_POW_RAND) src = B_W1;
+      else if (phase_in == PH_POW) src = (sIn.pow_k & 1) ? B_W1 : B_W;
+    } else if (phase_in == PH_POW) {
+      src = fresh ? sIn.pow_src : sCur.pow_src;
+    }
+    const int local = item - sD.item_begin;
+    const int slot = local * kThreads + threadIdx.x;
+    const bool row = threadIdx.x < kThreads && slot < sD.nv;
+    const bool f32 = sD.prec == PREC_MIXED;
+    float wf[3] = {0.f, 0.f, 0.f};
+    double wd[3] = {0.0, 0.0, 0.0};
+    if (row && src != kNoSrc) {
+      if (f32) pow_raw32(sD, src, slot, wf);
+      else pow_raw64(sD, src, slot, wd);
+    }
+    if (fresh && threadIdx.x >= kThreads) {  // the reduction warp
+      if (pend) {
+        step_advance(sD, sIn, sCur, sD.part + (size_t)(par ^ 1) * sD.nitems * 2, lane, sItems);
+      } else {
+        const int *a = reinterpret_cast<const int *>(&sIn);
+        int *b = reinterpret_cast<int *>(&sCur);
+        for (int w = lane; w < (int)(sizeof(InstState) / 4); w += 32) b[w] = a[w];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_inst = inst;
+    const int phase = sCur.phase;
+    if (power_phase(phase)) {
+      double part[2] = {0.0, 0.0};
+      if (row) {
+        const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
+        if (phase == PH_POW_RAND) {
+          row_power_rand(sD, v, part);
+        } else {
+          if (phase == PH_POW && sCur.pow_src != src) {  // not the predicted source
+            if (f32) pow_raw32(sD, sCur.pow_src, slot, wf);
+            else pow_raw64(sD, sCur.pow_src, slot, wd);
+          }
+          if (f32) row_power32_fin(sD, sCur, v, wf, part);
+          else row_power64_fin(sD, sCur, v, wd, part);
+        }
+      }
+      const double r = block_reduce_rows(part, red, nslots(phase));
+      if (threadIdx.x < 2) sD.part[(size_t)par * sD.nitems * 2 + 2 * (size_t)local + threadIdx.x] = r;
+    }
+    if (threadIdx.x == 0 && item == sD.item_begin) st_out[inst] = sCur;
+  }
+}
+
+// The end of a loop body: each instance's state from the body's last launch,
+// advanced by that launch's partials when its rows ran, back to the run's
+// state array; the last CTA to finish sets the loop condition (more bodies
+// while an instance is in a power phase and fewer than PowCtl::limit launches
+// have run).  One warp per CTA, instances grid-strided.
+__global__ void __launch_bounds__(32)
+    power_settle_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc,
+                        cudaGraphConditionalHandle h, int signal) {
+  __shared__ __align__(16) double2 sItems[kSumStage];
+  if (*(volatile unsigned int *)&pc->stop) return;
+  const EngineArgs args = *pargs;
+  constexpr int last = (kPowerUnroll - 1) & 1;
+  const InstState *st_in = args.pst[last];
+  InstState *st_out = const_cast<InstState *>(args.states);
+  const int lane = threadIdx.x;
+  unsigned int busy = 0u;
+  for (int inst = blockIdx.x; inst < args.ninst; inst += gridDim.x) {
+    const InstDesc &D = args.desc[inst];
+    InstState S = st_in[inst];
+    if (power_phase(S.phase)) {
+      double s2[2];
+      warp_item_sums(D.part + (size_t)last * D.nitems * 2, D.nitems, lane, sItems, s2);
+      advance_power_sums(D, S, s2);
+    }
+    if (lane == 0) {
+      st_out[inst] = S;
+      busy += power_phase(S.phase) ? 1u : 0u;
+    }
+  }
+  if (lane == 0) {
+    if (busy) atomicAdd(&pc->busy, busy);
+    const unsigned int old = atom_add_acq_rel(&pc->fin, 1u);
+    if (old == gridDim.x - 1u) {
+      const unsigned int b = atomicAdd(&pc->busy, 0u);
+      const unsigned int launches = pc->launches + (unsigned int)kPowerUnroll;
+      const bool more = b > 0u && launches < pc->limit;
+      pc->launches = launches;
+      pc->busy = 0u;
+      pc->fin = 0u;
+      pc->stop = more ? 0u : 1u;
+      __threadfence();
+      if (signal) cudaGraphSetConditional(h, more ? 1u : 0u);
+    }
+  }
+}
+
 // ---------------------------------------------------- cluster solver -----
 // One thread-block cluster per small instance.  Every CTA of the cluster
 // holds the instance's desc and state in shared memory and advances its own
@@ -2381,11 +2658,15 @@ cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes) {
 // instantiation serves every later run with the same grid.
 // variant 0: power phases, 40 registers; 1: power phases, 64 registers;
 // 2: every phase (the graph form of the engine).
+// 3: the power-step loop (power_step_kernel, kStepThreads threads).
 const void *power_kernel_fn(int variant) {
-  return variant == 2 ? (const void *)phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true>
+  return variant == 3 ? (const void *)power_step_kernel<MPRGP_STEP_MIN_BLOCKS>
+         : variant == 2 ? (const void *)phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true>
          : variant   ? (const void *)phase_kernel<4, false>
                      : (const void *)phase_kernel<MPRGP_POWER_MIN_BLOCKS, false>;
 }
+int power_block_threads(int variant) { return variant == 3 ? kStepThreads : kThreads; }
+constexpr int kSettleGrid = 32;  // CTAs of power_settle_kernel (instances grid-strided)
 cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, PowCtl *d_pc,
                               cudaGraph_t *graph, cudaGraphExec_t *exec) {
   *graph = nullptr;
@@ -2402,7 +2683,37 @@ cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, P
   cp.conditional.size = 1;
   cudaGraphNode_t cond;
   if (e == cudaSuccess) e = cudaGraphAddNode(&cond, g, nullptr, nullptr, 0, &cp);
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && variant == 3) {
+    // kPowerUnroll step launches (their position in the body as argument),
+    // then the settle kernel, which sets the condition
+    cudaGraphNode_t prev = nullptr;
+    for (int u = 0; u < kPowerUnroll && e == cudaSuccess; ++u) {
+      int node = u;
+      void *kargs[] = {(void *)&d_args, (void *)&d_pc, (void *)&node};
+      cudaKernelNodeParams kp;
+      memset(&kp, 0, sizeof(kp));
+      kp.func = (void *)power_kernel_fn(3);
+      kp.gridDim = dim3(grid);
+      kp.blockDim = dim3(kStepThreads);
+      kp.kernelParams = kargs;
+      cudaGraphNode_t kn;
+      e = cudaGraphAddKernelNode(&kn, cp.conditional.phGraph_out[0], prev ? &prev : nullptr,
+                                 prev ? 1 : 0, &kp);
+      prev = kn;
+    }
+    if (e == cudaSuccess) {
+      int signal = 1;
+      void *kargs[] = {(void *)&d_args, (void *)&d_pc, (void *)&h, (void *)&signal};
+      cudaKernelNodeParams kp;
+      memset(&kp, 0, sizeof(kp));
+      kp.func = (void *)power_settle_kernel;
+      kp.gridDim = dim3(kSettleGrid);
+      kp.blockDim = dim3(32);
+      kp.kernelParams = kargs;
+      cudaGraphNode_t kn;
+      e = cudaGraphAddKernelNode(&kn, cp.conditional.phGraph_out[0], &prev, 1, &kp);
+    }
+  } else if (e == cudaSuccess) {
     int signal = 1;
     void *kargs[] = {(void *)&d_args, (void *)&d_pc, (void *)&h, (void *)&signal};
     cudaKernelNodeParams kp;
@@ -2432,6 +2743,17 @@ cudaError_t build_power_graph(int grid, int variant, const EngineArgs *d_args, P
 // last working one return at once).
 cudaError_t launch_power_direct(int grid, int variant, int launches, const EngineArgs *d_args,
                                 PowCtl *d_pc, cudaStream_t stream) {
+  if (variant == 3) {  // whole bodies: kPowerUnroll steps and the settle kernel
+    const cudaGraphConditionalHandle h0 = 0;
+    for (int k = 0; k < launches; k += kPowerUnroll) {
+      for (int u = 0; u < kPowerUnroll; ++u)
+        power_step_kernel<MPRGP_STEP_MIN_BLOCKS><<<grid, kStepThreads, 0, stream>>>(d_args, d_pc, u);
+      power_settle_kernel<<<kSettleGrid, 32, 0, stream>>>(d_args, d_pc, h0, 0);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
   for (int k = 0; k < launches; ++k) {
     const cudaGraphConditionalHandle h0 = 0;
     if (variant == 2) phase_kernel<MPRGP_ALLPHASE_MIN_BLOCKS, true><<<grid, kThreads, 0, stream>>>(d_args, d_pc, h0, 0);
@@ -2487,7 +2809,8 @@ cudaError_t power_persistent_max_blocks_per_sm(int *n) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_persistent_kernel<4>, kThreads, 0);
 }
 cudaError_t power_max_blocks_per_sm(int variant, int *n) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel_fn(variant), kThreads, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel_fn(variant),
+                                                       power_block_threads(variant), 0);
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
                         const int *slice_off, const int *rowmap, int *out_cols, double *out64,

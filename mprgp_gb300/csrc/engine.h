@@ -168,6 +168,9 @@ struct EngineArgs {
   int stage_bytes;         // dynamic shared memory for staging (0 = off)
   int pad;
   Ctl *ctl;
+  // the power-step loop's two state copies (desc order), written by the
+  // launches of even / odd position in a loop body
+  InstState *pst[2];
 };
 
 }  // namespace mprgp

@@ -484,6 +484,49 @@ def test_persistent_power_loop_equals_launch_loop(precision):
         c.close()
 
 
+@pytest.mark.parametrize("precision", [M.PREC_MIXED, M.PREC_FP64])
+def test_power_step_loop_equals_launch_loop(precision):
+    """The power-step loop (each launch advances the states the previous one
+    left, the reduction warp overlapping the rows' products; a settle kernel
+    per body) gives bitwise the launch loop's results, as a graph loop and as
+    stream launches: one instance alone and a batch with several items per
+    CTA."""
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(16, 16, 40, 2, 91), (24, 20, 30, 1, 92), (20, 12, 60, 2, 93)]]
+    c = M.Context(0)
+    try:
+        c.set_cluster(0)  # every instance on the engine path
+        res = {}
+        for bits in (0, 64, 64 | 4):
+            c.set_tuning(bits, 0)
+            single = _solve_all(c, qps[:1], precision)
+            probs, opts = [], []
+            for qp in qps * 6:  # 18 instances, about 1,900 items
+                probs.append(M.load_beam(c, qp, precisions=3))
+                probs[-1].set_power_cache(False)
+                opts.append(M.default_options(tol=1e-10 * np.linalg.norm(qp.b), max_it=20000,
+                                              kind=M.KIND_PLANES, project_x0=1, seed=SEED,
+                                              precision=precision))
+            stats = c.solve_batch(probs, opts)
+            batch = [(pr.get_x(), st) for pr, st in zip(probs, stats)]
+            for pr in probs:
+                pr.close()
+            res[bits] = (single, batch)
+        for other in (64, 64 | 4):
+            for (xa, fa, sa), (xb, fb, sb) in zip(res[0][0], res[other][0]):
+                assert sa.code == 0 and sb.code == 0
+                assert np.array_equal(xa, xb) and np.array_equal(fa, fb)
+                assert (sa.iterations, sa.phases, sa.power_iters) == (sb.iterations, sb.phases,
+                                                                       sb.power_iters)
+                assert sa.spec_rad == sb.spec_rad
+            for (xa, sa), (xb, sb) in zip(res[0][1], res[other][1]):
+                assert sa.code == 0 and sb.code == 0 and np.array_equal(xa, xb)
+                assert sa.spec_rad == sb.spec_rad and sa.power_iters == sb.power_iters
+                assert sa.phases == sb.phases
+    finally:
+        c.close()
+
+
 def test_invalid_column_reports_invalid(ctx):
     """A block column outside 0..nv-1 is caught on the device as A is
     converted (the conversion keeps every index in range): the solve and the

@@ -70,6 +70,45 @@ def test_same_alone_and_in_the_mix(ctx, precision, lanes):
     srv.close()
 
 
+@pytest.mark.parametrize("lanes", [0, 3])
+def test_power_step_loop_served(ctx, lanes):
+    """Served with the power-step loop and power runs cut into short pieces
+    (20 launches a step: the loop stops at a body boundary and the next run
+    resumes from the settled state), every result equals the launch loop's
+    result for the request solved alone."""
+    dims = [(14, 8, 30), (16, 8, 32), (12, 10, 24), (5, 5, 5)]
+    qps = [M.beam(*d, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=40 + i)
+           for i, (d, e) in enumerate(zip(dims, [2, 1, 2, 0]))]
+    precision = M.PREC_MIXED
+    alone = [ctx.solve_bsr(q, opts_for(q, precision), q.x0) for q in qps]
+    ctx.set_tuning(64, 0)
+    try:
+        srv = M.Server(ctx, quantum_phases=64, power_launches=20, max_slots=4, lanes=lanes)
+        tickets, done = {}, {}
+        for i, q in enumerate(qps):
+            tickets[srv.submit(i, q, opts_for(q, precision))] = i
+        steps = 0
+        while len(done) < len(qps):
+            srv.step()
+            steps += 1
+            for t, i in list(tickets.items()):
+                state, x, face, st, times = srv.result(t)
+                if state == 2:
+                    assert st.code == 0
+                    done[i] = (x, face, st)
+                    del tickets[t]
+            assert steps < 200000
+        srv.close()
+    finally:
+        ctx.set_tuning(0, 0)
+    for i, (xa, fa, sa) in enumerate(alone):
+        xs, fs, ss = done[i]
+        assert np.array_equal(xs, xa), i
+        assert np.array_equal(fs, fa)
+        assert (ss.iterations, ss.power_iters) == (sa.iterations, sa.power_iters)
+        assert ss.spec_rad == sa.spec_rad
+
+
 @pytest.mark.parametrize("lanes", [0, 2, 3])
 def test_followup_warm_start(ctx, lanes):
     qp = M.beam(6, 5, 10, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=3)
