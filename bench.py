@@ -20,7 +20,9 @@ Other workloads: c1 (one 32x32x128 beam, 421,443 DOF; --form plain|mixed),
 c0 (4x4x16, floor), c2 (256 uneven beams in one batched run), c3 (48x48x144,
 E=1e6, nu=0.49, 20 warm-started timesteps, mixed vs FP64 per step).
 --impl reference times the CPU restatement of the reference MPRGP (oracle/)
-on the host cores instead.
+on the host cores instead.  --spmv times the standalone y = A x
+(mprgp_problem_spmv) on the c0/c1/c3 matrix, FP64 and FP32, with its HBM
+and FP64-unit roofline fractions.
 """
 from __future__ import annotations
 
@@ -72,6 +74,9 @@ def parse():
                          "small/large lanes, 3 plus a lane for the large ones' power method)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the launch-shape autotuner (mprgp_gb300.autotune) before warm-up")
+    ap.add_argument("--spmv", action="store_true",
+                    help="time the standalone y = A x (mprgp_problem_spmv) on the config's "
+                         "matrix instead of the solver, FP64 and FP32 values")
     ap.add_argument("--tuning", type=int, default=None,
                     help="launch-form bits for mprgp_context_set_tuning (bit 2: power loop from "
                          "host-stream launches instead of the CUDA-graph WHILE loop)")
@@ -982,8 +987,77 @@ def run_reference_serve(args):
     print(json.dumps(line))
 
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (non-tensor) nominal rate
+
+
+def run_spmv(args):
+    """The standalone y = A x of the config's beam (FixedSparseMatrix::multiply
+    through mprgp_problem_spmv), one launch per step, L2 flushed before each;
+    x and y FP64 at the API, A in FP64 and in FP32.  Reports HBM throughput on
+    the algorithmic bytes and, for the FP64 matrix, the FP64 rate on the
+    algorithmic flops (18 per 3x3 block): the FP64 product is bound by GB300's
+    FP64 unit before HBM."""
+    import torch
+    import mprgp_gb300 as M
+    M.build()
+    name = args.config if args.config in ("c0", "c1", "c3") else "c1"
+    qp = workload_qp(name)
+    ctx = M.Context(0)
+    pr = M.load_beam(ctx, qp, precisions=3)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    x = torch.from_numpy(np.random.default_rng(0).standard_normal(qp.n)).cuda()
+    y = torch.empty_like(x)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    peak, peak_src = measured_peaks()
+    out = {}
+    with ClockSampler(0) as clk:
+        for prec, s_a, key in ((M.PREC_FP64, 8, "fp64"), (M.PREC_MIXED, 4, "fp32")):
+            for _ in range(args.warmup):
+                pr.spmv(x.data_ptr(), y.data_ptr(), prec)
+            ctx.sync()
+            ts = []
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                pr.spmv(x.data_ptr(), y.data_ptr(), prec)
+                e1.record(stream)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = float(np.median(ts))
+            # x and y are FP64 at the API whatever the matrix precision
+            byt = qp.nnzb * (9 * s_a + 4) + (qp.nv + 1) * 4 + 2 * qp.n * 8
+            out[key] = {"ms": round(ms, 5), "GB/s": round(byt / ms / 1e6, 1),
+                        "hbm_frac": round(byt / ms / 1e6 / peak, 4), "bytes": int(byt)}
+            if s_a == 8:
+                tf = 18.0 * qp.nnzb / ms / 1e9
+                out[key]["fp64_tflops"] = round(tf, 4)
+                out[key]["fp64_frac_of_nominal"] = round(tf / FP64_NOMINAL_TFLOPS, 4)
+    pr.close()
+    line = {"metric": "standalone y = A x throughput (FixedSparseMatrix::multiply, FP64 x and y)",
+            "value": out["fp64"]["GB/s"], "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["fp64"]["ms"], "higher_is_better": True,
+            "scaling": "none", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_desc(name, qp)["workload"], "config": name,
+                       "l2": "flushed before each launch (256 MB device write)"},
+            "spmv": out,
+            "roofline": {"bound": "fp64", "achieved": out["fp64"]["fp64_tflops"],
+                         "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                         "frac": out["fp64"]["fp64_frac_of_nominal"],
+                         "peak_source": "nominal (GB300 FP64 1.25 TFLOP/s)",
+                         "hbm_frac": out["fp64"]["hbm_frac"], "hbm_peak_gbs": peak,
+                         "hbm_peak_source": peak_src},
+            "gpu_launches": 2 * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.spmv:
+        run_spmv(args)
+        return
     if args.form is None:
         args.form = "mixed" if args.config in ("c2", "c3", "c4") else "plain"
     if args.impl == "reference":
