@@ -173,9 +173,21 @@ struct mprgp_problem {
     unsigned long long seed = 0, gen = 0;
     double spec_rad = 0.0;
   } pcache;
+  // Result of the last power method that started from the stored vector ev
+  // and left ev unchanged (it ran to its iteration limit): a deterministic
+  // function of (A, ev, precision form), reused while the three stay the
+  // same -- a resident scene's follow-up timesteps warm-start from ev.
+  struct {
+    int valid = 0, prec = 0, power_iters = 0;
+    unsigned long long gen = 0, ev_gen = 0;
+    double spec_rad = 0.0;
+  } pcache_ev;
   int pcache_on = 1;
   unsigned long long matrix_gen = 0;  // bumped by every set_matrix
+  unsigned long long ev_gen = 0;      // bumped whenever ev may have been rewritten
   int run_random = 0, run_cached = 0;  // how the current solve's power method starts
+  int run_ev = 0;                      // ... from ev (ev_gen at its start: run_ev_gen)
+  unsigned long long run_ev_gen = 0;
 };
 
 namespace {
@@ -630,10 +642,14 @@ int engine_lane_of(const mprgp_context *c, int nv) {
 // Whether a solve of `p` started now with options `o` begins with the power
 // method (it does unless the exact power-method cache applies).
 int engine_needs_power(const mprgp_problem *p, const mprgp_options *o) {
-  if (o->use_ev && p->ev_valid) return 1;  // warm-started power method
   int kind, alg, pre;
   if (resolve_options(p, o, &kind, &alg, &pre)) return 1;
   const int prec = (alg == ALG_MONOTONE) ? o->precision : PREC_FP64;
+  if (o->use_ev && p->ev_valid) {  // warm-started power method
+    const bool cached = p->pcache_on && p->pcache_ev.valid && p->pcache_ev.prec == prec &&
+                        p->pcache_ev.gen == p->matrix_gen && p->pcache_ev.ev_gen == p->ev_gen;
+    return cached ? 0 : 1;
+  }
   const bool cached = p->pcache_on && p->pcache.valid && p->pcache.seed == o->seed &&
                       p->pcache.prec == prec && p->pcache.gen == p->matrix_gen;
   return cached ? 0 : 1;
@@ -729,14 +745,23 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
     const InstDesc &D = desc[R.pos[i]];
     p->phase_host = S.phase;
     p->run_random = S.phase == PH_POW_RAND;
+    p->run_ev = S.phase == PH_POW && S.pow_src < 0;
+    p->run_ev_gen = p->ev_gen;
     p->run_cached = 0;
-    if (p->run_random && p->pcache_on && p->pcache.valid && p->pcache.seed == opts[i].seed &&
-        p->pcache.prec == D.prec && p->pcache.gen == p->matrix_gen) {
+    const bool hit_random = p->run_random && p->pcache_on && p->pcache.valid &&
+                            p->pcache.seed == opts[i].seed && p->pcache.prec == D.prec &&
+                            p->pcache.gen == p->matrix_gen;
+    const bool hit_ev = p->run_ev && p->pcache_on && p->pcache_ev.valid &&
+                        p->pcache_ev.prec == D.prec && p->pcache_ev.gen == p->matrix_gen &&
+                        p->pcache_ev.ev_gen == p->ev_gen;
+    if (hit_random || hit_ev) {
       // the state advance_power leaves when the power method ends
-      S.spec_rad = p->pcache.spec_rad;
-      S.power_iters = p->pcache.power_iters;
+      S.spec_rad = hit_ev ? p->pcache_ev.spec_rad : p->pcache.spec_rad;
+      S.power_iters = hit_ev ? p->pcache_ev.power_iters : p->pcache.power_iters;
       S.alpha_bar = 2.0 / S.spec_rad;
-      S.ev_upd = 0;  // the vector it would store is the one already stored
+      // random start: the vector it would store is the one already stored;
+      // start from ev: the cached run stored none
+      S.ev_upd = 0;
       S.phase = D.project_x0 ? PH_PROJ0 : PH_INIT;
       p->run_cached = 1;
       p->phase_host = S.phase;
@@ -942,7 +967,18 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
     else if (!finished && unbounded) x.code = MPRGP_TIMEOUT;
     p->xc = x.xc;
     p->trace_n = x.trace_n;
+    if (x.ev_upd) p->ev_gen++;  // PH_INIT has stored, or will store, a new ev
     if (finished && x.ev_upd && x.code > MPRGP_BREAKDOWN) p->ev_valid = 1;
+    if (finished && !err && p->run_ev && !p->run_cached && !x.ev_upd &&
+        p->ev_gen == p->run_ev_gen) {
+      auto &pc = p->pcache_ev;
+      pc.valid = 1;
+      pc.prec = L.h_desc[R.pos[i]].prec;
+      pc.gen = p->matrix_gen;
+      pc.ev_gen = p->ev_gen;
+      pc.spec_rad = x.spec_rad;
+      pc.power_iters = x.power_iters;
+    }
     if (finished && !err && p->run_random && !p->run_cached) {
       auto &pc = p->pcache;
       pc.valid = 1;
@@ -1250,8 +1286,8 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   const int rc = build_layout(p, layout_key(p));
   if (rc) return rc;
   p->planes_dirty = 1;  // 1/diag(J D^-1 J^T) depends on D
-  p->matrix_gen++;      // a new A: the cached power method no longer applies
-  p->pcache.valid = 0;
+  p->matrix_gen++;      // a new A: the cached power methods no longer apply
+  p->pcache.valid = p->pcache_ev.valid = 0;
   return MPRGP_OK;
 }
 
@@ -1381,12 +1417,13 @@ int mprgp_problem_get_face(mprgp_problem *p, unsigned char *face) {
 int mprgp_problem_set_power_cache(mprgp_problem *p, int enable) {
   if (!p) return fail(MPRGP_INVALID, "set_power_cache");
   p->pcache_on = enable ? 1 : 0;
-  if (!enable) p->pcache.valid = 0;
+  if (!enable) p->pcache.valid = p->pcache_ev.valid = 0;
   return MPRGP_OK;
 }
 
 int mprgp_problem_set_ev(mprgp_problem *p, const double *ev) {
   if (!p) return fail(MPRGP_INVALID, "set_ev");
+  p->ev_gen++;
   if (!ev) { p->ev_valid = 0; return MPRGP_OK; }
   CK(cudaMemcpyAsync(p->ev, ev, sizeof(double) * 3 * (size_t)p->nv, cudaMemcpyHostToDevice,
                      p->ctx->stream));

@@ -130,6 +130,13 @@ __device__ __forceinline__ unsigned int atom_add_acq_rel(unsigned int *p, unsign
                : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
+__device__ __forceinline__ unsigned long long atom_add_acq_rel(unsigned long long *p,
+                                                               unsigned long long v) {
+  unsigned long long old;
+  asm volatile("atom.add.acq_rel.gpu.global.u64 %0, [%1], %2;"
+               : "=l"(old) : "l"(p), "l"(v) : "memory");
+  return old;
+}
 __device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
@@ -1932,7 +1939,8 @@ template <bool kAll>
 __device__ __forceinline__ void phase_item(const EngineArgs &args, int item, PowCtl *pc,
                                            cudaGraphConditionalHandle h, int signal,
                                            InstDesc &sD, InstState &sS, RedBuf &red,
-                                           double (&sums)[kPart], int &s_last) {
+                                           double (&sums)[kPart], int &s_last,
+                                           unsigned int active) {
   const int inst = instance_of(args.item_inst, args.item_prefix, args.ninst, item);
   __syncthreads();  // the previous item's readers of sD/sS are done
   // desc and state in one round of loads when the run's states are an array
@@ -2002,21 +2010,21 @@ __device__ __forceinline__ void phase_item(const EngineArgs &args, int item, Pow
     }
     *sD.st = S;
     *sD.cnt = 0u;
-    // `active` is read before this finalize is counted: only the last
-    // finalize of the launch rewrites it, after every other one was counted.
-    const unsigned int active = pc->active;
-    if (kAll ? S.phase != PH_DONE : power_phase(S.phase)) atomicAdd(&pc->busy, 1u);
-    const unsigned int old = atom_add_acq_rel(&pc->fin, 1u);
-    if (old == active - 1u) {
-      const unsigned int busy = atomicAdd(&pc->busy, 0u);
+    // One atomic counts this finalize (low word) and, if the instance goes
+    // on, a busy instance (high word); `active` was read at the launch's
+    // start (only the last finalize of a launch rewrites it).  The next
+    // launch sees these writes at the kernel boundary.
+    const bool still = kAll ? S.phase != PH_DONE : power_phase(S.phase);
+    const unsigned long long old =
+        atom_add_acq_rel(&pc->finbusy, 1ull + (still ? (1ull << 32) : 0ull));
+    if ((unsigned int)old == active - 1u) {
+      const unsigned int busy = (unsigned int)(old >> 32) + (still ? 1u : 0u);
       const unsigned int launches = pc->launches + 1u;
       const bool more = busy > 0u && launches < pc->limit;
       pc->launches = launches;
       pc->active = busy;
-      pc->busy = 0u;
-      pc->fin = 0u;
+      pc->finbusy = 0ull;
       pc->stop = more ? 0u : 1u;
-      __threadfence();
       if (signal) cudaGraphSetConditional(h, more ? 1u : 0u);
     }
   }
@@ -2037,9 +2045,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   __shared__ int s_last;
   if (*(volatile unsigned int *)&pc->stop) return;  // written by an earlier launch
   if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
+  const unsigned int active = *(volatile unsigned int *)&pc->active;
   const EngineArgs args = *pargs;
   for (int item = blockIdx.x; item < args.total_items; item += gridDim.x)
-    phase_item<kAll>(args, item, pc, h, signal, sD, sS, red, sums, s_last);
+    phase_item<kAll>(args, item, pc, h, signal, sD, sS, red, sums, s_last, active);
 }
 
 // ------------------------------------------------ persistent power loop -----

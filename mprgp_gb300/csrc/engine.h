@@ -131,11 +131,15 @@ struct Ctl {
 // Loop control of the power-method graph (see power_kernel).
 struct PowCtl {
   unsigned int active;    // instances in a power phase when the current launch began
-  unsigned int fin;       // of those, finalized in the current launch
-  unsigned int busy;      // of those, still in a power phase after their finalize
+  unsigned int fin;       // settle-kernel CTAs done in the current body (power-step loop)
+  unsigned int busy;      // instances still in a power phase (settle kernel) / the last
+                          // phase with one (persistent power loop)
   unsigned int launches;  // launches that did work so far
   unsigned int limit;     // stop after this many launches
   unsigned int stop;      // set when the loop is over: later launches return at once
+  // the phase kernel's finalizes of the current launch (low word) and, of
+  // those, the instances still going on (high word), counted by one atomic
+  unsigned long long finbusy;
 };
 constexpr int kPowerUnroll = 8;  // power launches per evaluation of the loop condition
 constexpr int kPowOwn = 4;       // items per CTA of the persistent power loop

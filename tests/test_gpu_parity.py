@@ -308,6 +308,55 @@ def test_power_cache_is_exact(ctx, precision):
     pr.close()
 
 
+@pytest.mark.parametrize("precision", [M.PREC_FP64, M.PREC_MIXED])
+def test_warm_start_power_cache_is_exact(ctx, precision):
+    """A solve whose power method starts from the stored vector ev and runs to
+    its iteration limit leaves ev unchanged; the next solve of the same
+    problem from the same ev reuses its result and is bitwise the solve that
+    runs it again.  A new ev or a new A invalidates the reuse."""
+    qp = M.beam(6, 5, 12, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=13)
+    # a tol the power method does not reach in 1001 iterations from a fixed,
+    # non-eigen start vector: it stores no new ev
+    opt = M.default_options(tol=1e-10 * np.linalg.norm(qp.b), max_it=20000, kind=M.KIND_PLANES,
+                            project_x0=1, seed=SEED, precision=precision, use_ev=1)
+    ev = np.random.default_rng(5).standard_normal(qp.n)
+    ev /= np.linalg.norm(ev)
+    pr = M.load_beam(ctx, qp, precisions=3)
+    pr.set_ev(ev)
+    runs = []
+    for cache in (True, True, False):
+        pr.set_power_cache(cache)
+        pr.set_x(qp.x0)
+        st = pr.solve(opt)
+        runs.append((pr.get_x(), pr.get_face(), st))
+    (x0, f0, s0), (x1, f1, s1), (x2, f2, s2) = runs
+    assert s0.power_iters == 1001  # ran to the limit: ev kept
+    for x, f, st in ((x1, f1, s1), (x2, f2, s2)):
+        assert np.array_equal(x, x0) and np.array_equal(f, f0)
+        assert (st.code, st.iterations, st.power_iters, st.spec_rad, st.alpha_bar, st.residual) == \
+            (s0.code, s0.iterations, s0.power_iters, s0.spec_rad, s0.alpha_bar, s0.residual)
+    assert s1.spmv_fp64 + s1.spmv_fp32 < s0.spmv_fp64 + s0.spmv_fp32  # reused
+    assert s2.spmv_fp64 + s2.spmv_fp32 == s0.spmv_fp64 + s0.spmv_fp32  # cache off: recomputed
+    # with the cache off a solve still records its result: back on, the next
+    # solve reuses it
+    pr.set_power_cache(True)
+    pr.set_x(qp.x0)
+    sb = pr.solve(opt)
+    assert sb.spmv_fp64 + sb.spmv_fp32 < s0.spmv_fp64 + s0.spmv_fp32
+    assert np.array_equal(pr.get_x(), x0) and sb.spec_rad == s0.spec_rad
+    # a new ev (here the same values, uploaded again) and a new A invalidate it
+    pr.set_ev(ev)
+    pr.set_x(qp.x0)
+    s3 = pr.solve(opt)
+    assert s3.spmv_fp64 + s3.spmv_fp32 == s0.spmv_fp64 + s0.spmv_fp32
+    pr.set_matrix(qp.row_ptr, qp.cols, qp.vals, 3)
+    pr.set_x(qp.x0)
+    s4 = pr.solve(opt)
+    assert s4.spmv_fp64 + s4.spmv_fp32 == s0.spmv_fp64 + s0.spmv_fp32
+    assert np.array_equal(pr.get_x(), x0)
+    pr.close()
+
+
 GOLDEN = sorted(__import__("glob").glob(__import__("os").path.join(
     __import__("os").path.dirname(__file__), "golden", "*.npz")))
 
