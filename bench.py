@@ -183,16 +183,18 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def autotune_ctx(args, ctx, sample, precision):
+def autotune_ctx(args, ctx, sample, precision, power_cache=False):
     """Untimed: pick launch shapes for this workload on a sample of it (an
-    explicit --tuning wins)."""
+    explicit --tuning wins).  power_cache: tune the solves that reuse a first
+    solve's power method (timestep loops)."""
     if args.tuning is not None:
         ctx.set_tuning(args.tuning, 0)
         return {"explicit_tuning_bits": args.tuning}
     if args.no_autotune:
         return None
     from mprgp_gb300 import autotune
-    r = autotune.tune(ctx, sample, precision=precision, reps=1, use_cache=False)
+    r = autotune.tune(ctx, sample, precision=precision, reps=1, use_cache=False,
+                      power_cache=power_cache)
     return {"config": r["config"], "sample_ms": round(r["ms"], 3),
             "default_ms": round(r["default_ms"], 3), "candidates": len(r["tried"]),
             "seconds": round(r["seconds"], 2), "sample_size": len(sample)}
@@ -591,7 +593,8 @@ def run_timesteps(args):
     ctx = M.Context(local)
     mixed = args.form != "plain"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
-    tuning = autotune_ctx(args, ctx, [qp], prec)
+    # every timestep after the first reuses the power method (A is fixed)
+    tuning = autotune_ctx(args, ctx, [qp], prec, power_cache=True)
     fem = M.FemMesh(ctx, tets, X, params["young"], params["poisson"], params["rho"])
     prob, ref = M.Problem(ctx, qp.nv), M.Problem(ctx, qp.nv)
     torch.cuda.synchronize()
