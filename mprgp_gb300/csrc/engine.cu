@@ -2196,13 +2196,19 @@ __device__ __forceinline__ void warp_item_sums(const double *pp, int nitems, int
     for (int j = lane; j < n; j += 32) cp_async16(stage + j, pp + 2 * (size_t)(base + j));
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     __syncwarp();
+    // round by round (base is a multiple of kThreads), so the sixteen sums of
+    // a round are independent; each thread's items still add in item order
+    for (int r = 0; r < n; r += kThreads) {
 #pragma unroll
-    for (int i = 0; i < kThreads / 32; ++i)
-      for (int j = lane + 32 * i; j < n; j += kThreads) {  // base is a multiple of kThreads
-        const double2 q = stage[j];
-        t0[i] += q.x;
-        t1[i] += q.y;
+      for (int i = 0; i < kThreads / 32; ++i) {
+        const int j = r + lane + 32 * i;
+        if (j < n) {
+          const double2 q = stage[j];
+          t0[i] += q.x;
+          t1[i] += q.y;
+        }
       }
+    }
   }
   double a0 = t0[0], a1 = t1[0];
 #pragma unroll
@@ -2254,13 +2260,15 @@ __device__ __forceinline__ void advance_power_sums(const InstDesc &D, InstState 
 // update does not take registers from the row warps' matrix pass.
 __device__ __noinline__ void step_advance(const InstDesc &D, const InstState &in, InstState &out,
                                           const double *pp, int lane, double2 *stage) {
+  {  // the whole warp copies, lane 0 then advances the copy in place
+    const int *a = reinterpret_cast<const int *>(&in);
+    int *b = reinterpret_cast<int *>(&out);
+    for (int w = lane; w < (int)(sizeof(InstState) / 4); w += 32) b[w] = a[w];
+  }
   double s2[2];
   warp_item_sums(pp, D.nitems, lane, stage, s2);
-  if (lane == 0) {
-    InstState S = in;
-    advance_power_sums(D, S, s2);
-    out = S;
-  }
+  __syncwarp();
+  if (lane == 0) advance_power_sums(D, out, s2);
 }
 
 template <int kMinBlocks>
