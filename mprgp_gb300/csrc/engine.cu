@@ -2043,10 +2043,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
   __shared__ RedBuf red;
   __shared__ double sums[kPart];
   __shared__ int s_last;
-  if (*(volatile unsigned int *)&pc->stop) return;  // written by an earlier launch
-  if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
+  // the loop control and the arguments in one round of loads (the stop test
+  // would otherwise hold back the others)
+  const unsigned int stop = *(volatile unsigned int *)&pc->stop;  // written by an earlier launch
   const unsigned int active = *(volatile unsigned int *)&pc->active;
   const EngineArgs args = *pargs;
+  if (stop) return;
+  if (threadIdx.x == 0) g_staged = 0;  // this kernel never stages A (no dynamic smem)
   for (int item = blockIdx.x; item < args.total_items; item += gridDim.x)
     phase_item<kAll>(args, item, pc, h, signal, sD, sS, red, sums, s_last, active);
 }
@@ -2279,12 +2282,14 @@ __global__ void __launch_bounds__(kStepThreads, kMinBlocks)
   __shared__ RedBuf red;
   __shared__ __align__(16) double2 sItems[kSumStage];
   __shared__ int s_inst;
-  if (*(volatile unsigned int *)&pc->stop) return;  // the loop is over
+  // the stop flag and the arguments in one round of loads
+  const unsigned int stop = *(volatile unsigned int *)&pc->stop;  // the loop is over
+  const EngineArgs args = *pargs;
+  if (stop) return;
   if (threadIdx.x == 0) {
     g_staged = 0;
     s_inst = -1;
   }
-  const EngineArgs args = *pargs;
   const int par = node & 1;
   const InstState *st_in = node == 0 ? args.states : args.pst[par ^ 1];
   InstState *st_out = args.pst[par];
@@ -2366,8 +2371,9 @@ __global__ void __launch_bounds__(32)
     power_settle_kernel(const EngineArgs *__restrict__ pargs, PowCtl *pc,
                         cudaGraphConditionalHandle h, int signal) {
   __shared__ __align__(16) double2 sItems[kSumStage];
-  if (*(volatile unsigned int *)&pc->stop) return;
+  const unsigned int stop = *(volatile unsigned int *)&pc->stop;
   const EngineArgs args = *pargs;
+  if (stop) return;
   constexpr int last = (kPowerUnroll - 1) & 1;
   const InstState *st_in = args.pst[last];
   InstState *st_out = const_cast<InstState *>(args.states);
