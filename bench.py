@@ -78,7 +78,8 @@ def parse():
                     help="time the standalone y = A x (mprgp_problem_spmv) on the config's "
                          "matrix instead of the solver, FP64 and FP32 values")
     ap.add_argument("--tuning", type=int, default=None,
-                    help="launch-form bits for mprgp_context_set_tuning (bit 2: power loop from "
+                    help="launch-form bits for mprgp_context_set_tuning (bit 6: phase-kernel power "
+                         "loop instead of the power-step loop; bit 2: power loop from "
                          "host-stream launches instead of the CUDA-graph WHILE loop)")
     return ap.parse_args()
 
@@ -200,6 +201,22 @@ def autotune_ctx(args, ctx, sample, precision, power_cache=False):
             "seconds": round(r["seconds"], 2), "sample_size": len(sample)}
 
 
+def power_form(tuning):
+    """The power-method loop a tuning selects (autotuner config or explicit
+    mprgp_context_set_tuning bits)."""
+    if not tuning:
+        return "step"
+    if "config" in tuning:
+        f = tuning["config"].get("power", "step")
+        return {"step-stream": "step", "stream": "graph"}.get(f, f)
+    bits = tuning.get("explicit_tuning_bits", 0)
+    if bits & 2:
+        return "engine"
+    if bits & 32:
+        return "persistent"
+    return "graph" if bits & 64 else "step"
+
+
 def cpu_baseline(qp, threads=1):
     """One full solve of the same QP by the CPU restatement of the reference."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -300,8 +317,13 @@ def run_gb300(args):
     if power_ms > 0:  # the power loop ran as its own kernel
         pow_launch_ms = power_ms / max(1, passes)
         achieved = pass_bytes / (pow_launch_ms / 1e3) / 1e9
-        traffic = committed_traffic(args.config, args.form, "power_kernel")
-        dominant = "mprgp::power_kernel (CUDA-graph loop)"
+        form = power_form(tuning)
+        kname = {"step": "power_step_kernel", "persistent": "power_persistent_kernel"}.get(
+            form, "power_kernel")
+        traffic = committed_traffic(args.config, args.form, kname)
+        dominant = {"step": "mprgp::power_step_kernel (power-step loop, CUDA graph)",
+                    "persistent": "mprgp::power_persistent_kernel (one cooperative launch)"}.get(
+            form, "mprgp::phase_kernel (power phases, CUDA-graph loop)")
         eng_ms = (solver1 - solver0) - power_ms
     else:  # the tuning put the power phases into the persistent engine
         pow_launch_ms = (solver1 - solver0) / max(1, len(stats))

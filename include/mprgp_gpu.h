@@ -133,12 +133,14 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * cooperative engine; bit 5 = 1 runs the power method as one persistent
  * cooperative launch (a grid barrier per phase, state kept on chip) in
  * synchronous runs whose items fit four per resident CTA, the graph loop
- * otherwise; bit 6 = 1 runs the power method as the power-step loop: no
+ * otherwise.  By default the power kernel runs as the power-step loop: no
  * launch finalizes its own phase -- every CTA of the next launch reduces the
  * item partials and advances its copy of the state with one extra warp while
  * its rows already form their products, and a settle kernel ends each graph
- * body (bit 2 applies to it too); ctas_per_sm caps the persistent grid
- * (0 = every resident CTA).  Every setting gives bitwise the same results. */
+ * body; bit 6 = 1 runs the phase kernel instead, whose last CTA finalizes
+ * each launch (bits 2 and 3 apply to both loops as described).  ctas_per_sm
+ * caps the persistent grid (0 = every resident CTA).  Every setting gives
+ * bitwise the same results. */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
 /* Small instances -- up to `cluster` items of 256 vertices -- are solved by
  * one thread-block cluster each, one CTA per item (state in shared memory,

@@ -9,14 +9,15 @@ the tuner checks that for the setting it picks.
                vertex rows; instances up to that many items take it)
   cluster_items  items per CTA allowed in the largest cluster (larger
                instances then also run as independent clusters)
-  power        the power method's loop: a CUDA-graph WHILE loop of the power
-               kernel, plain stream launches of it, phases of the persistent
-               engine, one persistent cooperative launch of its own (grid
-               barrier per phase; synchronous runs whose items fit, else the
-               graph loop), or the power-step loop (each launch advances the
-               states the previous one left while its rows form their
-               products; graph or stream launches)
-  power_regs   the power kernel's register budget: 40 (6 CTAs per SM) or
+  power        the power method's loop: the power-step loop (each launch
+               advances the states the previous one left while its rows form
+               their products; CUDA-graph WHILE loop or plain stream
+               launches; the default), the phase kernel whose last CTA
+               finalizes each launch (graph or stream), phases of the
+               persistent engine, or one persistent cooperative launch of its
+               own (grid barrier per phase; synchronous runs whose items fit,
+               else the power-step graph loop)
+  power_regs   the phase kernel's register budget: 40 (6 CTAs per SM) or
                64 (4 CTAs per SM, more loads in flight per thread)
   engine       the large instances' MPRGP phases: the persistent cooperative
                engine, or a CUDA-graph loop of one launch per phase
@@ -40,19 +41,19 @@ import numpy as np
 
 from . import KIND_PLANES, PREC_MIXED, Context, default_options, load_beam
 
-DEFAULT = {"cluster": 16, "cluster_items": 1, "power": "graph", "power_regs": 40,
+DEFAULT = {"cluster": 16, "cluster_items": 1, "power": "step", "power_regs": 40,
            "engine": "persistent", "ctas_per_sm": 0, "stage": 0}
 SPACE = {
     "cluster": [16, 8, 4, 0],
     "cluster_items": [1, 2, 4],
-    "power": ["graph", "stream", "engine", "persistent", "step", "step-stream"],
+    "power": ["step", "step-stream", "graph", "stream", "engine", "persistent"],
     "power_regs": [40, 64],
     "engine": ["persistent", "graph"],
     "ctas_per_sm": [0, 3, 2],
     "stage": [0, 1],
 }
-_POWER_BITS = {"graph": 0, "engine": 2, "stream": 4, "persistent": 32, "step": 64,
-               "step-stream": 64 | 4}
+_POWER_BITS = {"step": 0, "step-stream": 4, "graph": 64, "stream": 64 | 4, "engine": 2,
+               "persistent": 32}
 
 
 def cache_path() -> str:

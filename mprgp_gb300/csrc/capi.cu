@@ -109,8 +109,8 @@ struct mprgp_context {
   int power_graph = 1;   // power-kernel loop as a CUDA-graph WHILE node (1) or stream launches (0)
   int power_variant = 0; // power kernel with 40 registers (0, 6 CTAs/SM) or 64 (1, 4 CTAs/SM)
   int bps_power_v[4] = {0, 0, 0, 0};  // per power-kernel variant (2: all phases, 3: power steps)
-  int power_step = 0;    // power loop as the power-step loop (1; deferred finalize) or the
-                         // phase kernel with a finalize per launch (0)
+  int power_step = 1;    // power loop as the power-step loop (1, the default; deferred
+                         // finalize) or the phase kernel with a finalize per launch (0)
   int power_persistent = 0;  // power loop as one persistent cooperative launch when the run
                             // is synchronous and its items fit (1)
   int bps_power_pp = 0;      // resident CTAs per SM of that kernel
@@ -1150,7 +1150,7 @@ int mprgp_context_set_tuning(mprgp_context *c, int stage, int ctas_per_sm) {
   c->power_variant = (stage & 8) ? 1 : 0;
   c->engine_graph = (stage & 16) ? 1 : 0;
   c->power_persistent = (stage & 32) ? 1 : 0;
-  c->power_step = (stage & 64) ? 1 : 0;
+  c->power_step = (stage & 64) ? 0 : 1;
   c->bps_power = c->bps_power_v[c->power_variant];
   stage &= 1;
   c->stage = stage;

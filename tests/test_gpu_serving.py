@@ -72,16 +72,19 @@ def test_same_alone_and_in_the_mix(ctx, precision, lanes):
 
 @pytest.mark.parametrize("lanes", [0, 3])
 def test_power_step_loop_served(ctx, lanes):
-    """Served with the power-step loop and power runs cut into short pieces
-    (20 launches a step: the loop stops at a body boundary and the next run
-    resumes from the settled state), every result equals the launch loop's
-    result for the request solved alone."""
+    """Served with the power-step loop (the default) and power runs cut into
+    short pieces (20 launches a step: the loop stops at a body boundary and
+    the next run resumes from the settled state), every result equals the
+    launch loop's result for the request solved alone."""
     dims = [(14, 8, 30), (16, 8, 32), (12, 10, 24), (5, 5, 5)]
     qps = [M.beam(*d, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=40 + i)
            for i, (d, e) in enumerate(zip(dims, [2, 1, 2, 0]))]
     precision = M.PREC_MIXED
-    alone = [ctx.solve_bsr(q, opts_for(q, precision), q.x0) for q in qps]
-    ctx.set_tuning(64, 0)
+    ctx.set_tuning(64, 0)  # the launch loop for the requests alone
+    try:
+        alone = [ctx.solve_bsr(q, opts_for(q, precision), q.x0) for q in qps]
+    finally:
+        ctx.set_tuning(0, 0)
     try:
         srv = M.Server(ctx, quantum_phases=64, power_launches=20, max_slots=4, lanes=lanes)
         tickets, done = {}, {}
