@@ -576,6 +576,47 @@ def test_power_step_loop_equals_launch_loop(precision):
         c.close()
 
 
+@pytest.mark.parametrize("precision", [M.PREC_MIXED, M.PREC_FP64])
+def test_power_step_loop_mixed_starts(precision):
+    """A batch whose instances start in different places -- half of them with
+    the power method cached (they skip it), half running it -- gives in the
+    power-step loop what each instance gives alone in the launch loop: the
+    step kernels carry the states of instances outside the power method
+    through unchanged."""
+    qps = [M.beam(a, b, c, extra_planes_max=e, extra_planes_min=e, plane_mode=2, seed=s)
+           for (a, b, c, e, s) in [(16, 16, 40, 2, 71), (24, 20, 30, 1, 72), (20, 12, 60, 2, 73),
+                                   (18, 14, 36, 1, 74)]]
+    c = M.Context(0)
+    try:
+        c.set_cluster(0)
+        c.set_tuning(64, 0)  # the launch loop, one instance at a time
+        ref = _solve_all(c, qps, precision)
+        c.set_tuning(0, 0)   # the power-step loop
+        probs, opts = [], []
+        for i, qp in enumerate(qps):
+            pr = M.load_beam(c, qp, precisions=3)
+            opt = M.default_options(tol=1e-10 * np.linalg.norm(qp.b), max_it=20000,
+                                    kind=M.KIND_PLANES, project_x0=1, seed=SEED,
+                                    precision=precision)
+            if i % 2 == 0:  # a first solve stores the power method's result
+                pr.set_x(qp.x0)
+                assert pr.solve(opt).code == 0
+            pr.set_x(qp.x0)
+            probs.append(pr)
+            opts.append(opt)
+        stats = c.solve_batch(probs, opts)
+        for i, (pr, st, (xr, fr, sr)) in enumerate(zip(probs, stats, ref)):
+            assert st.code == 0 and sr.code == 0
+            assert np.array_equal(pr.get_x(), xr) and np.array_equal(pr.get_face(), fr)
+            assert (st.iterations, st.power_iters, st.spec_rad) == \
+                (sr.iterations, sr.power_iters, sr.spec_rad)
+            assert (st.power_passes == 0) == (i % 2 == 0)  # cached ones skipped it
+        for pr in probs:
+            pr.close()
+    finally:
+        c.close()
+
+
 def test_invalid_column_reports_invalid(ctx):
     """A block column outside 0..nv-1 is caught on the device as A is
     converted (the conversion keeps every index in range): the solve and the
