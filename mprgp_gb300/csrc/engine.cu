@@ -1783,6 +1783,7 @@ __device__ __forceinline__ int find_instance(const int *prefix, int n, int item)
 // the item prefix when the run has no map.
 __device__ __forceinline__ int instance_of(const int *item_inst, const int *prefix, int n,
                                            int item) {
+  if (n == 1) return 0;  // a run of one instance needs no load
   return item_inst ? ldro(item_inst + item) : find_instance(prefix, n, item);
 }
 
