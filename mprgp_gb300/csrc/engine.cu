@@ -2499,20 +2499,48 @@ __global__ void __launch_bounds__(kThreads, MPRGP_CLUSTER_MIN_BLOCKS) cluster_ke
       if (threadIdx.x < ns || (wmin && threadIdx.x == kMinSlot)) cpart[par][li][threadIdx.x] = r;
     }
     cluster_sync_acq_rel();
-    double acc[kPart];
+    if (nitems <= 32) {
+      // One warp per slot does what the block reduction below does when each
+      // thread holds at most one item: lane l takes item l (thread l's sum),
+      // then seven more terms from threads that hold none (the identity:
+      // +0.0, or DBL_MAX for the min slot), then the shuffle tree -- the same
+      // operations in the same order, without the block's barriers.
+      const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+      const int nrows = ns + (wmin ? 1 : 0);
+      // the slots this phase does not produce read as 0.0
+      if (threadIdx.x < kPart && threadIdx.x >= ns && !(wmin && threadIdx.x == kMinSlot))
+        sums[threadIdx.x] = 0.0;
+      if (wp < nrows) {
+        const bool is_min = wmin && wp == ns;
+        const int k = is_min ? kMinSlot : wp;
+        double a = is_min ? DBL_MAX : 0.0;
+        if (lane < nitems) {
+          const unsigned int base =
+              dsmem_addr(&cpart[par][lane / (int)csize][0], (unsigned int)lane % csize);
+          const double x = ld_dsmem(base + 8u * (unsigned int)k);
+          a = is_min ? fmin(a, x) : a + x;
+        }
 #pragma unroll
-    for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-    for (int it = threadIdx.x; it < nitems; it += kThreads) {
-      const unsigned int base = dsmem_addr(&cpart[par][it / (int)csize][0], (unsigned int)it % csize);
-#pragma unroll
-      for (int k = 0; k < kPart; ++k) {
-        if (k == kMinSlot ? !wmin : k >= ns) continue;
-        const double x = ld_dsmem(base + 8u * (unsigned int)k);
-        acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+        for (int i = 1; i < kThreads / 32; ++i) a = is_min ? fmin(a, DBL_MAX) : a + 0.0;
+        a = is_min ? warp_min(a) : warp_sum(a);
+        if (lane == 0) sums[k] = a;
       }
+    } else {
+      double acc[kPart];
+#pragma unroll
+      for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+      for (int it = threadIdx.x; it < nitems; it += kThreads) {
+        const unsigned int base = dsmem_addr(&cpart[par][it / (int)csize][0], (unsigned int)it % csize);
+#pragma unroll
+        for (int k = 0; k < kPart; ++k) {
+          if (k == kMinSlot ? !wmin : k >= ns) continue;
+          const double x = ld_dsmem(base + 8u * (unsigned int)k);
+          acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+        }
+      }
+      const double t = block_reduce(acc, red, ns, wmin);
+      if (threadIdx.x < kPart) sums[threadIdx.x] = t;
     }
-    const double t = block_reduce(acc, red, ns, wmin);
-    if (threadIdx.x < kPart) sums[threadIdx.x] = t;
     __syncthreads();
     if (threadIdx.x == 0) advance(sD, sS, sums);  // in place: no copy of the state
     __syncthreads();
