@@ -184,7 +184,7 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def autotune_ctx(args, ctx, sample, precision, power_cache=False):
+def autotune_ctx(args, ctx, sample, precision, power_cache=False, fixed=None):
     """Untimed: pick launch shapes for this workload on a sample of it (an
     explicit --tuning wins).  power_cache: tune the solves that reuse a first
     solve's power method (timestep loops)."""
@@ -195,7 +195,7 @@ def autotune_ctx(args, ctx, sample, precision, power_cache=False):
         return None
     from mprgp_gb300 import autotune
     r = autotune.tune(ctx, sample, precision=precision, reps=1, use_cache=False,
-                      power_cache=power_cache)
+                      power_cache=power_cache, fixed=fixed)
     return {"config": r["config"], "sample_ms": round(r["ms"], 3),
             "default_ms": round(r["default_ms"], 3), "candidates": len(r["tried"]),
             "seconds": round(r["seconds"], 2), "sample_size": len(sample)}
@@ -820,7 +820,15 @@ def run_serve(args):
 
     mixed = args.form != "plain"
     prec = M.PREC_MIXED if mixed else M.PREC_FP64
-    tuning = autotune_ctx(args, ctx, serve_sample(win, 48), prec)
+    # Serving keeps the cluster solver (one item per CTA), the power-step
+    # loop and the persistent engine: measured on this stream, they give the
+    # best solves/s at the lowest median latency.  The tuner's sample (one
+    # batched solve) measures batch throughput alone -- without the cluster
+    # solver the small requests wait for the batched runs, about doubling
+    # their median latency -- so only the remaining knobs are tuned.
+    tuning = autotune_ctx(args, ctx, serve_sample(win, 48), prec,
+                          fixed={"cluster": 16, "cluster_items": 1, "power": "step",
+                                 "power_regs": 40, "engine": "persistent"})
     pl = StreamPlayer(ctx, win, rel_tol=REL_TOL, seed=SEED)
     served = dict(max_slots=512, quantum=512, power_launches=1003, cluster_quantum=0,
                   lanes=args.lanes)

@@ -112,14 +112,17 @@ def _time(ctx, probs, opts, x0s, reps):
 
 
 def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5EED,
-         use_cache=True, verbose=False, power_cache=False) -> dict:
+         use_cache=True, verbose=False, power_cache=False, fixed=None) -> dict:
     """Picks and applies the fastest launch shapes for batched solves of
     `qps`; returns {"config", "ms", "default_ms", "tried", "seconds", "cached"}.
+    `fixed` pins knobs to given values (they are not searched).
     power_cache=True tunes the solves that follow a first one on the same
     matrices (a timestep loop): the power method's result is reused, so the
     timed solves are the MPRGP phases alone."""
     t0 = time.perf_counter()
-    sig = signature(ctx, qps, precision) + ("-pc" if power_cache else "")
+    fixed = dict(fixed or {})
+    sig = signature(ctx, qps, precision) + ("-pc" if power_cache else "") + \
+        "".join(f"-{k}{v}" for k, v in sorted(fixed.items()))
     path = cache_path()
     if use_cache:
         hit = _load(path).get(sig)
@@ -146,7 +149,7 @@ def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5
                     print(f"autotune {cfg} {tried[key][0]:.3f} ms", flush=True)
             return tried[key]
 
-        best = dict(DEFAULT)
+        best = dict(DEFAULT, **fixed)
         if power_cache:  # an untimed first solve computes the power method once
             apply(ctx, best)
             _time(ctx, probs, opts, x0s, 1)
@@ -161,6 +164,7 @@ def tune(ctx: Context, qps, precision=PREC_MIXED, reps=2, rel_tol=1e-8, seed=0x5
                  [{"engine": v} for v in SPACE["engine"]],
                  [{"ctas_per_sm": v} for v in SPACE["ctas_per_sm"]],
                  [{"stage": v} for v in SPACE["stage"]]]
+        steps = [st for st in steps if not any(k in fixed for k in st[0])]
         for step in steps:
             for change in step:
                 cand = dict(best, **change)
