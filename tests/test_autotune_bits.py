@@ -1,6 +1,7 @@
 """Host logic of the autotuner (no GPU): the launch-form bits each setting
 maps to (mprgp_context_set_tuning, include/mprgp_gpu.h), the cluster-size
 fallback, and the knobs a caller pins."""
+import numpy as np
 import pytest
 
 from mprgp_gb300 import autotune
@@ -60,3 +61,56 @@ def test_default_is_the_power_step_loop_with_every_knob_at_zero_bits():
 def test_cluster_falls_back_to_offered_sizes():
     _, calls = bits_of({"cluster": 16}, max_cluster=4)
     assert ("cluster", 4) in calls and ("cluster", 16) not in calls
+
+
+class FakeProblem:
+    def __init__(self):
+        self.cache = None
+
+    def set_power_cache(self, on):
+        self.cache = on
+
+    def close(self):
+        pass
+
+
+class FakeQP:
+    nv = 4000
+    b = np.ones(12)
+    x0 = np.zeros(12)
+
+
+def _tune_with_fake_times(monkeypatch, cost, **kw):
+    """tune() over a fake context whose timed solves cost cost(cluster, bits)."""
+    ctx = FakeCtx()
+    ctx.info = lambda: (152, 4)
+    timed = []
+
+    def fake_time(c, probs, opts, x0s, reps):
+        cl = [k[1] for k in c.calls if k[0] == "cluster"][-1]
+        bits = [k[1] for k in c.calls if k[0] == "tuning"][-1]
+        timed.append((cl, bits, reps))
+        return cost(cl, bits), [np.zeros(3) for _ in probs]
+
+    monkeypatch.setattr(autotune, "load_beam", lambda c, q, precisions=3: FakeProblem())
+    monkeypatch.setattr(autotune, "_time", fake_time)
+    r = autotune.tune(ctx, [FakeQP(), FakeQP()], use_cache=False, **kw)
+    return r, ctx, timed
+
+
+def test_tuner_keeps_pinned_knobs_and_takes_clear_wins(monkeypatch):
+    # the graph-loop engine (bit 16) is 10 % faster, cluster 8 would be too
+    cost = lambda cl, bits: 100.0 * (0.9 if bits & 16 else 1.0) * (0.9 if cl == 8 else 1.0)
+    r, ctx, timed = _tune_with_fake_times(monkeypatch, cost, fixed={"cluster": 16})
+    assert r["config"]["cluster"] == 16 and r["config"]["engine"] == "graph"
+    assert {cl for cl, _, _ in timed} == {16}  # the pinned knob was never searched
+    # a 1 % difference is not a clear win: the incumbent stays
+    cost2 = lambda cl, bits: 100.0 * (0.99 if bits & 16 else 1.0)
+    r2, _, _ = _tune_with_fake_times(monkeypatch, cost2)
+    assert r2["config"]["engine"] == autotune.DEFAULT["engine"]
+
+
+def test_tuner_power_cache_runs_one_untimed_solve_first(monkeypatch):
+    r, ctx, timed = _tune_with_fake_times(monkeypatch, lambda cl, bits: 100.0, power_cache=True,
+                                          reps=2)
+    assert timed[0][2] == 1 and all(t[2] == 2 for t in timed[1:])
