@@ -125,9 +125,9 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * the persistent engine instead of the dedicated power kernel; bit 2 = 1
  * issues the power kernel's launches from the host stream instead of a
  * CUDA-graph WHILE loop (and likewise the graph loop of bit 4 when a run has
- * a phase quantum: one launch per phase of it); bit 3 = 1 uses the power
- * kernel built for 64
- * registers per thread (4 CTAs per SM) instead of 40 (6 CTAs per SM);
+ * a phase quantum: one launch per phase of it); bit 3 = 1 builds the phase
+ * kernel of bit 6 for 64 registers per thread (4 CTAs per SM) instead of 40
+ * (6 CTAs per SM);
  * bit 4 = 1 runs the large instances' phases as a CUDA-graph loop of
  * ordinary launches (one phase per launch) instead of the persistent
  * cooperative engine; bit 5 = 1 runs the power method as one persistent
@@ -138,7 +138,7 @@ int mprgp_context_counters(mprgp_context *ctx, long long *launches, double *solv
  * item partials and advances its copy of the state with one extra warp while
  * its rows already form their products, and a settle kernel ends each graph
  * body; bit 6 = 1 runs the phase kernel instead, whose last CTA finalizes
- * each launch (bits 2 and 3 apply to both loops as described).  ctas_per_sm
+ * each launch (bit 2 applies to both loops).  ctas_per_sm
  * caps the persistent grid (0 = every resident CTA).  Every setting gives
  * bitwise the same results. */
 int mprgp_context_set_tuning(mprgp_context *ctx, int stage, int ctas_per_sm);
