@@ -204,3 +204,29 @@ def test_reference_stall_is_reproduced():
     _, _, s, _ = H.oracle_solve("general", A, b, qp.x0, J, c, tol=1e-8 * np.linalg.norm(b),
                                 max_it=300)
     assert s["code"] == -1 and s["num_exp"] > 250 and s["num_prop"] == 0
+
+
+def test_power_method_keeps_ev_unless_it_converges():
+    """specRad (MPRGPSolver.h:42-79) writes ev only when it stops early (the
+    difference test or a vanishing norm).  A warm start that runs to the
+    1001-iteration cap leaves ev as it was, so a second solve from the same ev
+    runs the identical power method -- the property the GPU's exact reuse of
+    warm-started power methods rests on."""
+    qp = M.beam(6, 5, 12, extra_planes_max=2, extra_planes_min=2, plane_mode=2, seed=13)
+    A, b, J, c = H.qp_from_beam(qp)
+    ev0 = np.random.default_rng(5).standard_normal(qp.n)
+    ev0 /= np.linalg.norm(ev0)
+    nb = float(np.linalg.norm(b))
+    # a stopping test the power method does not meet in 1001 iterations from
+    # this start: ev unchanged, results repeat
+    x1, _, s1, ev1 = H.oracle_solve("general", A, b, qp.x0, J, c, tol=1e-10 * nb,
+                                    max_it=20000, ev=ev0)
+    assert s1["power_iters"] == 1001 and np.array_equal(ev1, ev0)
+    x2, _, s2, ev2 = H.oracle_solve("general", A, b, qp.x0, J, c, tol=1e-10 * nb,
+                                    max_it=20000, ev=ev1)
+    assert np.array_equal(ev2, ev0) and np.array_equal(x2, x1)
+    assert (s2["spec_rad"], s2["iterations"]) == (s1["spec_rad"], s1["iterations"])
+    # a loose one: it stops early and stores a new ev
+    _, _, s3, ev3 = H.oracle_solve("general", A, b, qp.x0, J, c, tol=1e-2 * nb, max_it=20000,
+                                   ev=ev0)
+    assert s3["power_iters"] < 1001 and not np.array_equal(ev3, ev0)
