@@ -935,8 +935,7 @@ def run_serve(args):
         "solve": {"iterations_max": int(max(its)), "iterations_mean": round(float(np.mean(its)), 1)},
         "roofline": {"bound": "hbm",
                      "kernel": "all solver kernels (cluster_kernel, the power-method loop, the "
-                               "engine's MPRGP phases; no single one dominates the stream: "
-                               "profiles/launches_c4_serving.md)",
+                               "engine's MPRGP phases; no single one dominates the stream)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "traffic": None,
