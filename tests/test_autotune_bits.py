@@ -114,3 +114,19 @@ def test_tuner_power_cache_runs_one_untimed_solve_first(monkeypatch):
     r, ctx, timed = _tune_with_fake_times(monkeypatch, lambda cl, bits: 100.0, power_cache=True,
                                           reps=2)
     assert timed[0][2] == 1 and all(t[2] == 2 for t in timed[1:])
+
+
+def test_bench_names_the_power_loop_of_a_tuning():
+    """bench.py labels the c1 roofline by the power-method loop a tuning
+    selects (autotuner config or explicit bits)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    assert bench.power_form(None) == "step"
+    assert bench.power_form({"config": dict(autotune.DEFAULT)}) == "step"
+    assert bench.power_form({"config": dict(autotune.DEFAULT, power="stream")}) == "graph"
+    assert bench.power_form({"explicit_tuning_bits": 0}) == "step"
+    assert bench.power_form({"explicit_tuning_bits": 64 | 4}) == "graph"
+    assert bench.power_form({"explicit_tuning_bits": 32}) == "persistent"
+    assert bench.power_form({"explicit_tuning_bits": 2}) == "engine"
