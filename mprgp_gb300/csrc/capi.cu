@@ -174,9 +174,10 @@ struct mprgp_problem {
     double spec_rad = 0.0;
   } pcache;
   // Result of the last power method that started from the stored vector ev
-  // and left ev unchanged (it ran to its iteration limit): a deterministic
-  // function of (A, ev, precision form), reused while the three stay the
-  // same -- a resident scene's follow-up timesteps warm-start from ev.
+  // and left ev unchanged (it ran to its iteration limit; specRad writes ev
+  // only when it stops early, MPRGPSolver.h:62-74): a deterministic function
+  // of (A, ev, precision form), reused while the three stay the same -- a
+  // resident scene's follow-up timesteps warm-start from ev.
   struct {
     int valid = 0, prec = 0, power_iters = 0;
     unsigned long long gen = 0, ev_gen = 0;
