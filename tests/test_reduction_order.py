@@ -7,7 +7,12 @@ bitwise the launch form's finalize: thread t sums items t, t+256, ... in
 order, block_reduce's warp adds the threads' sums l, l+32, ..., l+224, and a
 shuffle tree closes.  The GPU tests check the two kernels against each other
 for instances of up to 1,536 items (one round); this restatement checks the
-orders agree for any item count, including several rounds."""
+orders agree for any item count, including several rounds.
+
+The cluster solver's cross-CTA reduction for clusters of up to 32 items runs
+as one warp per slot: lane l takes item l and then adds the seven identity
+terms the block reduction would add from threads that hold no item, so even
+a -0.0 partial comes out as the block reduction leaves it."""
 import numpy as np
 import pytest
 
@@ -88,3 +93,49 @@ def test_the_check_sees_a_changed_order():
     for i in range(1, K_THREADS // 32):
         a = a + t[:, i, 0]
     assert warp_sum(a) != finalize_order(p)[0]
+
+
+def block_reduce_of_items(vals, is_min=False):
+    """The cluster solver's general cross-CTA path for one slot: thread t
+    takes item t (identity start), then block_reduce's warp, then the tree."""
+    ident = np.finfo(np.float64).max if is_min else 0.0
+    acc = np.full(K_THREADS, ident)
+    for t, x in enumerate(vals):
+        acc[t] = min(acc[t], x) if is_min else acc[t] + x
+    a = acc[0:32].copy()
+    for i in range(1, K_THREADS // 32):
+        b = acc[32 * i:32 * i + 32]
+        a = np.minimum(a, b) if is_min else a + b
+    if is_min:
+        v = a.copy()
+        for o in (16, 8, 4, 2, 1):
+            v = np.minimum(v, v[np.arange(32) ^ o])
+        return v[0]
+    return warp_sum(a)
+
+
+def one_warp_of_items(vals, is_min=False):
+    """The one-warp path (clusters of up to 32 items): lane l takes item l,
+    then seven identity terms, then the tree."""
+    ident = np.finfo(np.float64).max if is_min else 0.0
+    a = np.full(32, ident)
+    for l, x in enumerate(vals):
+        a[l] = min(a[l], x) if is_min else a[l] + x
+    for _ in range(1, K_THREADS // 32):
+        a = np.minimum(a, ident) if is_min else a + 0.0
+    if is_min:
+        v = a.copy()
+        for o in (16, 8, 4, 2, 1):
+            v = np.minimum(v, v[np.arange(32) ^ o])
+        return v[0]
+    return warp_sum(a)
+
+
+@pytest.mark.parametrize("nitems", [1, 2, 7, 16, 31, 32])
+@pytest.mark.parametrize("is_min", [False, True])
+def test_one_warp_cross_cta_reduction_is_the_block_reduction(nitems, is_min):
+    vals = list(_partials(nitems)[:, 0])
+    if nitems > 1:
+        vals[1] = -0.0  # the identity terms keep what the block reduction does with it
+    got, want = one_warp_of_items(vals, is_min), block_reduce_of_items(vals, is_min)
+    assert np.float64(got).tobytes() == np.float64(want).tobytes()
