@@ -84,12 +84,15 @@ def parse():
     return ap.parse_args()
 
 
-def workload_qp(name):
-    import mprgp_gb300 as M
+def workload_qp(name, builder=None):
+    """The config's beam QP, from the library's generator or `builder` (the
+    oracle's, bitwise the same, for the CPU arm)."""
+    if builder is None:
+        import mprgp_gb300 as M
+        builder = M.beam
     a, b, c, extra, mode, E, nu, sig = WORKLOADS[name]
-    qp = M.beam(a, b, c, extra_planes_max=extra, extra_planes_min=extra, plane_mode=mode,
-                young=E, poisson=nu, v0_sigma=sig, seed=1)
-    return qp
+    return builder(a, b, c, extra_planes_max=extra, extra_planes_min=extra, plane_mode=mode,
+                   young=E, poisson=nu, v0_sigma=sig, seed=1)
 
 
 def workload_desc(name, qp):
@@ -449,10 +452,8 @@ def run_reference(args):
     world, rank, local = dist_env()
     if rank != 0:
         return
-    import mprgp_gb300 as M
-    M.build()
     threads = os.cpu_count() or 1
-    qp = workload_qp(args.config)
+    qp = workload_qp(args.config, builder=oracle_helpers().oracle_beam)
     for _ in range(args.warmup):
         cpu_baseline(qp, threads)
     times, st = [], None
@@ -768,31 +769,81 @@ def serve_desc(win):
             f"A/x/active set resident); tol 1e-8*||b|| each")
 
 
-def serve_sample(win, count):
-    """The first `count` new-scene requests of the window (CPU sample)."""
-    return [r.qp for r in win.reqs if not r.followup][:count]
+def serve_chains(win):
+    """The window's requests grouped by scene: each chain is a new scene
+    followed by its follow-up timesteps, in arrival order."""
+    chains = {}
+    for i, r in enumerate(win.reqs):
+        chains.setdefault(r.scene, []).append(i)
+    return [chains[s] for s in sorted(chains)]
 
 
-def cpu_solve_many(qps, threads):
-    """Solves independent QPs on `threads` host threads with the CPU
-    restatement of the reference (one single-threaded solve per thread)."""
-    from concurrent.futures import ThreadPoolExecutor
+def oracle_helpers():
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import helpers as H
+    return H
+
+
+def cpu_chain(win, chain, fb=None):
+    """Solves one scene chain with the CPU restatement of the reference MPRGP
+    the way MprgpFemSolver steps a scene: the new scene from P(x0), each
+    follow-up warm-started from the previous solution (no projection) and the
+    stored power-method vector (MprgpFemSolver.cpp:533 passes &power_ev).
+    Follow-up right-hand sides come from `fb` (request index -> b) when given,
+    else from this chain's own solutions (workloads.next_step_rhs).
+    Returns {request index: (x, stats)}."""
+    from mprgp_gb300 import workloads as W
+    H = oracle_helpers()
+    qp = win.reqs[chain[0]].qp
+    A, b, J, c = H.qp_from_beam(qp)
+    out = {}
+    ev, x_prev, v_prev, x_new, b_cur = None, qp.x0, np.zeros_like(qp.x0), None, b
+    for i in chain:
+        if win.reqs[i].followup:
+            if fb is not None:
+                b_next = fb[i]
+                v_new = (x_new - x_prev) / qp.params["dt"]
+            else:
+                b_next, v_new = W.next_step_rhs(qp, b_cur, x_prev, x_new, v_prev,
+                                                qp.params["dt"])
+            x_prev, v_prev, b_cur = x_new, v_new, b_next
+            start, proj = x_new, False
+        else:
+            start, proj = qp.x0, True
+        tol = REL_TOL * float(np.linalg.norm(b_cur))
+        x, _, st, ev = H.oracle_solve_warm("general", A, b_cur, start, J, c, ev=ev, tol=tol,
+                                           max_it=20000, seed=SEED, project_x0=proj)
+        out[i] = (x, st)
+        x_new = x
+    return out
+
+
+def cpu_chains(win, chains, threads, fb=None):
+    """Solves scene chains concurrently, one chain per host thread (each solve
+    single-threaded, as the reference's serial path), longest chains first.
+    Returns (seconds, {request index: (x, stats)})."""
+    from concurrent.futures import ThreadPoolExecutor
+    H = oracle_helpers()
     H.oracle().oracle_set_threads(1)
-    prepared = [H.qp_from_beam(q) + (q.x0,) for q in qps]
-
-    def one(args):
-        A, b, J, c, x0 = args
-        tol = REL_TOL * float(np.linalg.norm(b))
-        x, face, st, _ = H.oracle_solve("general", A, b, x0, J, c, tol=tol, max_it=20000,
-                                        seed=SEED)
-        return st
-
+    order = sorted(chains, key=lambda ch: -len(ch) * win.reqs[ch[0]].qp.nv)
+    out = {}
     t = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        sts = list(ex.map(one, prepared))
-    return time.perf_counter() - t, sts
+        for part in ex.map(lambda ch: cpu_chain(win, ch, fb), order):
+            out.update(part)
+    return time.perf_counter() - t, out
+
+
+def serve_config(win):
+    """The `config` both arms of the serving benchmark report (one dict, so
+    the two lines describe the same workload)."""
+    return {"workload": serve_desc(win), "config": "c4", "arrival_rate_hz": SERVE_RATE,
+            "requests": len(win.reqs), "seed": SERVE_SEED,
+            "l2": "GPU arm: flushed before every window (256 MB device write); CPU arm: the "
+                  "window's QPs (about 2 GB) exceed every host cache"}
+
+
+SERVE_REF_REQUESTS = 64    # requests per reference-arm step (whole scene chains)
 
 
 def run_serve(args):
@@ -826,7 +877,7 @@ def run_serve(args):
     # batched solve) measures batch throughput alone -- without the cluster
     # solver the small requests wait for the batched runs, about doubling
     # their median latency -- so only the remaining knobs are tuned.
-    tuning = autotune_ctx(args, ctx, serve_sample(win, 48), prec,
+    tuning = autotune_ctx(args, ctx, [r.qp for r in win.reqs if not r.followup][:48], prec,
                           fixed={"cluster": 16, "cluster_items": 1, "power": "step",
                                  "power_regs": 40, "engine": "persistent"})
     pl = StreamPlayer(ctx, win, rel_tol=REL_TOL, seed=SEED)
@@ -873,6 +924,18 @@ def run_serve(args):
             xs, xp = timed[0].xs[i], base.xs[i]
             errs.append(float(np.linalg.norm(xs - xp) / max(np.linalg.norm(xp), 1e-300)))
             same_face += int(np.array_equal(timed[0].faces[i], base.faces[i]))
+    # the served form in plain FP64 (same server, same stream): separates the
+    # gain of serving/batching from the gain of the mixed precision
+    served64 = None
+    if mixed and not args.no_plain:
+        r64 = [check(pl.play(SERVE_RATE, M.PREC_FP64, "device", flush=flush, stream=stream,
+                             **served), "served FP64") for _ in range(max(1, min(args.steps, 3)))]
+        ms64 = sum(r.event_ms for r in r64)
+        lat64 = np.concatenate([r.latency_s for r in r64]) * 1e3
+        served64 = {"value": round(n_req * len(r64) / (ms64 / 1e3), 3), "unit": "solves/s",
+                    "windows": len(r64),
+                    "p50_ms": round(float(np.percentile(lat64, 50)), 3),
+                    "p99_ms": round(float(np.percentile(lat64, 99)), 3)}
     # arrival-rate sweep (one window each)
     sweep = []
     for rate in (() if args.no_sweep else SERVE_SWEEP):
@@ -907,21 +970,19 @@ def run_serve(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 A (f32 accumulate) + f64 steps/projection/residual" if mixed else "f64",
         "data": "synthetic (seeded beam QPs, no dataset)",
-        "config": {"workload": serve_desc(win), "config": "c4",
-                   "form": "served-" + ("mixed" if mixed else "fp64"),
-                   "arrival_rate_hz": SERVE_RATE,
-                   "server": {"slots": served["max_slots"], "quantum_phases": served["quantum"],
-                              "power_loop_per_step": served["power_launches"],
-                              "small_instances": "cluster solver, to completion within a run",
-                              "lanes": {0: "one synchronous run per step",
-                                        2: "two asynchronous lanes (small, large)"}.get(
-                                  args.lanes, f"{args.lanes} asynchronous lanes (small, large, "
-                                              f"{args.lanes - 2} for the large requests' power "
-                                              f"method)")},
-                   "inputs": "staged in device memory before the timed region (e2e: pinned host)",
-                   "autotune": tuning,
-                   "l2": "flushed before every window (256 MB device write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": serve_config(win),
+        "setup": {"form": "served-" + ("mixed" if mixed else "fp64"),
+                  "server": {"slots": served["max_slots"], "quantum_phases": served["quantum"],
+                             "power_loop_per_step": served["power_launches"],
+                             "small_instances": "cluster solver, to completion within a run",
+                             "lanes": {0: "one synchronous run per step",
+                                       2: "two asynchronous lanes (small, large)"}.get(
+                                 args.lanes, f"{args.lanes} asynchronous lanes (small, large, "
+                                             f"{args.lanes - 2} for the large requests' power "
+                                             f"method)")},
+                  "inputs": "staged in device memory before the timed region (e2e: pinned host)",
+                  "autotune": tuning,
+                  "parallelism": "replicas" if world > 1 else "single GPU"},
         "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                        "p99": round(float(np.percentile(lat, 99)), 3)},
         "plain_fp64_one_at_a_time": None if base is None else {
@@ -929,6 +990,7 @@ def run_serve(args):
             "p50_ms": round(float(np.percentile(base.latency_s, 50)) * 1e3, 3),
             "p99_ms": round(float(np.percentile(base.latency_s, 99)) * 1e3, 3),
             "speedup_of_value": round(value / world / base.solves_per_s, 2)},
+        "served_fp64": served64,
         "error_vs_fp64": {"max_rel_x": float(max(errs)), "median_rel_x": float(np.median(errs)),
                           "identical_active_sets": same_face, "of": n_req},
         "sweep": sweep,
@@ -960,18 +1022,54 @@ def run_serve(args):
                        "path": "mprgp_server_submit (C ABI) by reference to pinned host buffers, "
                                "copied at admission; x and face read back at completion"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        qs, spent, sts = [], 0.0, []
-        for q in serve_sample(win, SERVE_CPU_SAMPLE):
-            dt, st = cpu_solve_many([q], 1)
+        # The oracle, single-threaded, on whole scene chains of the window
+        # (follow-ups with the served right-hand sides, so that both sides
+        # solve the same QPs), about 15 s of host time; its solutions are
+        # the served results' reference (error_vs_oracle).
+        spent, solved = 0.0, {}
+        for ch in serve_chains(win):
+            dt, part = cpu_chains(win, [ch], 1, fb=pl.fb)
             spent += dt
-            qs.append(q)
+            solved.update(part)
             if spent > 15.0:
                 break
+        nf = sum(win.reqs[i].followup for i in solved)
         line["cpu_baseline"] = {
-            "value": round(len(qs) / spent, 4), "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": f"the first {len(qs)} new-scene requests of the window, solved one after "
-                      f"another by the CPU restatement of the reference MPRGP (oracle/), "
-                      f"single-threaded; {spent:.1f} s"}
+            "value": round(len(solved) / spent, 4), "unit": "solves/s", "cores": 1,
+            "kind": "port",
+            "sample": f"whole scene chains from the start of the window: {len(solved)} requests "
+                      f"({nf} follow-up timesteps warm-started from the previous solution and "
+                      f"power vector), solved one after another by the CPU restatement of the "
+                      f"reference MPRGP (oracle/), single-threaded; {spent:.1f} s"}
+        line["error_vs_oracle"] = oracle_errors(win, solved, timed[0])
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def oracle_errors(win, solved, served):
+    """Served x and active sets against the oracle's FP64 solutions of the same
+    requests: ||x - x_oracle|| / ||x_oracle|| and DECIDE_FACE of both."""
+    from mprgp_gb300 import planes_to_J
+    H = oracle_helpers()
+    scene_qp = {r.scene: r.qp for r in win.reqs if not r.followup}
+    errs, same, kkt = [], 0, []
+    for i, (xo, st) in sorted(solved.items()):
+        qp = scene_qp[win.reqs[i].scene]
+        jptr, jidx, jval, c = planes_to_J(qp.nv, qp.plane_ptr, qp.planes)
+        J = H.Csr(jptr, jidx, jval, len(c), qp.n)
+        xs = served.xs[i]
+        errs.append(float(np.linalg.norm(xs - xo) / max(np.linalg.norm(xo), 1e-300)))
+        same += int(np.array_equal(H.decide_face_planes(J, c, xs), H.decide_face_planes(J, c, xo)))
+        kkt.append(int(st["code"]) == 0)
+    return {"max_rel_x": max(errs), "median_rel_x": float(np.median(errs)),
+            "identical_active_sets": same, "of": len(errs), "oracle_converged": int(sum(kkt)),
+            "requests": "the cpu_baseline sample; served mixed form at 1e-8||b|| vs the oracle "
+                        "(reference MPRGP restatement, FP64) at 1e-8||b||"}
+
+
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -980,26 +1078,47 @@ def run_serve(args):
 
 
 def run_reference_serve(args):
-    """Reference arm of c4: the CPU restatement of the reference MPRGP solving
-    a bounded sample of the stream's requests on every host core (independent
-    requests, one single-threaded solve per core)."""
+    """Reference arm of c4: the CPU restatement of the reference MPRGP serving
+    the same window on every host core.  The window's beams come from the
+    oracle's generator (bitwise the library's; the GPU library is not
+    loaded).  A scene chain -- a new scene and its follow-up timesteps, each
+    warm-started from the previous solution and power vector, its right-hand
+    side from that solution -- runs on one thread; chains run concurrently.
+    Each step solves the next whole chains of the window, in rotation, until
+    it holds SERVE_REF_REQUESTS requests, so that --steps K --warmup W
+    covers the window in a few minutes."""
     world, rank, local = dist_env()
     if rank != 0:
         return
-    import mprgp_gb300 as M
     from mprgp_gb300 import workloads as W
-    M.build()
-    win = W.serving_window(SERVE_COUNT, SERVE_SEED)
-    sample = serve_sample(win, SERVE_CPU_SAMPLE)
+    H = oracle_helpers()
+    win = W.serving_window(SERVE_COUNT, SERVE_SEED, builder=H.oracle_beam)
+    chains = serve_chains(win)
     threads = os.cpu_count() or 1
+    cursor = 0
+
+    def next_sample():
+        nonlocal cursor
+        out, n = [], 0
+        while n < SERVE_REF_REQUESTS:
+            ch = chains[cursor % len(chains)]
+            cursor += 1
+            out.append(ch)
+            n += len(ch)
+        return out
+
     for _ in range(args.warmup):
-        cpu_solve_many(sample, threads)
-    times, last = [], None
+        cpu_chains(win, next_sample(), threads)
+    times, counts, conv, nfol = [], [], 0, 0
     for _ in range(args.steps):
-        dt, last = cpu_solve_many(sample, threads)
+        sample = next_sample()
+        dt, out = cpu_chains(win, sample, threads)
         times.append(dt)
+        counts.append(len(out))
+        conv += sum(int(st["code"]) == 0 for _, st in out.values())
+        nfol += sum(win.reqs[i].followup for i in out)
     total = sum(times)
-    v = len(sample) * args.steps / total
+    v = sum(counts) / total
     line = {
         "impl": "reference",
         "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
@@ -1007,15 +1126,18 @@ def run_reference_serve(args):
         "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded beam QPs, no dataset)",
-        "config": {"workload": serve_desc(win), "config": "c4", "form": "reference-cpu"},
+        "config": serve_config(win),
         "cpu_baseline": {"value": round(v, 4), "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: the first {len(sample)} new-scene requests of the "
-                                   f"window, solved concurrently on {threads} host threads by the "
-                                   f"CPU restatement of the reference MPRGP (oracle/), one "
-                                   f"single-threaded solve per thread"},
+                         "sample": f"each step: the next whole scene chains of the same window "
+                                   f"in rotation ({sum(counts)} requests over {args.steps} steps, "
+                                   f"{nfol} of them follow-up timesteps warm-started from the "
+                                   f"previous solution and power vector), chains concurrently on "
+                                   f"{threads} host threads, each solve single-threaded, by the "
+                                   f"CPU restatement of the reference MPRGP (oracle/)"},
         "e2e": {"value": round(v, 4), "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "solve": {"converged": sum(int(s["code"]) == 0 for s in last), "of": len(last)},
+        "gpu_launches": 0,
+        "solve": {"converged": conv, "of": sum(counts)},
     }
     print(json.dumps(line))
 

@@ -112,6 +112,11 @@ void *mprgp_context_stream(mprgp_context *ctx); /* the cudaStream_t it launches 
 int mprgp_context_sync(mprgp_context *ctx);
 /* SM count and resident engine CTAs per SM (the persistent grid's shape). */
 int mprgp_context_info(mprgp_context *ctx, int *nsm, int *blocks_per_sm);
+/* No counterpart in the reference.  Device bytes that new problems of the
+ * context can take now: the device's free memory (cudaMemGetInfo, so other
+ * users of the GPU count) plus the blocks the context's memory pool holds
+ * but no problem uses.  The server's admission reads the same figure. */
+int mprgp_context_room(mprgp_context *ctx, size_t *bytes);
 /* Counters since the context was created: kernels launched (engine runs,
  * cluster-solver launches, setup kernels and every iteration of the
  * power-method graph loop), the device time of the solver runs (power loop,
@@ -220,18 +225,21 @@ int mprgp_solve_bsr(mprgp_context *ctx, int nv, int nnzb, const int *row_ptr, co
 
 /* ---- solve without allocating device memory ------------------------------ */
 /* No counterpart in the reference.  For callers that cannot call cudaMalloc
- * while they solve (a simulation step recorded into a CUDA graph and
- * replayed, a real-time loop kept off the allocator, a host under a fixed
- * GPU memory budget).  Every pointer is a device pointer the caller owns:
+ * while they solve (a real-time loop kept off the allocator, which can
+ * synchronize the device; a plug-in inside a host program that owns all
+ * device memory; a host under a fixed GPU memory quota).  Every pointer is
+ * a device pointer the caller owns:
  * A as 3x3-block CSR, b, the per-vertex planes (n, p) with n.x + p >= 0, x
  * (solved in place) and optionally face (one byte per plane row).  The
  * solver's working memory lives in one 64 MiB file-scope device array that
  * every GPU loading the library holds until exit; problems that do not fit
  * (about 37k vertices in FP64) are rejected with MPRGP_INVALID.  The first
  * call on a device looks up that array's address (one-time set-up; make it
- * before any stream capture).  All calls share the array: calls whose GPU
- * work overlaps race and must be serialized.  Kinds DECOUPLED and PLANES,
- * monotone algorithm, FP64 or MIXED; no stored power vector (use_ev = 0). */
+ * before any stream capture; the address is kept, so a device reset after
+ * it is not supported).  All calls share the array: calls whose GPU work
+ * overlaps race and must be serialized.  On an error status x and face are
+ * left unchanged.  Kinds DECOUPLED and PLANES, monotone algorithm, FP64 or
+ * MIXED; no stored power vector (use_ev = 0). */
 int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *row_ptr, const int *cols,
                         const double *vals, const double *b, const int *plane_ptr,
                         const double *planes, const mprgp_options *opt, double *x,
@@ -301,6 +309,12 @@ typedef struct mprgp_server_config {
                          2, plus lanes - 2 lanes that run the large requests'
                          power method (power_launches per run; they share one
                          queue) before they join the large lane */
+  size_t hbm_reserve; /* device bytes admission leaves free for other users of
+                         the GPU: a new scene is admitted only while the
+                         device's free memory (re-read at admission, plus the
+                         context pool's unused blocks) stays above this after
+                         it; otherwise it waits, and completes with MPRGP_OOM
+                         if nothing else is in flight (0 = none) */
 } mprgp_server_config;
 typedef struct mprgp_server mprgp_server;
 int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprgp_server **out);

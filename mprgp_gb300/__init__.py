@@ -51,7 +51,8 @@ class Stats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget", C.c_size_t), ("max_slots", C.c_int), ("quantum_phases", C.c_int),
-                ("power_launches", C.c_int), ("cluster_quantum", C.c_int), ("lanes", C.c_int)]
+                ("power_launches", C.c_int), ("cluster_quantum", C.c_int), ("lanes", C.c_int),
+                ("hbm_reserve", C.c_size_t)]
 
 
 class BeamParams(C.Structure):
@@ -117,6 +118,7 @@ def _sig(lib):
       C.c_double, C.c_int, C.c_double, C.POINTER(IcaStats))
     s("mprgp_server_create", C.c_int, _P, C.POINTER(ServerConfig), C.POINTER(_P))
     s("mprgp_server_destroy", C.c_int, _P)
+    s("mprgp_context_room", C.c_int, _P, C.POINTER(C.c_size_t))
     s("mprgp_server_submit", C.c_int, _P, C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P,
       C.c_int, C.c_int, C.POINTER(Options), C.POINTER(C.c_longlong))
     s("mprgp_server_step", C.c_int, _P, _IP, _IP, _IP)
@@ -347,6 +349,12 @@ class Context:
         """Items per CTA allowed in the largest cluster (1..4)."""
         _check(lib().mprgp_context_set_cluster_items(self.h, items), "set_cluster_items")
 
+    def room(self) -> int:
+        """Device bytes new problems of this context can take now."""
+        b = C.c_size_t()
+        _check(lib().mprgp_context_room(self.h, C.byref(b)), "context_room")
+        return b.value
+
     def set_tuning(self, stage: int = 0, ctas_per_sm: int = 0):
         _check(lib().mprgp_context_set_tuning(self.h, stage, ctas_per_sm), "set_tuning")
 
@@ -529,10 +537,10 @@ class Server:
     """Continuous-batching QP server (mprgp_server_*)."""
 
     def __init__(self, ctx: Context, hbm_budget=0, max_slots=0, quantum_phases=0,
-                 power_launches=256, cluster_quantum=0, lanes=0):
+                 power_launches=256, cluster_quantum=0, lanes=0, hbm_reserve=0):
         self.ctx = ctx
         cfg = ServerConfig(hbm_budget, max_slots, quantum_phases, power_launches, cluster_quantum,
-                           lanes)
+                           lanes, hbm_reserve)
         self.h = C.c_void_p()
         _check(lib().mprgp_server_create(ctx.h, C.byref(cfg), C.byref(self.h)), "server_create")
         self.nv = {}

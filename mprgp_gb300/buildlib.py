@@ -23,8 +23,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["engine.cu", "capi.cu", "noalloc.cu", "server.cu", "fem.cu", "planes.cu", "ica.cu",
            "beam.cpp"]
 # ica.cu reproduces a CPU restatement operation for operation: no contraction
-# of products and sums into fused multiply-adds there.
-FILE_FLAGS = {"ica.cu": ["-fmad=false"]}
+# of products and sums into fused multiply-adds there.  beam.cpp's host
+# arithmetic is rounded as written on every host (GCC contracts to FMA by
+# default where the host ISA has one), so the beam QPs are the same bits on
+# x86_64 and aarch64.
+FILE_FLAGS = {"ica.cu": ["-fmad=false"], "beam.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:
@@ -44,7 +47,7 @@ def _compile(src: str, ptxas_verbose: bool) -> str:
         if ptxas_verbose:
             cmd += ["-Xptxas", "-v"]
     else:
-        cmd += ["-x", "c++"]
+        cmd += ["-x", "c++"] + FILE_FLAGS.get(src, [])
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")

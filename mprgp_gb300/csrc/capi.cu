@@ -629,6 +629,21 @@ bool other_lanes_active(const mprgp_context *c, int k) {
 
 namespace mprgp {
 
+// Device bytes a new allocation of the context can use now: the device's
+// free memory plus what the context's pool holds reserved but unused (the
+// pool keeps freed blocks for reuse instead of returning them).
+int context_room(mprgp_context *c, size_t *room) {
+  size_t fr = 0, tot = 0;
+  cudaError_t e = cudaMemGetInfo(&fr, &tot);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
+  unsigned long long reserved = 0, used = 0;  // the pool attributes are 64-bit
+  e = cudaMemPoolGetAttribute(c->pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+  if (e == cudaSuccess) e = cudaMemPoolGetAttribute(c->pool, cudaMemPoolAttrUsedMemCurrent, &used);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemPoolGetAttribute");
+  *room = fr + (size_t)(reserved > used ? reserved - used : 0);
+  return MPRGP_OK;
+}
+
 // Whether any asynchronous lane of the context has a run in flight.
 int context_lanes_busy(const mprgp_context *c) {
   return other_lanes_active(c, 0) ? 1 : 0;
@@ -1192,6 +1207,11 @@ int mprgp_context_info(mprgp_context *c, int *nsm, int *blocks_per_sm) {
   if (nsm) *nsm = c->nsm;
   if (blocks_per_sm) *blocks_per_sm = c->bps;
   return MPRGP_OK;
+}
+
+int mprgp_context_room(mprgp_context *c, size_t *bytes) {
+  if (!c || !bytes) return fail(MPRGP_INVALID, "context_room");
+  return mprgp::context_room(c, bytes);
 }
 
 size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {

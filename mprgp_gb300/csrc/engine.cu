@@ -1390,6 +1390,11 @@ __device__ void outer_top(const InstDesc &D, InstState &S, const double *s) {
   S.active = (int)s[4];
   if (S.iteration >= D.max_it) { go_final(D, S); return; }
   S.residual = sqrt(s[0]);
+  if (S.residual != S.residual) {  // NaN: A, b or x carry a NaN; no step can converge
+    S.code = -2;                   // MPRGP_BREAKDOWN
+    S.phase = PH_DONE;
+    return;
+  }
   if (S.residual <= D.tol) {
     if (D.alg == ALG_PLAIN) S.iters_out = S.iteration;
     go_final(D, S);

@@ -1,9 +1,10 @@
 // mprgp_solve_noalloc: a plane-constrained MPRGP solve that allocates nothing.
 //
-// Some callers cannot call cudaMalloc while they solve: a simulation step
-// recorded once into a CUDA graph and replayed, a real-time control loop
-// that must not touch the allocator, or a host that shares the GPU under a
-// fixed memory budget.  This entry point takes every input and output as a
+// Some callers cannot call cudaMalloc while they solve: a real-time control
+// loop that must not enter the allocator (an allocation can synchronize the
+// device and take unbounded time), a plug-in living inside a host program
+// that owns and budgets all device memory itself, or a host that shares the
+// GPU under a fixed memory quota.  This entry point takes every input and output as a
 // device pointer the caller already owns and runs the same persistent engine
 // as mprgp_problem_solve, with all of its working memory (the SELL copy of
 // A, the solver vectors, the per-item partial sums, the state and the grid
@@ -17,7 +18,11 @@
 //   * The first call on a device does a one-time set-up on that device: it
 //     looks up the array's device address (cudaGetSymbolAddress) and the
 //     resident size of the engine grid.  Make that first call before any
-//     stream capture.
+//     stream capture.  The address is kept for the life of the process, so
+//     resetting the device (cudaDeviceReset) after the first call is not
+//     supported.
+//   * On an error (MPRGP_TIMEOUT, MPRGP_BREAKDOWN, ...) x and face are left
+//     as the caller passed them, as mprgp_solve_bsr does.
 //   * Every call shares the one array and leaves its contents behind; the
 //     call clears what must start at zero.  Calls whose GPU work overlaps --
 //     on different streams, or from different host threads -- race on the
@@ -313,10 +318,12 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (c1.err) out.code = c1.err;
   else if (out.phase != PH_DONE) out.code = MPRGP_TIMEOUT;
-  NCK(cudaMemcpyAsync(x, d_vec + (size_t)(B_X0 + out.xc) * n, sizeof(double) * n,
-                      cudaMemcpyDeviceToDevice, s));
-  if (face && m > 0) NCK(cudaMemcpyAsync(face, d_face, m, cudaMemcpyDeviceToDevice, s));
-  NCK(cudaStreamSynchronize(s));
+  if (out.code >= MPRGP_NOT_CONVERGED) {  // results only for a finished solve
+    NCK(cudaMemcpyAsync(x, d_vec + (size_t)(B_X0 + out.xc) * n, sizeof(double) * n,
+                        cudaMemcpyDeviceToDevice, s));
+    if (face && m > 0) NCK(cudaMemcpyAsync(face, d_face, m, cudaMemcpyDeviceToDevice, s));
+    NCK(cudaStreamSynchronize(s));
+  }
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     stats->code = out.code;
@@ -334,6 +341,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
     stats->spmv_fp32 = out.spmv32;
     stats->phases = out.phases;
     stats->device_ms = ms;
+    stats->power_passes = out.pow_spmv;
   }
   if (c1.err) return err(c1.err, "solve_noalloc: device wait limit reached");
   return out.code;

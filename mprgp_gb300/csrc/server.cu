@@ -38,6 +38,7 @@ int engine_begin(mprgp_context *c, int lane, int n, mprgp_problem *const *probs,
 int engine_ready(mprgp_context *c, int lane);
 int engine_end(mprgp_context *c, int lane, mprgp_stats *stats, int *done);
 int engine_lane_of(const mprgp_context *c, int nv);
+int context_room(mprgp_context *c, size_t *room);
 int engine_needs_power(const mprgp_problem *p, const mprgp_options *o);
 int engine_in_power(const mprgp_problem *p);
 void set_last_error(const char *what);
@@ -94,6 +95,7 @@ int err(int code, const char *what) {
 struct mprgp_server {
   mprgp_context *ctx = nullptr;
   size_t budget = 0, used = 0;
+  size_t reserve = 0;  // device bytes admission leaves free for other users
   int max_slots = 64, quantum = 256, power_launches = 256, cluster_quantum = 0;
   long long next_ticket = 1, clock = 0;
   std::deque<long long> queue;
@@ -132,6 +134,43 @@ bool make_room(mprgp_server *s, size_t need) {
     release_scene(s, victim);
   }
   return true;
+}
+
+// Device room for new scenes, read once per admission pass (lazily) and
+// tracked as scenes are admitted or evicted within it.
+struct Room {
+  bool known = false;
+  size_t bytes = 0;
+};
+
+// Whether a new scene of `need` bytes leaves the server's reserve free on the
+// device.  The device's free memory is re-read (other users of the GPU
+// allocate too), and idle scenes are evicted, least recently used first,
+// while it does not fit (their memory returns to the context's pool, which
+// counts as room).
+int device_fits(mprgp_server *s, Room &room, size_t need, bool *fits) {
+  for (;;) {
+    if (!room.known) {
+      const int rc = mprgp::context_room(s->ctx, &room.bytes);
+      if (rc) return rc;
+      room.known = true;
+    }
+    if (room.bytes >= need && room.bytes - need >= s->reserve) {
+      *fits = true;
+      return MPRGP_OK;
+    }
+    auto victim = s->scenes.end();
+    for (auto it = s->scenes.begin(); it != s->scenes.end(); ++it)
+      if (!it->second.busy && (victim == s->scenes.end() ||
+                               it->second.last_use < victim->second.last_use))
+        victim = it;
+    if (victim == s->scenes.end()) {
+      *fits = false;
+      return MPRGP_OK;
+    }
+    release_scene(s, victim);
+    room.known = false;
+  }
 }
 
 int admit(mprgp_server *s, Request &r) {
@@ -192,8 +231,11 @@ int in_flight(const mprgp_server *s) {
   return k;
 }
 
-// Admission: FIFO, skipping requests that do not fit yet.
+// Admission: FIFO, skipping requests that do not fit yet.  A new scene that
+// does not fit while nothing else is in flight can never fit: it completes
+// with MPRGP_OOM.
 void admit_queued(mprgp_server *s) {
+  Room room;
   for (auto it = s->queue.begin(); it != s->queue.end();) {
     if (in_flight(s) >= s->max_slots) break;
     Request &r = s->reqs[*it];
@@ -203,6 +245,7 @@ void admit_queued(mprgp_server *s) {
       if (sc == s->scenes.end()) {  // evicted meanwhile: cannot warm start
         r.state = 2;
         r.code = MPRGP_INVALID;
+        r.stats.code = r.code;
         s->completed.push_back(r.ticket);
         it = s->queue.erase(it);
         continue;
@@ -213,15 +256,35 @@ void admit_queued(mprgp_server *s) {
       const size_t bytes = mprgp_problem_bytes(r.nv, r.nnzb, r.m, prec);
       auto sc = s->scenes.find(r.scene);
       ok = (sc == s->scenes.end() || !sc->second.busy) && make_room(s, bytes);
+      if (ok) {
+        const int rc = device_fits(s, room, bytes, &ok);
+        if (rc == MPRGP_OK && !ok && in_flight(s) == 0) {
+          mprgp::set_last_error("server: a new scene does not fit in the device's free memory");
+          r.state = 2;
+          r.code = MPRGP_OOM;
+          r.stats.code = r.code;
+          s->completed.push_back(r.ticket);
+          it = s->queue.erase(it);
+          continue;
+        }
+        ok = ok && rc == MPRGP_OK;
+      }
     }
     if (!ok) {
       ++it;
       continue;
     }
     const int rc = admit(s, r);
+    if (rc == MPRGP_OOM && in_flight(s) > 0) {  // an allocation failed: retry later
+      room.known = false;
+      ++it;
+      continue;
+    }
+    if (!r.followup) room.known = false;  // the new scene took device memory
     if (rc) {
       r.state = 2;
       r.code = rc;
+      r.stats.code = r.code;
       s->completed.push_back(r.ticket);
       it = s->queue.erase(it);
       continue;
@@ -407,6 +470,7 @@ int mprgp_server_create(mprgp_context *ctx, const mprgp_server_config *cfg, mprg
   size_t fr = 0, tot = 0;
   cudaMemGetInfo(&fr, &tot);
   s->budget = (cfg && cfg->hbm_budget) ? cfg->hbm_budget : (size_t)(0.8 * (double)fr);
+  s->reserve = cfg ? cfg->hbm_reserve : 0;
   if (cfg && cfg->max_slots > 0) s->max_slots = cfg->max_slots;
   if (cfg && cfg->quantum_phases > 0) s->quantum = cfg->quantum_phases;
   if (cfg && cfg->quantum_phases < 0) s->quantum = 0;  // each step runs to completion

@@ -79,10 +79,13 @@ class Window:
 
 
 def serving_window(count=128, seed=7, followup_frac=0.3, lo=(4, 4, 4), hi=(32, 32, 64),
-                   v0_sigma=0.2) -> Window:
+                   v0_sigma=0.2, builder=None) -> Window:
     """`count` requests of the serving stream with Poisson arrival gaps: beams
     log-uniform from lo to hi cubes, floor plus 0-2 walls (1-3 planes per
-    vertex), 30 % follow-up timesteps of an earlier scene of the window."""
+    vertex), 30 % follow-up timesteps of an earlier scene of the window.
+    `builder(a, b, c, **kw)` makes each beam (default: the library's
+    generator, mprgp_beam_build)."""
+    build = beam if builder is None else builder
     rng = np.random.default_rng(seed)
     t, reqs, times, scenes = 0.0, [], [], 0
     while len(reqs) < count:
@@ -93,8 +96,8 @@ def serving_window(count=128, seed=7, followup_frac=0.3, lo=(4, 4, 4), hi=(32, 3
             continue
         dims = tuple(log_uniform_int(rng, l, h) for l, h in zip(lo, hi))
         extra = int(rng.integers(0, 3))
-        qp = beam(*dims, extra_planes_max=extra, extra_planes_min=extra, plane_mode=2,
-                  v0_sigma=v0_sigma, seed=int(rng.integers(1, 2**31)))
+        qp = build(*dims, extra_planes_max=extra, extra_planes_min=extra, plane_mode=2,
+                   v0_sigma=v0_sigma, seed=int(rng.integers(1, 2**31)))
         reqs.append(Request(t, qp, scenes, extra={"dims": dims, "walls": extra}))
         scenes += 1
     return Window(reqs, np.asarray(times))

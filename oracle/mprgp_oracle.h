@@ -723,6 +723,7 @@ class MPRGPBase {
   }
   void initialize(const Vec &result) {  // :148-162
     gradient(result);
+    g_exact = true;
     projector.DECIDE_FACE(result);
     projector.PHI(g, phi);
     precond.solve(g, z, phi);
@@ -782,6 +783,9 @@ class MPRGPBase {
     Vec &xTmp = beta;
     xTmp = result;
     projector.project(xTmp, result);
+    // The recursive update below is A x - B in exact arithmetic only when the
+    // projection moved nothing.
+    g_exact = (xTmp == result);
     for (size_t i = 0; i < g.size(); ++i) g[i] -= alpha_cg * AD[i];
     projector.DECIDE_FACE(result);
     projector.PHI(g, phi);
@@ -801,12 +805,85 @@ class MPRGPBase {
     for (size_t i = 0; i < y.size(); ++i) y[i] -= alpha_bar * phi[i];
     projector.project(y, result);
     gradient(result);
+    g_exact = true;
     projector.DECIDE_FACE(result);
     projector.PHI(g, phi);
     precond.solve(g, z, phi);
     p = z;
   }
+  // f(P(y)) - f(x) for y = x - alpha p, from scalars (the scalar_test switch):
+  //   f(y) - f(x)    = -alpha p.(A x - B) + alpha^2/2 p^T A p,
+  //   f(P(y)) - f(y) = d.(A y - B) + d^T A d / 2,   d = P(y) - y,
+  // where A x - B = g + e (e = 0 unless g is a recursive update that left
+  // A x - B, see g_exact) and A y - B = g - alpha A p + e.  Writes y.
+  // Returns f(y) - f(x) and sets corr = f(P(y)) - f(y).
+  double scalar_decrease(const Vec &result, double alpha, double pd, const Vec &AP, const Vec *e,
+                         double &corr) {
+    const size_t n = result.size();
+    y.resize(n);
+    for (size_t i = 0; i < n; ++i) y[i] = result[i] - alpha * p[i];
+    double pg = dot(p, g);
+    if (e) pg += dot(p, *e);
+    const double dfy = -alpha * pg + 0.5 * alpha * alpha * pd;
+    projector.project(y, tempx);
+    Vec d(n), gy(n);
+    bool moved = false;
+    for (size_t i = 0; i < n; ++i) {
+      d[i] = tempx[i] - y[i];
+      gy[i] = g[i] - alpha * AP[i] + (e ? (*e)[i] : 0.0);
+      moved = moved || d[i] != 0.0;
+    }
+    corr = 0.0;
+    if (moved) {
+      Vec Ad;
+      mul(d, Ad);
+      corr = dot(d, gy) + 0.5 * dot(d, Ad);
+    }
+    return dfy;
+  }
+  // CGMonotonicStep with the decrease test from scalars.  Same iterates and
+  // control flow as the reference loop below; only "fy <= fx" is evaluated
+  // as (f(P(y)) - f(x)) <= 0 without forming either function value.
+  double CGMonotonicStepScalar(Vec &result, bool &result_is_prop) {
+    Vec &AP = gp;
+    Vec e;
+    const Vec *ep = nullptr;
+    if (!g_exact) {  // e = (A x - B) - g, constant along the CG run
+      mul(result, e);
+      for (size_t i = 0; i < e.size(); ++i) e[i] = (e[i] - B[i]) - g[i];
+      ep = &e;
+    }
+    mul(p, AP);
+    double pd = dot(p, AP);
+    double alpha_cg = dot(z, g) / pd;
+    double corr = 0.0, fx_off = 0.0;
+    double dec = scalar_decrease(result, alpha_cg, pd, AP, ep, corr) + corr;
+    result_is_prop = true;
+    while (result_is_prop && residual_out > tolerance_factor && dec <= 0.0 &&
+           iteration < (int)max_iterations) {
+      result = y;
+      fx_off = -corr;  // f(x) is now f(P(y)) while x is y
+      for (size_t i = 0; i < g.size(); ++i) g[i] -= alpha_cg * AP[i];
+      projector.PHI(g, phi);
+      precond.solve(g, z, phi);
+      const double b = dot(z, AP) / dot(p, AP);
+      for (size_t i = 0; i < p.size(); ++i) p[i] = z[i] - b * p[i];
+      residual_out = computeGradients(g, false);
+      result_is_prop = proportional(result);
+      mul(p, AP);
+      pd = dot(p, AP);
+      alpha_cg = dot(z, g) / pd;
+      const double committed = dec;
+      dec = scalar_decrease(result, alpha_cg, pd, AP, ep, corr) + corr + fx_off;
+      ++num_cg;
+      ++iteration;
+      rec(1, committed);
+    }
+    rec(2, dec);
+    return residual_out;
+  }
   double CGMonotonicStep(Vec &result, bool &result_is_prop) {  // :272-316
+    if (scalar_test) return CGMonotonicStepScalar(result, result_is_prop);
     Vec &AP = gp;
     mul(p, AP);
     double pd = dot(p, AP);
@@ -855,8 +932,15 @@ class MPRGPBase {
   int num_cg = 0, num_exp = 0, numprop = 0, iteration = 0;
   int power_iters = 0, spmv = 0;
 
+  bool g_exact = true;  // g equals A x - B in exact arithmetic
+
  public:
   Trace *trace = nullptr;
+  // Not the reference: evaluate CGMonotonicStep's test f(P(y)) <= f(x)
+  // (MPRGPSolver.h:289, 305-309) from scalars, as the GPU solver does,
+  // instead of comparing two separately rounded function values.  Off by
+  // default; tests switch it on to show that the GPU takes the same steps.
+  bool scalar_test = false;
 
  protected:
   void rec(int ev, double val) {

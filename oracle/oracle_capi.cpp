@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstring>
 
+#include "beam_oracle.h"
 #include "ica_oracle.h"
 #include "mprgp_oracle.h"
 
@@ -48,10 +49,12 @@ void copy_face(const std::vector<char> &f, unsigned char *out) {
 }
 
 Trace *g_trace = nullptr;  // set by oracle_set_trace (test diagnostics)
+bool g_scalar_test = false;  // set by oracle_set_scalar_test
 
 template <typename SOLVER>
 int run(SOLVER &solver, Vec &x, double *stats) {
   solver.trace = g_trace;
+  solver.scalar_test = g_scalar_test;
   const int code = solver.solve(x);
   write_stats(solver.stats(), stats);
   return code;
@@ -73,22 +76,15 @@ extern "C" {
 // kind's projector and preconditioner instead of MPRGPMonotonic.
 // stats (10 doubles): code, iterations, cg, exp, prop, power iters, residual,
 // alpha_bar, spectral radius, SpMV count.
-int oracle_solve(int kind, int preconditioned, int n, const int *a_ptr, const int *a_idx,
-                 const double *a_val, const double *b, int m, const int *j_ptr,
-                 const int *j_idx, const double *j_val, const double *c, const double *L,
-                 const double *U, double tol, int max_it, uint64_t seed, double *ev,
-                 int ev_len, int project_x0, double *x, unsigned char *face_out,
-                 double *stats) {
+static int solve_impl(int kind, int preconditioned, int n, const int *a_ptr, const int *a_idx,
+                      const double *a_val, const double *b, int m, const int *j_ptr,
+                      const int *j_idx, const double *j_val, const double *c, const double *L,
+                      const double *U, double tol, int max_it, uint64_t seed, Vec *evp,
+                      int project_x0, double *x, unsigned char *face_out, double *stats) {
   const Csr Am = make_csr(n, n, a_ptr, a_idx, a_val);
   const FixedSparseMatrix FA(Am);
   const Vec B(b, b + n);
   Vec X(x, x + n);
-  Vec EV;
-  Vec *evp = nullptr;
-  if (ev) {
-    EV.assign(ev, ev + ev_len);
-    evp = &EV;
-  }
   int code = -100;
   const bool plain = kind >= 10;  // kind + 10: plain MPRGP::solve with that projector
   if (plain) kind -= 10;
@@ -183,11 +179,55 @@ int oracle_solve(int kind, int preconditioned, int n, const int *a_ptr, const in
     }
   }
   std::memcpy(x, X.data(), sizeof(double) * n);
+  return code;
+}
+
+int oracle_solve(int kind, int preconditioned, int n, const int *a_ptr, const int *a_idx,
+                 const double *a_val, const double *b, int m, const int *j_ptr,
+                 const int *j_idx, const double *j_val, const double *c, const double *L,
+                 const double *U, double tol, int max_it, uint64_t seed, double *ev,
+                 int ev_len, int project_x0, double *x, unsigned char *face_out,
+                 double *stats) {
+  Vec EV;
+  Vec *evp = nullptr;
+  if (ev) {
+    EV.assign(ev, ev + ev_len);
+    evp = &EV;
+  }
+  const int code = solve_impl(kind, preconditioned, n, a_ptr, a_idx, a_val, b, m, j_ptr, j_idx,
+                              j_val, c, L, U, tol, max_it, seed, evp, project_x0, x, face_out,
+                              stats);
   if (ev && evp) {
     for (int i = 0; i < ev_len && i < (int)EV.size(); ++i) ev[i] = EV[i];
   }
   return code;
 }
+
+// The same solve with the power-method warm start of MprgpFemSolver
+// (MprgpFemSolver.h:138, .cpp:533 pass &power_ev across frames): ev holds n
+// doubles; *ev_valid = 1 on entry starts specRad from ev (else from the
+// seeded random vector), and on return *ev_valid = 1 when ev holds a stored
+// vector -- the one given, or the iterate specRad stored when it stopped
+// early (MPRGPSolver.h:62-74).
+int oracle_solve_warm(int kind, int n, const int *a_ptr, const int *a_idx, const double *a_val,
+                      const double *b, int m, const int *j_ptr, const int *j_idx,
+                      const double *j_val, const double *c, double tol, int max_it,
+                      uint64_t seed, double *ev, int *ev_valid, int project_x0, double *x,
+                      unsigned char *face_out, double *stats) {
+  Vec EV;
+  if (*ev_valid) EV.assign(ev, ev + n);
+  const int code = solve_impl(kind, 1, n, a_ptr, a_idx, a_val, b, m, j_ptr, j_idx, j_val, c,
+                              nullptr, nullptr, tol, max_it, seed, &EV, project_x0, x, face_out,
+                              stats);
+  *ev_valid = (int)EV.size() == n ? 1 : 0;
+  if (*ev_valid) std::memcpy(ev, EV.data(), sizeof(double) * n);
+  return code;
+}
+
+// Switches the monotone solvers' CG decrease test between the reference's
+// comparison of two function values (0, the default) and the scalar form
+// the GPU solver evaluates (1).  Applies to the solves that follow.
+void oracle_set_scalar_test(int on) { g_scalar_test = on != 0; }
 
 // Projector primitives, one call per operation, for the projector property
 // tests (test_case/MPRGPTest.cpp:11-68).  op: 0 project(x)->out,
@@ -291,6 +331,45 @@ int oracle_ica_solve(int nv, const int *row_ptr, const int *cols, const double *
     stats[3] = (double)st.pgs_sweeps;
   }
   return st.converged ? 0 : -1;
+}
+
+// The synthetic beam QP (beam_oracle.h).  ip = {a, b, c, planes_max,
+// planes_min, mode, facet_layers}; dp = {edge, young, poisson, rho, dt,
+// gravity, lift, v0_sigma, active_frac, band, max_tilt}.  Returns a handle
+// (NULL for an invalid spec) and the sizes; oracle_beam_take copies the
+// arrays out (row_ptr nv+1, cols nnzb, vals 9 nnzb, b and x0 3 nv,
+// plane_ptr nv+1, planes 4 m) and frees the handle.
+void *oracle_beam_new(const int *ip, const double *dp, uint64_t seed, int *nv, int *nnzb,
+                      int *nplanes) {
+  BeamSpec s;
+  s.a = ip[0]; s.b = ip[1]; s.c = ip[2];
+  s.planes_max = ip[3]; s.planes_min = ip[4]; s.mode = ip[5]; s.facet_layers = ip[6];
+  s.edge = dp[0]; s.young = dp[1]; s.poisson = dp[2]; s.rho = dp[3]; s.dt = dp[4];
+  s.gravity = dp[5]; s.lift = dp[6]; s.v0_sigma = dp[7]; s.active_frac = dp[8];
+  s.band = dp[9]; s.max_tilt = dp[10];
+  s.seed = seed;
+  BeamQPData *q = new BeamQPData;
+  if (!build_beam(s, *q)) {
+    delete q;
+    return nullptr;
+  }
+  *nv = q->nv;
+  *nnzb = (int)q->cols.size();
+  *nplanes = (int)(q->planes.size() / 4);
+  return q;
+}
+
+void oracle_beam_take(void *h, int *row_ptr, int *cols, double *vals, double *b, double *x0,
+                      int *plane_ptr, double *planes) {
+  BeamQPData *q = static_cast<BeamQPData *>(h);
+  std::memcpy(row_ptr, q->row_ptr.data(), sizeof(int) * q->row_ptr.size());
+  std::memcpy(cols, q->cols.data(), sizeof(int) * q->cols.size());
+  std::memcpy(vals, q->vals.data(), sizeof(double) * q->vals.size());
+  std::memcpy(b, q->b.data(), sizeof(double) * q->b.size());
+  std::memcpy(x0, q->x0.data(), sizeof(double) * q->x0.size());
+  std::memcpy(plane_ptr, q->plane_ptr.data(), sizeof(int) * q->plane_ptr.size());
+  std::memcpy(planes, q->planes.data(), sizeof(double) * q->planes.size());
+  delete q;
 }
 
 }  // extern "C"

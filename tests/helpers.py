@@ -48,6 +48,16 @@ def oracle():
         L.oracle_ica_solve.restype = C.c_int
         L.oracle_ica_solve.argtypes = [C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int, C.c_double,
                                        C.c_int, C.c_double, _P]
+        L.oracle_solve_warm.restype = C.c_int
+        L.oracle_solve_warm.argtypes = [C.c_int, C.c_int, _P, _P, _P, _P, C.c_int, _P, _P, _P, _P,
+                                        C.c_double, C.c_int, C.c_uint64, _P, _P, C.c_int, _P, _P,
+                                        _P]
+        L.oracle_set_scalar_test.restype = None
+        L.oracle_set_scalar_test.argtypes = [C.c_int]
+        L.oracle_beam_new.restype = C.c_void_p
+        L.oracle_beam_new.argtypes = [_P, _P, C.c_uint64, _P, _P, _P]
+        L.oracle_beam_take.restype = None
+        L.oracle_beam_take.argtypes = [C.c_void_p, _P, _P, _P, _P, _P, _P, _P]
         _orc = L
     return _orc
 
@@ -157,6 +167,75 @@ def oracle_solve(kind, A: Csr, b, x, J: Csr | None = None, c=None, L=None, U=Non
     stats = dict(zip(STAT_KEYS, st.tolist()))
     stats["code"] = code
     return x, face[:m], stats, evbuf
+
+
+def oracle_solve_warm(kind, A: Csr, b, x, J: Csr, c, ev=None, tol=1e-3, max_it=1000,
+                      seed=0x5EED, project_x0=True):
+    """The restated solve with MprgpFemSolver's power-method warm start
+    (MprgpFemSolver.cpp:533 passes &power_ev): `ev` is the stored vector or
+    None.  Returns (x, face, stats dict, ev or None)."""
+    O = oracle()
+    n = A.rows
+    x = np.ascontiguousarray(x, np.float64).copy()
+    st = np.zeros(10)
+    face = np.zeros(max(J.rows, 1), np.uint8)
+    evbuf = np.zeros(n) if ev is None else np.ascontiguousarray(ev, np.float64).copy()
+    valid = C.c_int(0 if ev is None else 1)
+    code = O.oracle_solve_warm(KIND[kind] if isinstance(kind, str) else kind, n, ptr(A.ptr),
+                               ptr(A.idx), ptr(A.val), ptr(np.ascontiguousarray(b, np.float64)),
+                               J.rows, ptr(J.ptr), ptr(J.idx), ptr(J.val),
+                               ptr(np.ascontiguousarray(c, np.float64)), tol, max_it, seed,
+                               ptr(evbuf), C.byref(valid), int(project_x0), ptr(x), ptr(face),
+                               ptr(st))
+    stats = dict(zip(STAT_KEYS, st.tolist()))
+    stats["code"] = code
+    return x, face[:J.rows], stats, (evbuf if valid.value else None)
+
+
+def oracle_scalar_test(on: bool):
+    """Switches the oracle's monotone CG test to the scalar form the GPU
+    evaluates (on) or back to the reference's comparison of f values."""
+    oracle().oracle_set_scalar_test(int(on))
+
+
+# Defaults of the synthetic beam (the library's mprgp_beam_default).
+BEAM_DEFAULTS = dict(edge=0.05, young=1e5, poisson=0.45, rho=1000.0, dt=0.01, gravity=-9.8,
+                     lift=0.01, v0_sigma=0.1, extra_planes_max=0, extra_planes_min=0,
+                     active_frac=1.0, seed=1, plane_band=0.025, max_tilt=1.5707963267948966,
+                     plane_mode=2, facet_layers=1)
+
+
+def oracle_beam(a: int, b: int, c: int, **kw):
+    """The synthetic beam QP built by the oracle's generator (beam_oracle.h),
+    with the library's keyword names; returns a mprgp_gb300.BeamQP without
+    loading the GPU library."""
+    from mprgp_gb300 import BeamQP
+    p = dict(BEAM_DEFAULTS)
+    unknown = set(kw) - set(p)
+    if unknown:
+        raise TypeError(f"unknown beam parameters {sorted(unknown)}")
+    p.update(kw)
+    ip = np.array([a, b, c, p["extra_planes_max"], p["extra_planes_min"], p["plane_mode"],
+                   p["facet_layers"]], np.int32)
+    dp = np.array([p[k] for k in ("edge", "young", "poisson", "rho", "dt", "gravity", "lift",
+                                  "v0_sigma", "active_frac", "plane_band", "max_tilt")], np.float64)
+    O = oracle()
+    nv, nnzb, npl = C.c_int(), C.c_int(), C.c_int()
+    h = O.oracle_beam_new(ptr(ip), ptr(dp), int(p["seed"]), C.byref(nv), C.byref(nnzb),
+                          C.byref(npl))
+    if not h:
+        raise ValueError(f"invalid beam parameters {a}x{b}x{c} {kw}")
+    nv, nnzb, npl = nv.value, nnzb.value, npl.value
+    row_ptr = np.zeros(nv + 1, np.int32)
+    cols = np.zeros(nnzb, np.int32)
+    vals = np.zeros((nnzb, 9))
+    rhs, x0 = np.zeros(3 * nv), np.zeros(3 * nv)
+    pptr = np.zeros(nv + 1, np.int32)
+    planes = np.zeros((npl, 4))
+    O.oracle_beam_take(h, ptr(row_ptr), ptr(cols), ptr(vals), ptr(rhs), ptr(x0), ptr(pptr),
+                       ptr(planes))
+    params = dict(p, a=a, b=b, c=c)
+    return BeamQP(nv, row_ptr, cols, vals, rhs, x0, pptr, planes, params)
 
 
 def qp_from_beam(qp):
