@@ -1027,7 +1027,9 @@ def run_serve(args):
         # solve the same QPs), about 15 s of host time; its solutions are
         # the served results' reference (error_vs_oracle).
         spent, solved = 0.0, {}
-        for ch in serve_chains(win):
+        chains = serve_chains(win)
+        for k in np.random.default_rng(SERVE_SEED).permutation(len(chains)):
+            ch = chains[k]
             dt, part = cpu_chains(win, [ch], 1, fb=pl.fb)
             spent += dt
             solved.update(part)
@@ -1037,7 +1039,8 @@ def run_serve(args):
         line["cpu_baseline"] = {
             "value": round(len(solved) / spent, 4), "unit": "solves/s", "cores": 1,
             "kind": "port",
-            "sample": f"whole scene chains from the start of the window: {len(solved)} requests "
+            "sample": f"whole scene chains of the window in a seeded random order: {len(solved)} "
+                      f"requests "
                       f"({nf} follow-up timesteps warm-started from the previous solution and "
                       f"power vector), solved one after another by the CPU restatement of the "
                       f"reference MPRGP (oracle/), single-threaded; {spent:.1f} s"}

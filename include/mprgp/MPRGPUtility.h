@@ -6,9 +6,11 @@
 //   Vec<T>            ~ Eigen::Matrix<T,-1,1>
 //   SparseMatrix<T>   ~ Eigen::SparseMatrix<T> (row-major CSR, built from triplets)
 //   VVEC4X / VVVEC4X  ~ the reference's per-vertex plane lists (Vector4d n, p)
-// and restates the binary QP file formats of writeQP/loadQP
-// (MPRGPUtility.h:157-485) so QPs dumped by the reference's FEM driver
-// (MprgpFemSolver.h:129-133) load here unchanged.
+// and restates the QP file formats of writeQP/loadQP (MPRGPUtility.h:157-485:
+// binary (A, B, J, c, x0), binary per-vertex planes, text with global
+// planes) so QPs dumped by the reference's FEM driver
+// (MprgpFemSolver.h:129-133) load here unchanged and files written here are
+// byte for byte the reference's.
 #pragma once
 
 #include <algorithm>
@@ -92,6 +94,15 @@ class SparseMatrix {
       for (int k = ptr_[r]; k < ptr_[r + 1]; ++k) t.emplace_back(r, idx_[k], val_[k]);
     return t;
   }
+  // The entries in the order the reference's files hold them: Eigen's
+  // default column-major storage walked column by column, rows ascending.
+  std::vector<Triplet<T>> triplets_by_column() const {
+    std::vector<Triplet<T>> t = triplets();
+    std::stable_sort(t.begin(), t.end(), [](const Triplet<T> &a, const Triplet<T> &b) {
+      return a.c != b.c ? a.c < b.c : a.r < b.r;
+    });
+    return t;
+  }
   const std::vector<int> &outerIndex() const { return ptr_; }
   const std::vector<int> &innerIndex() const { return idx_; }
   const std::vector<T> &values() const { return val_; }
@@ -114,6 +125,14 @@ inline int COUNT_CONSTRAINTS(const std::vector<char> &face) {
   int c = 0;
   for (char f : face) c += (int)f;
   return c;
+}
+
+// The same global planes for every one of num_nodes vertices
+// (MPRGPUtility.h:110-117).
+template <typename T>
+VVVEC4X<T> &convert(const VVEC4X<T> &in, VVVEC4X<T> &out, const size_t num_nodes) {
+  out.assign(num_nodes, in);
+  return out;
 }
 
 // Planes -> (J, c) with J x >= c: row = n at the vertex's 3 columns, c = -p
@@ -140,7 +159,7 @@ bool writeSparseMatrix(std::ofstream &out, const SparseMatrix<T> &A) {
   out.write((const char *)&r, sizeof(r));
   out.write((const char *)&c, sizeof(c));
   out.write((const char *)&nz, sizeof(nz));
-  const std::vector<Triplet<T>> t = A.triplets();
+  const std::vector<Triplet<T>> t = A.triplets_by_column();
   if (!t.empty()) out.write((const char *)t.data(), sizeof(Triplet<T>) * nz);
   return out.good();
 }
@@ -230,6 +249,70 @@ bool loadQP(SparseMatrix<T> &A, Vec<T> &B, VVVEC4X<T> &planes, Vec<T> &x0,
   }
   readVec(in, x0, A.rows());
   return in.good();
+}
+
+// ---- text QP file with global planes (MPRGPUtility.h:208-257, 295-357) ----
+// "dimension n", "planes m", "A", "non_zeros nnz", one "row\tcol\tvalue" line
+// per entry (column by column), "B" and one tab-separated line of n values,
+// "P" and one "nx\tny\tnz\tp" line per plane, "x0" and one line of n values;
+// numbers with 12 significant digits.  The planes apply to every vertex
+// (convert(planes, per_node, n / 3)).
+template <typename T>
+bool writeQP(const SparseMatrix<T> &A, const Vec<T> &B, const VVEC4X<T> &planes,
+             const Vec<T> &x0, const std::string &file_name) {
+  std::ofstream out(file_name.c_str());
+  if (!out.is_open()) return false;
+  out << "dimension " << A.rows() << "\n";
+  out << "planes " << planes.size() << "\n";
+  out << "A\n";
+  out << "non_zeros " << A.nonZeros() << "\n";
+  out.precision(12);
+  for (const Triplet<T> &t : A.triplets_by_column())
+    out << t.row() << "\t" << t.col() << "\t" << t.value() << "\n";
+  auto line = [&out](const Vec<T> &v) {
+    for (size_t i = 0; i < v.size(); ++i) out << (i ? "\t" : "") << v[i];
+    out << "\n";
+  };
+  out << "B\n";
+  line(B);
+  out << "P\n";
+  for (const auto &pl : planes)
+    out << pl[0] << "\t" << pl[1] << "\t" << pl[2] << "\t" << pl[3] << "\n";
+  out << "x0\n";
+  line(x0);
+  return out.good();
+}
+template <typename T>
+bool loadQP(SparseMatrix<T> &A, Vec<T> &B, VVEC4X<T> &planes, Vec<T> &x0,
+            const std::string &file_name) {
+  std::ifstream in(file_name.c_str());
+  if (!in.is_open()) return false;
+  std::string tag;
+  long long n = -1, m = -1, nnz = -1;
+  in >> tag >> n >> tag >> m;
+  in >> tag >> tag >> nnz;
+  if (!in.good() || n < 0 || m < 0 || nnz < 0) return false;
+  std::vector<Triplet<T>> t;
+  t.reserve((size_t)nnz);
+  for (long long k = 0; k < nnz; ++k) {
+    long long r, c;
+    T v;
+    in >> r >> c >> v;
+    if (!in.good() || r < 0 || c < 0 || r >= n || c >= n) return false;
+    t.emplace_back((int)r, (int)c, v);
+  }
+  A.resize((int)n, (int)n);
+  A.setFromTriplets(t.begin(), t.end());
+  in >> tag;
+  B.resize((size_t)n);
+  for (auto &v : B) in >> v;
+  in >> tag;
+  planes.resize((size_t)m);
+  for (auto &pl : planes) in >> pl[0] >> pl[1] >> pl[2] >> pl[3];
+  in >> tag;
+  x0.resize((size_t)n);
+  for (auto &v : x0) in >> v;
+  return !in.fail();
 }
 
 }  // namespace MATH

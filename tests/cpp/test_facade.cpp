@@ -1,8 +1,12 @@
 // Drop-in test of the C++ façade: the reference's own unit tests
 // (test_case/MPRGPTest.cpp) written against include/mprgp/MPRGPSolver.h,
 // plus the reference's binary QP file round trip (MPRGPUtility.h:407-485)
-// and the file-form solve (MPRGPSolver.h:576-589).  Prints one line per
-// check; exits non-zero on failure.
+// and the file-form solve (MPRGPSolver.h:576-589).  Given the fixture
+// directory tests/golden/qp_files as argv[1], it also solves the fixtures the
+// way a reference user would -- the decoupled file form on the (J, c) file,
+// and the text file's global planes through convert() and MPRGPGeneralCon --
+// and writes each solution to x_<form>.txt for the oracle comparison.
+// Prints one line per check; exits non-zero on failure.
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -31,7 +35,19 @@ static SparseMatrix<double> from_dense(const std::vector<double> &M, int r, int 
   return S;
 }
 
-int main() {
+static void save(const Vec<double> &x, const char *path) {
+  FILE *f = std::fopen(path, "w");
+  for (double v : x) std::fprintf(f, "%.17g\n", v);
+  std::fclose(f);
+}
+
+static double norm(const Vec<double> &v) {
+  double s = 0.0;
+  for (double t : v) s += t * t;
+  return std::sqrt(s);
+}
+
+int main(int argc, char **argv) {
   std::mt19937 gen(7);
   std::uniform_real_distribution<double> U(-1.0, 1.0);
   // test_solver (MPRGPTest.cpp:70-98): random SPD 5x5, J = I.
@@ -132,6 +148,35 @@ int main() {
     CHECK(ica.getResidual() <= 1e-12);
     std::printf("ica: iterations %d residual %.3e |x_ica - x_mprgp| %.3e\n", ica.getIterations(),
                 ica.getResidual(), std::sqrt(d));
+  }
+  if (argc > 1) {  // the reference file forms, solved as a reference user would
+    const std::string dir = argv[1];
+    {
+      SparseMatrix<double> A, J;
+      Vec<double> B, c, x0;
+      CHECK(loadQP(A, B, J, c, x0, dir + "/beam_1x2x2.jc.b"));
+      Vec<double> y;
+      const int rc = MPRGPDecoupledCon<double>::solve<true>(dir + "/beam_1x2x2.jc.b", y,
+                                                            1e-10 * norm(B), 10000);
+      std::printf("file-form (J, c) solve: code %d\n", rc);
+      CHECK(rc == 0 && y.size() == B.size());
+      save(y, "x_jc.txt");
+    }
+    {
+      SparseMatrix<double> A, J;
+      Vec<double> B, c, x;
+      VVEC4X<double> planes;
+      VVVEC4X<double> per_node;
+      CHECK(loadQP(A, B, planes, x, dir + "/beam_1x2x2.txt"));
+      convert(planes, per_node, (size_t)A.rows() / 3);
+      convert(per_node, J, c);
+      FixedSparseMatrix<double> FA(A);
+      const int rc = MPRGPGeneralCon<double>::solve<FixedSparseMatrix<double>, true>(
+          FA, B, J, c, x, 1e-10 * norm(B), 10000);
+      std::printf("text-form solve (global planes): code %d\n", rc);
+      CHECK(rc == 0);
+      save(x, "x_text.txt");
+    }
   }
   std::printf("%s (%d failures)\n", failures ? "FAILED" : "OK", failures);
   return failures ? 1 : 0;

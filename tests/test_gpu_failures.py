@@ -120,15 +120,21 @@ def test_admission_waits_for_device_room(fresh_ctx, lanes):
     evicted, then both are solved."""
     ctx = fresh_ctx
     qps = [corner(24, 24, 48, seed=s) for s in (1, 2)]
-    one = M.lib().mprgp_problem_bytes(qps[0].nv, qps[0].nnzb, len(qps[0].planes), 3)
-    # warm the context (its run buffers come from the same pool)
+    mixed = lambda q: opts(q, precision=M.PREC_MIXED)  # noqa: E731
+    # warm the context (its run buffers come from the same pool) and measure
+    # what one resident scene takes
     warm = M.Server(ctx, quantum_phases=-1, power_launches=1003, lanes=lanes)
-    assert _serve(warm, qps[:1], lambda q: opts(q, precision=M.PREC_MIXED))[0] == {0: 0}
+    assert _serve(warm, qps[:1], mixed)[0] == {0: 0}
     warm.close()
-    room = ctx.room()
+    srv = M.Server(ctx, quantum_phases=-1, power_launches=1003, lanes=lanes)
+    before = ctx.room()
+    assert _serve(srv, qps[:1], mixed)[0] == {0: 0}
+    one = before - ctx.room()
+    srv.close()
+    assert one > 0
     srv = M.Server(ctx, quantum_phases=-1, power_launches=1003, lanes=lanes,
-                   hbm_reserve=room - int(1.5 * one))
-    codes, max_scenes = _serve(srv, qps, lambda q: opts(q, precision=M.PREC_MIXED))
+                   hbm_reserve=ctx.room() - int(1.5 * one))
+    codes, max_scenes = _serve(srv, qps, mixed)
     srv.close()
     assert codes == {0: 0, 1: 0}
     assert max_scenes == 1

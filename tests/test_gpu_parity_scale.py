@@ -83,6 +83,12 @@ def test_steps_equal_scalar_test_oracle(ctx, case, rel_tol):
           f"{int(ss['num_prop'])}); oracle, reference test {int(sr['iterations'])} "
           f"({int(sr['num_cg'])}/{int(sr['num_exp'])}/{int(sr['num_prop'])})")
     assert sg.code == 0 and ss["code"] == 0 and sr["code"] == 0
+    # The oracle records the CG loop's exit (event 2) also when the loop ends
+    # because the residual met the tolerance; the GPU goes straight to the
+    # final projection there.  That last entry is the only difference allowed.
+    if len(ts) == len(tg) + 1:
+        assert ts[-1, 0] == 2 and ts[-1, 2] <= tol and tg[-1, 0] == 1, (ts[-3:], tg[-3:])
+        ts = ts[:-1]
     # the whole step sequence: event kind and iteration number of every entry
     assert len(tg) == len(ts), (len(tg), len(ts))
     assert np.array_equal(tg[:, :2], ts[:, :2])
