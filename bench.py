@@ -74,6 +74,9 @@ def parse():
                          "small/large lanes, 3 plus a lane for the large ones' power method)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the launch-shape autotuner (mprgp_gb300.autotune) before warm-up")
+    ap.add_argument("--single", action="store_true",
+                    help="c3: one solve of the timestep beam's first QP (the c0/c1 line) instead "
+                         "of the 20-timestep loop")
     ap.add_argument("--spmv", action="store_true",
                     help="time the standalone y = A x (mprgp_problem_spmv) on the config's "
                          "matrix instead of the solver, FP64 and FP32 values")
@@ -376,6 +379,8 @@ def run_gb300(args):
         line["e2e"] = run_e2e(ctx, qp, opt, args, world, mixed)
     if not args.no_ica and args.config in ("c0", "c1"):
         line["ica_comparison"] = run_ica(ctx, qp, tol, prob)
+    if not args.no_e2e and rank == 0 and args.form == "plain":
+        line["e2e_facade"] = run_facade_newton(qp)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, cst = cpu_baseline(qp, 1)
         line["cpu_baseline"] = {
@@ -409,6 +414,64 @@ def run_ica(ctx, qp, tol, prob):
             "pgs_sweeps": int(st.pgs_sweeps), "levels": st.levels,
             "device_ms": round(min(ms), 3), "residual": st.residual, "tol": tol,
             "rel_diff_to_mprgp_x": float(np.linalg.norm(x - x_m) / np.linalg.norm(x_m))}
+
+
+def write_qp_file(qp, path):
+    """The QP as the reference's binary (A, B, J, c, x0) file
+    (MPRGPUtility.h:407-443): triplets in column-major order."""
+    import mprgp_gb300 as M
+    ptr, idx, val = M.bsr_to_csr(qp.nv, qp.row_ptr, qp.cols, qp.vals)
+    rows = np.repeat(np.arange(qp.n, dtype=np.int32), np.diff(ptr))
+    jptr, jidx, jval, c = M.planes_to_J(qp.nv, qp.plane_ptr, qp.planes)
+    jrows = np.repeat(np.arange(len(c), dtype=np.int32), np.diff(jptr))
+    rec = np.dtype([("r", "<i4"), ("c", "<i4"), ("v", "<f8")])
+
+    def sparse(f, nr, nc, r, cc, v):
+        order = np.lexsort((r, cc))
+        np.array([nr, nc, len(v)], "<u8").tofile(f)
+        t = np.empty(len(v), rec)
+        t["r"], t["c"], t["v"] = r[order], np.asarray(cc)[order], np.asarray(v)[order]
+        t.tofile(f)
+
+    with open(path, "wb") as f:
+        sparse(f, qp.n, qp.n, rows, idx, val)
+        np.asarray(qp.b, "<f8").tofile(f)
+        sparse(f, len(c), qp.n, jrows, jidx, jval)
+        np.asarray(c, "<f8").tofile(f)
+        np.asarray(qp.x0, "<f8").tofile(f)
+
+
+def run_facade_newton(qp, steps=4):
+    """The C++ façade as the reference's FEM driver calls it: the same QP
+    (from a reference-layout file) solved `steps` times through
+    MPRGPGeneralCon<double>::solve with the same sparsity and new values each
+    time (tests/cpp/facade_newton.cpp).  Wall time per call, host conversion
+    and copies included: the first call builds the 3x3-block pattern, the
+    later ones refill its values."""
+    import subprocess
+    import tempfile
+    import mprgp_gb300 as M
+    libdir = os.path.dirname(M.build())
+    with tempfile.TemporaryDirectory() as tmp:
+        exe, qpf = os.path.join(tmp, "facade_newton"), os.path.join(tmp, "qp.b")
+        subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "facade_newton.cpp"), "-L", libdir,
+                        "-lmprgp_gb300", f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
+        write_qp_file(qp, qpf)
+        res = subprocess.run([exe, qpf, str(steps), str(REL_TOL)], capture_output=True,
+                             text=True, timeout=600)
+    kv = dict(t.split("=") for t in res.stdout.split())
+    if res.returncode != 0:
+        return {"error": res.stdout.strip() + res.stderr.strip()[-300:]}
+    later = float(kv["later_ms"])
+    return {"value": round(1e3 / later, 4), "unit": "solves/s",
+            "first_call_ms": float(kv["first_ms"]), "later_call_ms": later,
+            "calls": int(kv["solves"]), "pattern_builds": int(kv["pattern_builds"]),
+            "pattern_refills": int(kv["pattern_refills"]),
+            "path": "C++ façade MPRGPGeneralCon<double>::solve (include/mprgp/MPRGPSolver.h) "
+                    "from host Eigen-like CSR: a Newton loop's re-solves with the same "
+                    "sparsity (new values each call; the block pattern is kept, values "
+                    "refilled), wall time per call with conversion and copies"}
 
 
 def run_e2e(ctx, qp, opt, args, world, mixed):
@@ -1227,7 +1290,7 @@ def main():
         run_batch(args)
     elif args.config == "c4":
         run_serve(args)
-    elif args.config == "c3":
+    elif args.config == "c3" and not args.single:
         run_timesteps(args)
     else:
         run_gb300(args)

@@ -49,14 +49,14 @@ class ICASolver {
       code = MPRGP_NO_DEVICE;
       return false;
     }
-    int nv;
-    std::vector<int> row_ptr, cols, plane_ptr, order;
-    std::vector<double> vals, planes;
-    gpu::to_bsr(*pA, nv, row_ptr, cols, vals);
+    const gpu::BlockPattern &P = gpu::to_bsr(*pA);
+    const int nv = P.nv;
+    std::vector<int> plane_ptr, order;
+    std::vector<double> planes;
     if (!gpu::to_planes(J, p, nv, plane_ptr, planes, order)) return false;
     std::vector<double> xx(x.begin(), x.end()), lam(std::max<size_t>(order.size(), 1), 0.0);
     mprgp_ica_stats st{};
-    code = mprgp_ica_solve(ctx, nv, (int)cols.size(), row_ptr.data(), cols.data(), vals.data(),
+    code = mprgp_ica_solve(ctx, nv, (int)P.cols.size(), P.row_ptr.data(), P.cols.data(), P.vals.data(),
                            R.data(), plane_ptr.data(), planes.empty() ? nullptr : planes.data(),
                            xx.data(), lam.data(), max_it, tol, gs_max_it, gs_tol, &st);
     if (code < MPRGP_NOT_CONVERGED) return false;

@@ -96,53 +96,100 @@ const SparseMatrix<T> &matrix_of(const SparseMatrix<T> &A) {
   return A;
 }
 
-// n x n scalar CSR -> 3x3 blocks over nv = ceil(n / 3) vertices.  Padded
-// unknowns get a unit-free diagonal equal to the smallest diagonal entry of A
-// (never above the spectral radius) and no coupling.
+// The 3x3-block form of an n x n scalar CSR over nv = ceil(n / 3) vertices,
+// with the map from each scalar entry to its block value.  Padded unknowns
+// get a unit-free diagonal equal to the smallest positive diagonal entry of
+// A (never above the spectral radius) and no coupling.  The FEM driver
+// re-solves with the same sparsity every Newton iteration
+// (MprgpFemSolver.cpp:521-533), so the pattern is kept per thread and a
+// matrix with the same pattern only refills the values.
+struct BlockPattern {
+  std::vector<int> sptr, sidx;  // the scalar pattern the blocks were built for
+  int n = -1, nv = 0;
+  std::vector<int> row_ptr, cols;
+  std::vector<size_t> where;  // scalar entry k -> its block value
+  std::vector<size_t> diag;   // scalar entries on the diagonal
+  std::vector<size_t> pad;    // block values of the padded unknowns' diagonal
+  std::vector<double> vals;
+  long long builds = 0, refills = 0;
+};
+inline BlockPattern &block_pattern() {
+  static thread_local BlockPattern p;
+  return p;
+}
+
 template <typename T>
-void to_bsr(const SparseMatrix<T> &A, int &nv, std::vector<int> &row_ptr,
-            std::vector<int> &cols, std::vector<double> &vals) {
+void build_pattern(const SparseMatrix<T> &A, BlockPattern &P) {
   const int n = A.rows();
-  nv = (n + 2) / 3;
   const auto &ptr = A.outerIndex();
   const auto &idx = A.innerIndex();
-  const auto &val = A.values();
-  double dmin = 0.0;
-  bool first = true;
-  for (int i = 0; i < n; ++i) {
-    const double d = (double)A.coeff(i, i);
-    if (d > 0 && (first || d < dmin)) { dmin = d; first = false; }
-  }
-  if (first) dmin = 1.0;
-  row_ptr.assign(nv + 1, 0);
-  cols.clear();
-  vals.clear();
+  P.n = n;
+  P.nv = (n + 2) / 3;
+  P.sptr = ptr;
+  P.sidx = idx;
+  P.row_ptr.assign(P.nv + 1, 0);
+  P.cols.clear();
+  P.where.assign(idx.size(), 0);
+  P.diag.clear();
+  P.pad.clear();
   std::vector<int> bc;
-  for (int v = 0; v < nv; ++v) {
+  for (int v = 0; v < P.nv; ++v) {
     bc.clear();
     for (int r = 3 * v; r < std::min(n, 3 * v + 3); ++r)
       for (int k = ptr[r]; k < ptr[r + 1]; ++k) bc.push_back(idx[k] / 3);
     bc.push_back(v);
     std::sort(bc.begin(), bc.end());
     bc.erase(std::unique(bc.begin(), bc.end()), bc.end());
-    const size_t base = cols.size();
-    cols.insert(cols.end(), bc.begin(), bc.end());
-    vals.resize(9 * cols.size(), 0.0);
+    const size_t base = P.cols.size();
+    P.cols.insert(P.cols.end(), bc.begin(), bc.end());
+    auto slot = [&](int cb) {
+      return base + (size_t)(std::lower_bound(bc.begin(), bc.end(), cb) - bc.begin());
+    };
     for (int i = 0; i < 3; ++i) {
       const int r = 3 * v + i;
       if (r >= n) {
-        const size_t q = base + (std::lower_bound(bc.begin(), bc.end(), v) - bc.begin());
-        vals[9 * q + 4 * i] = dmin;
+        P.pad.push_back(9 * slot(v) + 4 * i);
         continue;
       }
       for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
-        const int cb = idx[k] / 3;
-        const size_t q = base + (std::lower_bound(bc.begin(), bc.end(), cb) - bc.begin());
-        vals[9 * q + 3 * i + (idx[k] % 3)] += (double)val[k];
+        P.where[k] = 9 * slot(idx[k] / 3) + 3 * i + (idx[k] % 3);
+        if (idx[k] == r) P.diag.push_back((size_t)k);
       }
     }
-    row_ptr[v + 1] = (int)cols.size();
+    P.row_ptr[v + 1] = (int)P.cols.size();
   }
+  ++P.builds;
+}
+
+// The block values of A on pattern P: entries summed in scalar order.
+template <typename T>
+void fill_values(const SparseMatrix<T> &A, BlockPattern &P) {
+  const auto &val = A.values();
+  P.vals.assign(9 * P.cols.size(), 0.0);
+  for (size_t k = 0; k < P.where.size(); ++k) P.vals[P.where[k]] += (double)val[k];
+  double dmin = 0.0;
+  bool first = true;
+  for (size_t k : P.diag) {  // the smallest positive diagonal entry
+    const double d = (double)val[k];
+    if (d > 0 && (first || d < dmin)) {
+      dmin = d;
+      first = false;
+    }
+  }
+  if (first) dmin = 1.0;
+  for (size_t q : P.pad) P.vals[q] = dmin;
+}
+
+// A's blocks, rebuilding the pattern only when A's sparsity changed.
+template <typename T>
+const BlockPattern &to_bsr(const SparseMatrix<T> &A) {
+  BlockPattern &P = block_pattern();
+  if (P.n != A.rows() || P.sptr != A.outerIndex() || P.sidx != A.innerIndex())
+    build_pattern(A, P);
+  else
+    ++P.refills;
+  fill_values(A, P);
+  return P;
 }
 
 // Rows of J (J x >= c) -> per-vertex planes (n, p = -c) in plane_ptr order;
@@ -186,10 +233,8 @@ int solve(const SparseMatrix<T> &A, const Vec<T> &B, const SparseMatrix<T> *J, c
   if (!ctx) return MPRGP_NO_DEVICE;
   const int n = A.rows();
   if (A.cols() != n || (int)B.size() != n || (int)x.size() != n) return MPRGP_INVALID;
-  int nv;
-  std::vector<int> row_ptr, cols;
-  std::vector<double> vals;
-  to_bsr(A, nv, row_ptr, cols, vals);
+  const BlockPattern &P = to_bsr(A);
+  const int nv = P.nv;
   const int np = 3 * nv;
   std::vector<double> b(np, 0.0), xx(np, 0.0), l, u, evv;
   for (int i = 0; i < n; ++i) {
@@ -226,8 +271,8 @@ int solve(const SparseMatrix<T> &A, const Vec<T> &B, const SparseMatrix<T> *J, c
   const size_t m = kind >= MPRGP_KIND_DECOUPLED ? order.size() : (size_t)np;
   std::vector<unsigned char> f(std::max<size_t>(m, 1), 0);
   mprgp_stats st{};
-  const int rc = mprgp_solve_bsr(ctx, nv, (int)cols.size(), row_ptr.data(), cols.data(),
-                                 vals.data(), b.data(), plane_ptr.empty() ? nullptr : plane_ptr.data(),
+  const int rc = mprgp_solve_bsr(ctx, nv, (int)P.cols.size(), P.row_ptr.data(), P.cols.data(),
+                                 P.vals.data(), b.data(), plane_ptr.empty() ? nullptr : plane_ptr.data(),
                                  planes.empty() ? nullptr : planes.data(),
                                  l.empty() ? nullptr : l.data(), u.empty() ? nullptr : u.data(), &opt,
                                  xx.data(), f.data(), ev ? evv.data() : nullptr, &st);

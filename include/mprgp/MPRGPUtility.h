@@ -106,6 +106,9 @@ class SparseMatrix {
   const std::vector<int> &outerIndex() const { return ptr_; }
   const std::vector<int> &innerIndex() const { return idx_; }
   const std::vector<T> &values() const { return val_; }
+  // Eigen's valuePtr(): the values in storage order, for in-place updates
+  // that keep the sparsity (a Newton iteration's new A).
+  T *valuePtr() { return val_.data(); }
 
  private:
   int rows_ = 0, cols_ = 0;

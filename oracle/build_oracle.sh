@@ -10,6 +10,4 @@ mkdir -p "$HERE/_build"
 g++ -std=c++17 -O3 -ffp-contract=off -fopenmp -fPIC -shared -Wall -Wno-unused-function \
   "$HERE/oracle_capi.cpp" -o "$HERE/_build/liboracle.so"
 echo "built $HERE/_build/liboracle.so"
-if [ -d "${MPRGP_REFERENCE_ROOT:-/root/reference}" ]; then
-  bash "$HERE/build_ref.sh" "${MPRGP_REFERENCE_ROOT:-/root/reference}"
-fi
+bash "$HERE/build_ref.sh"  # skips when the reference tree is absent

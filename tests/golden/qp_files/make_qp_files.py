@@ -51,12 +51,14 @@ def scalar_A(qp):
 
 
 def floor_J(qp):
-    """The floor row of every vertex: J = e_y at its 3 columns, c = 0."""
+    """The floor row of every vertex: J = e_y at its 3 columns and c = -p =
+    -0.0, as the reference's convert (MPRGPUtility.h:120-154) and its
+    collider (LinearConCollider.cpp:71) negate the plane offset p = 0."""
     rows = np.repeat(np.arange(qp.nv), 3)
     cols = (3 * np.arange(qp.nv)[:, None] + np.arange(3)[None, :]).reshape(-1)
     vals = np.tile([0.0, 1.0, 0.0], qp.nv)
     order = np.lexsort((rows, cols))
-    return rows[order], cols[order], vals[order], np.zeros(qp.nv)
+    return rows[order], cols[order], vals[order], -np.zeros(qp.nv)
 
 
 def sparse_bytes(nrows, ncols, r, c, v):

@@ -74,10 +74,9 @@ def quadprog_ref():
     global _qp
     if _qp is None:
         if not os.path.exists(QP_REF_LIB):
-            ref = os.environ.get("MPRGP_REFERENCE_ROOT", "/root/reference")
-            if os.path.isdir(ref):
-                subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), ref],
-                               check=True, capture_output=True)
+            # the recipe finds the reference tree (MPRGP_REFERENCE_ROOT) or skips
+            subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True,
+                           capture_output=True)
         if not os.path.exists(QP_REF_LIB):
             return None
         L = C.CDLL(QP_REF_LIB)

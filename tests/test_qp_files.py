@@ -38,6 +38,15 @@ def test_fixture_holds_the_beam_qp():
     assert np.array_equal(dense, Ac.dense())
     assert np.array_equal(B, qp.b) and np.array_equal(x0, qp.x0)
     assert J[0] == qp.nv and np.array_equal(c, np.zeros(qp.nv))
+    # the bench's writer of the same layout gives the same bytes
+    sys.path.insert(0, ROOT)
+    import bench
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "qp.b")
+        bench.write_qp_file(qp, path)
+        with open(path, "rb") as f1, open(os.path.join(QPDIR, "beam_1x2x2.jc.b"), "rb") as f2:
+            assert f1.read() == f2.read()
     At, Bt, P, xt = Q.read_text(os.path.join(QPDIR, "beam_1x2x2.txt"))
     dense_t = np.zeros((qp.n, qp.n))
     dense_t[At[2], At[3]] = At[4]
