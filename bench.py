@@ -113,6 +113,42 @@ def spmv_bytes(qp, s_a):
     return qp.nnzb * (9 * s_a + 4) + (qp.nv + 1) * 4 + 2 * qp.n * s_a
 
 
+# n-vector traffic of the solver phases beyond the matrix pass, in FP64
+# vectors of n = 3 nv unknowns (8n bytes each; an FP32 shadow counts half),
+# counted from the row functions of mprgp_gb300/csrc/engine.cu.  The matrix
+# pass's own x gather and y store are in spmv_bytes.
+#   power pass   FP32 form: t_k read, t_{k-1} read, t_k store (3 x 4n)   1.5
+#                FP64 form: the same in FP64                              3
+#   CG step      PH_CG_SPMV: g, z, p read; p', Ap stored (mixed: p' FP32
+#                shadow, second FP32 source)                              5 (+1)
+#                PH_CG_YF: x, p, Ap, g read; y, g_y, delta, z, beta
+#                stored (mixed: z FP32 shadow)                            9 (+0.5)
+#   expansion    PH_EXP_A 2, PH_EXP_B 4, PH_EXP_C 6 (mixed +1)           12 (+1)
+#   proportioning PH_PROP_A 4, PH_PROP_B 9 (mixed +1)                    13 (+1)
+#   any other phase (init, CG entry, residual replacement, projections)   6
+# and each phase that reads the constraints reads 49 B per plane row
+# (n, c, 1/|n|^2, 1/(n.D^-1 n), face).
+VEC_K = {"pow32": 1.5, "pow64": 3.0, "cg": 14.0, "cg_mixed": 15.5, "exp": 12.0, "exp_mixed": 13.0,
+         "prop": 13.0, "prop_mixed": 14.0, "other": 6.0}
+PLANE_ROW_BYTES = 49
+
+
+def vector_bytes(st, qp, mixed, include_power=True):
+    """Estimated n-vector and constraint bytes of a solve beyond its matrix
+    passes, from its step counts (VEC_K); include_power=False leaves out the
+    power method's."""
+    n8 = 8 * qp.n
+    m = len(qp.planes)
+    pw = int(st.power_passes)
+    cg, ex, pr = int(st.num_cg), int(st.num_exp), int(st.num_prop)
+    other = max(0, int(st.phases) - pw - 2 * cg - 3 * ex - 2 * pr)
+    k = (VEC_K["pow32" if mixed else "pow64"] * pw * include_power
+         + VEC_K["cg_mixed" if mixed else "cg"] * cg
+         + VEC_K["exp_mixed" if mixed else "exp"] * ex
+         + VEC_K["prop_mixed" if mixed else "prop"] * pr + VEC_K["other"] * other)
+    return int(k * n8 + PLANE_ROW_BYTES * m * (cg + 2 * ex + pr + other))
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -320,6 +356,7 @@ def run_gb300(args):
     all_bytes = sum(s.spmv_fp64 * spmv_bytes(qp, 8) + s.spmv_fp32 * spmv_bytes(qp, 4)
                     for s in stats)
     eng_bytes = all_bytes - passes * pass_bytes
+    eng_vec = sum(vector_bytes(s, qp, mixed, include_power=False) for s in stats)
     if power_ms > 0:  # the power loop ran as its own kernel
         pow_launch_ms = power_ms / max(1, passes)
         achieved = pass_bytes / (pow_launch_ms / 1e3) / 1e9
@@ -339,7 +376,7 @@ def run_gb300(args):
         traffic = None
         dominant = "mprgp::engine_kernel (power and MPRGP phases, one launch per solve)"
         eng_bytes, eng_ms = all_bytes, solver1 - solver0
-    eng_achieved = eng_bytes / (eng_ms / 1e3) / 1e9 if eng_ms > 0 else None
+    eng_achieved = (eng_bytes + eng_vec) / (eng_ms / 1e3) / 1e9 if eng_ms > 0 else None
     line = {
         "metric": "QP solves/s + p50/p99 latency at ||g_P||<=1e-8||b||: served vs plain FP64, 1 GB300",
         "value": round(value, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -367,10 +404,11 @@ def run_gb300(args):
         "roofline_engine": {"kernel": "mprgp::engine_kernel (MPRGP phases)",
                             "achieved": None if eng_achieved is None else round(eng_achieved, 2),
                             "frac": None if eng_achieved is None else round(eng_achieved / peak, 4),
-                            "bytes": int(eng_bytes), "ms": round(eng_ms, 3),
+                            "bytes": int(eng_bytes + eng_vec), "bytes_matrix": int(eng_bytes),
+                            "bytes_vectors": int(eng_vec), "ms": round(eng_ms, 3),
                             "traffic": committed_traffic(args.config, args.form, "engine_kernel"),
-                            "note": "matrix-pass bytes only; the MPRGP phases also move ~8-10 "
-                                    "n-vectors per phase and are FP64-issue bound (ncu)"},
+                            "note": "matrix passes plus the estimated vector traffic (VEC_K); "
+                                    "the MPRGP phases are FP64-issue bound (ncu)"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "wall_s_timed": round(wall, 3),
@@ -1014,16 +1052,17 @@ def run_serve(args):
                                      "p99_ms": round(float(np.percentile(b.latency_s, 99)) * 1e3, 3)}})
     # roofline of the solver kernels over the timed plays
     scene = {r.scene: r.qp for r in win.reqs if not r.followup}
-    alg = 0
+    alg = vec = 0
     for res in timed:
         for i, st in enumerate(res.stats):
             q = scene[win.reqs[i].scene]
             alg += st.spmv_fp64 * spmv_bytes(q, 8) + st.spmv_fp32 * spmv_bytes(q, 4)
+            vec += vector_bytes(st, q, mixed)
     # device time of the solver runs; concurrent lanes overlap, so their sum
     # is capped by the windows' own device time
     solver_ms = min(sum(r.solver_ms for r in timed), local_ms)
     peak, peak_kind = measured_peaks()
-    achieved = alg / (solver_ms / 1e3) / 1e9
+    achieved = (alg + vec) / (solver_ms / 1e3) / 1e9
     launches = sum(r.launches for r in timed)
     its = [st.iterations for st in timed[0].stats]
     line = {
@@ -1064,9 +1103,14 @@ def run_serve(args):
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "traffic": None,
-                     "bytes_per_launch": int(alg / max(1, launches)),
+                     "bytes_per_launch": int((alg + vec) / max(1, launches)),
                      "launch_ms": round(solver_ms / max(1, launches), 5),
-                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
+                     "bytes_matrix_per_step": int(alg / len(timed)),
+                     "bytes_vectors_per_step": int(vec / len(timed)),
+                     "achieved_matrix_only": round(alg / (solver_ms / 1e3) / 1e9, 2),
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) "
+                                   "or 4 (FP32); plus k*n*8 of vector traffic per phase (VEC_K "
+                                   "in bench.py) and 49 B per constraint row read"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }

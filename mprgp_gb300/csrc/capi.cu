@@ -846,7 +846,9 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   const int pp_cap = c->nsm * c->bps_power_pp;
   R.power_persistent = R.power && c->power_persistent && k == 0 && !other_lanes_active(c, k) &&
                        pp_cap > 0 && prefix[n_large] <= pp_cap * kPowOwn;
-  const int pp_grid = std::max(1, std::min(prefix[n_large], pp_cap));
+  // equally many items per CTA (the phase waits for the busiest CTA)
+  const int pp_per = pp_cap > 0 ? (prefix[n_large] + pp_cap - 1) / pp_cap : 1;
+  const int pp_grid = std::max(1, (prefix[n_large] + pp_per - 1) / std::max(1, pp_per));
   if (R.power) {
     if (c->power_graph && !R.power_persistent) {
       rc = power_graph(L, pgrid, R.power_variant, &pexec);

@@ -2060,108 +2060,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     phase_item<kAll>(args, item, pc, h, signal, sD, sS, red, sums, s_last, active);
 }
 
-// ------------------------------------------------ persistent power loop -----
-// Every power-method phase of a run's large instances in one cooperative
-// launch, a bounded grid barrier as the phase boundary.  Each CTA owns up to
-// kPowOwn items (grid-stride) and keeps their desc and state in shared
-// memory for the whole loop.  A phase: the owned items' rows and item
-// partials (double-buffered by phase parity in the instance's partial
-// array), the grid barrier, then every CTA reads all partials of each owned
-// item's instance, reduces them exactly as the launch form's finalize does
-// and advances its own copy of the state -- so every copy, and the result,
-// is bitwise that of the launch form.  The loop ends one phase after no
-// instance is left in a power phase (each CTA publishes the last phase at
-// which one of its instances was still busy, with atomicMax), or after
-// `limit` phases; then the CTA owning an instance's first item writes its
-// state back.
-
-template <int kMinBlocks>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
-    power_persistent_kernel(EngineArgs args, PowCtl *pc, int limit) {
-  __shared__ InstDesc sD[kPowOwn];
-  __shared__ InstState sS[kPowOwn];
-  __shared__ RedBuf red;
-  __shared__ double sums[kPart];
-  if (threadIdx.x == 0) g_staged = 0;
-  int own[kPowOwn];
-  int nown = 0;
-  for (int item = blockIdx.x; item < args.total_items && nown < kPowOwn; item += gridDim.x)
-    own[nown++] = item;
-  int inst_of[kPowOwn];
-  for (int o = 0; o < nown; ++o) {
-    inst_of[o] = instance_of(args.item_inst, args.item_prefix, args.ninst, own[o]);
-    const int *srcd = reinterpret_cast<const int *>(args.desc + inst_of[o]);
-    int *dstd = reinterpret_cast<int *>(&sD[o]);
-    for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kThreads) dstd[w] = ldro(srcd + w);
-  }
-  __syncthreads();
-  for (int o = 0; o < nown; ++o) {
-    const int *srcs = reinterpret_cast<const int *>(args.states ? args.states + inst_of[o] : sD[o].st);
-    int *dsts = reinterpret_cast<int *>(&sS[o]);
-    for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kThreads) dsts[w] = srcs[w];
-  }
-  __syncthreads();
-  int t = 0;
-  for (;; ++t) {
-    const int par = t & 1;
-    for (int o = 0; o < nown; ++o) {
-      const int phase = sS[o].phase;
-      if (!power_phase(phase)) continue;
-      const int local = own[o] - sD[o].item_begin;
-      const int slot = local * kThreads + threadIdx.x;
-      double part[kPart];
-#pragma unroll
-      for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-      if (slot < sD[o].nv) {
-        const int v = sD[o].A.rowmap ? ldro(sD[o].A.rowmap + slot) : slot;
-        row_power(sD[o], sS[o], v, slot, part);
-      }
-      const int ns = nslots(phase);
-      const double r = block_reduce(part, red, ns, false);
-      double *pp = sD[o].part + (size_t)par * sD[o].nitems * kPart;
-      if (threadIdx.x < ns) pp[(size_t)local * kPart + threadIdx.x] = r;
-    }
-    int unused;
-    if (!grid_barrier(args.ctl, args.wait_ns, unused)) return;
-    if (t > 0 && *(volatile unsigned int *)&pc->busy < (unsigned int)t) break;
-    bool busy = false;
-    for (int o = 0; o < nown; ++o) {
-      const int phase = sS[o].phase;
-      if (!power_phase(phase)) continue;
-      const int ns = nslots(phase);
-      const double *pp = sD[o].part + (size_t)par * sD[o].nitems * kPart;
-      double acc[kPart];
-#pragma unroll
-      for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-      for (int it = threadIdx.x; it < sD[o].nitems; it += kThreads) {
-#pragma unroll
-        for (int k = 0; k < kPart; ++k) {
-          if (k >= ns || k == kMinSlot) continue;
-          acc[k] += pp[(size_t)it * kPart + k];
-        }
-      }
-      const double tt = block_reduce(acc, red, ns, false);
-      if (threadIdx.x < kPart) sums[threadIdx.x] = tt;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        sS[o].phases++;
-        advance_power(sD[o], sS[o], sums);
-      }
-      __syncthreads();
-      busy |= power_phase(sS[o].phase);
-    }
-    if (busy && threadIdx.x == 0) atomicMax(&pc->busy, (unsigned int)(t + 1));
-    if (t + 1 >= limit) {
-      ++t;
-      break;
-    }
-  }
-  // the working phases run (the launch form's launch count)
-  if (blockIdx.x == 0 && threadIdx.x == 0) pc->launches = (unsigned int)t;
-  for (int o = 0; o < nown; ++o)
-    if (own[o] == sD[o].item_begin && threadIdx.x == 0) *sD[o].st = sS[o];
-}
-
 // ------------------------------------------------- power-step loop -----
 // The power method as a graph loop whose body is kPowerUnroll launches of
 // power_step_kernel and one of power_settle_kernel.  No launch finalizes its
@@ -2413,6 +2311,157 @@ __global__ void __launch_bounds__(32)
       if (signal) cudaGraphSetConditional(h, more ? 1u : 0u);
     }
   }
+}
+
+// ------------------------------------------------ persistent power loop -----
+// Every power-method phase of a run's large instances in one cooperative
+// launch, a bounded grid barrier as the phase boundary, with the power-step
+// loop's overlap: a phase's reduction and state update run in one extra warp
+// while the row warps already form the next phase's matrix products.
+//
+// Each CTA owns up to kPowOwn items (item b, b + grid, ...; the host sizes
+// the grid so that the CTAs own equally many) and keeps their desc and state
+// in shared memory for the whole loop.  Phase t: the reduction warp applies
+// phase t-1's item partials to each owned item's copy of the state (the
+// launch form's finalize order, warp_item_sums) while the row warps form the
+// first owned item's raw product A src with the source the advanced state
+// will name; then each owned item in a power phase finishes its rows with
+// the advanced state (scale, store, partials of phase t, double-buffered by
+// phase parity).  Every copy advances from the same sums in the same order as
+// the launch form, so results are bitwise those of the launch form.  The loop
+// ends after the first phase in which no instance had rows (each CTA with
+// rows publishes the phase with atomicMax before the barrier), or after
+// `limit` phases; then the CTA owning an instance's first item writes its
+// state back.
+// The reduction warp's work for one owned item: S advanced by the partials
+// pp.  Not inlined, so that its sums do not take registers from the rows.
+__device__ __noinline__ void persistent_apply(const InstDesc &D, InstState &S, const double *pp,
+                                              int lane, double2 *stage) {
+  double s2[2];
+  warp_item_sums(pp, D.nitems, lane, stage, s2);
+  __syncwarp();
+  if (lane == 0) advance_power_sums(D, S, s2);
+  __syncwarp();
+}
+
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kStepThreads, kMinBlocks)
+    power_persistent_kernel(EngineArgs args, PowCtl *pc, int limit) {
+  __shared__ InstDesc sD[kPowOwn];
+  __shared__ InstState sS[kPowOwn];
+  __shared__ RedBuf red;
+  __shared__ __align__(16) double2 sItems[kSumStage];
+  if (threadIdx.x == 0) g_staged = 0;
+  const int lane = threadIdx.x & 31;
+  const bool rw = threadIdx.x >= kThreads;  // the reduction warp
+  // owned items: blockIdx.x + o * gridDim.x, o < nown
+  const int nown = min(kPowOwn, (args.total_items - (int)blockIdx.x + (int)gridDim.x - 1) /
+                                    (int)gridDim.x);
+  for (int o = 0; o < nown; ++o) {
+    const int inst = instance_of(args.item_inst, args.item_prefix, args.ninst, (int)(blockIdx.x + o * gridDim.x));
+    const int *srcd = reinterpret_cast<const int *>(args.desc + inst);
+    int *dstd = reinterpret_cast<int *>(&sD[o]);
+    for (int w = threadIdx.x; w < (int)(sizeof(InstDesc) / 4); w += kStepThreads)
+      dstd[w] = ldro(srcd + w);
+    const int *srcs = reinterpret_cast<const int *>(args.states ? args.states + inst : nullptr);
+    int *dsts = reinterpret_cast<int *>(&sS[o]);
+    if (srcs)
+      for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kStepThreads)
+        dsts[w] = srcs[w];
+  }
+  __syncthreads();
+  if (!args.states) {  // the states live at the descs' home
+    for (int o = 0; o < nown; ++o) {
+      const int *srcs = reinterpret_cast<const int *>(sD[o].st);
+      int *dsts = reinterpret_cast<int *>(&sS[o]);
+      for (int w = threadIdx.x; w < (int)(sizeof(InstState) / 4); w += kStepThreads)
+        dsts[w] = srcs[w];
+    }
+    __syncthreads();
+  }
+  unsigned int pend = 0u;  // bit o: item o's rows ran in the previous phase
+  int t = 0;
+  for (;; ++t) {
+    const int par = t & 1;
+    // The first owned item's source vector, predicted from its state before
+    // the advance (the previous phase's output when rows ran there).
+    int src0 = kNoSrc;
+    if (nown > 0) {
+      const InstState &S0 = sS[0];
+      if (pend & 1u) {
+        if (S0.phase == PH_POW_RAND) src0 = B_W1;
+        else if (S0.phase == PH_POW) src0 = (S0.pow_k & 1) ? B_W1 : B_W;
+      } else if (S0.phase == PH_POW) {
+        src0 = S0.pow_src;
+      }
+    }
+    float wf[3] = {0.f, 0.f, 0.f};
+    double wd[3] = {0.0, 0.0, 0.0};
+    if (!rw && src0 != kNoSrc) {
+      const int slot = ((int)blockIdx.x - sD[0].item_begin) * kThreads + threadIdx.x;
+      if (slot < sD[0].nv) {
+        if (sD[0].prec == PREC_MIXED) pow_raw32(sD[0], src0, slot, wf);
+        else pow_raw64(sD[0], src0, slot, wd);
+      }
+    }
+    if (rw) {  // apply the previous phase's partials to every owned state
+      for (int o = 0; o < nown; ++o) {
+        if (!((pend >> o) & 1u)) continue;
+        persistent_apply(sD[o], sS[o], sD[o].part + (size_t)(par ^ 1) * sD[o].nitems * 2, lane,
+                         sItems);
+      }
+    }
+    __syncthreads();
+    unsigned int ran = 0u;
+    for (int o = 0; o < nown; ++o) {
+      const int phase = sS[o].phase;
+      if (!power_phase(phase)) continue;
+      ran |= 1u << o;
+      const InstDesc &D = sD[o];
+      const int local = (int)(blockIdx.x + o * gridDim.x) - D.item_begin;
+      const int slot = local * kThreads + threadIdx.x;
+      const bool row = !rw && slot < D.nv;
+      const bool f32 = D.prec == PREC_MIXED;
+      double part[2] = {0.0, 0.0};
+      if (row) {
+        const int v = D.A.rowmap ? ldro(D.A.rowmap + slot) : slot;
+        if (phase == PH_POW_RAND) {
+          row_power_rand(D, v, part);
+        } else {
+          const int src = sS[o].pow_src;
+          if (phase == PH_POW && (o > 0 || src != src0)) {  // not formed above
+            if (f32) pow_raw32(D, src, slot, wf);
+            else pow_raw64(D, src, slot, wd);
+          }
+          if (f32) row_power32_fin(D, sS[o], v, wf, part);
+          else row_power64_fin(D, sS[o], v, wd, part);
+        }
+      }
+      const double r = block_reduce_rows(part, red, nslots(phase));
+      if (threadIdx.x < 2) D.part[(size_t)par * D.nitems * 2 + 2 * (size_t)local + threadIdx.x] = r;
+    }
+    pend = ran;
+    if (ran && threadIdx.x == 0) atomicMax(&pc->busy, (unsigned int)(t + 1));
+    int unused;
+    if (!grid_barrier(args.ctl, args.wait_ns, unused)) return;
+    if (*(volatile unsigned int *)&pc->busy < (unsigned int)(t + 1)) break;  // no rows anywhere
+    if (t + 1 >= limit) {  // the last phase's partials, then stop
+      if (rw) {
+        for (int o = 0; o < nown; ++o) {
+          if (!((pend >> o) & 1u)) continue;
+          persistent_apply(sD[o], sS[o], sD[o].part + (size_t)par * sD[o].nitems * 2, lane,
+                           sItems);
+        }
+      }
+      __syncthreads();
+      ++t;
+      break;
+    }
+  }
+  // the working phases run (the launch form's launch count)
+  if (blockIdx.x == 0 && threadIdx.x == 0) pc->launches = (unsigned int)t;
+  for (int o = 0; o < nown; ++o)
+    if ((int)(blockIdx.x + o * gridDim.x) == sD[o].item_begin && threadIdx.x == 0) *sD[o].st = sS[o];
 }
 
 // ---------------------------------------------------- cluster solver -----
@@ -2860,10 +2909,11 @@ cudaError_t launch_power_persistent(const EngineArgs &args, PowCtl *d_pc, int li
                                     cudaStream_t stream) {
   void *params[] = {(void *)&args, (void *)&d_pc, (void *)&limit};
   return cudaLaunchCooperativeKernel((const void *)power_persistent_kernel<4>, dim3(grid),
-                                     dim3(kThreads), params, 0, stream);
+                                     dim3(kStepThreads), params, 0, stream);
 }
 cudaError_t power_persistent_max_blocks_per_sm(int *n) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_persistent_kernel<4>, kThreads, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_persistent_kernel<4>, kStepThreads,
+                                                       0);
 }
 cudaError_t power_max_blocks_per_sm(int variant, int *n) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, power_kernel_fn(variant),

@@ -115,9 +115,8 @@ def _serve(srv, qps, opt_of, cap=200000):
 
 @pytest.mark.parametrize("lanes", [0, 3])
 def test_admission_waits_for_device_room(fresh_ctx, lanes):
-    """Room for one scene only (the reserve leaves 1.5 scenes of the device's
-    current room): the second new scene waits until the first is idle and
-    evicted, then both are solved."""
+    """Room for one scene only: the second new scene waits until the first is
+    idle and evicted, then both are solved."""
     ctx = fresh_ctx
     qps = [corner(24, 24, 48, seed=s) for s in (1, 2)]
     mixed = lambda q: opts(q, precision=M.PREC_MIXED)  # noqa: E731
@@ -132,8 +131,11 @@ def test_admission_waits_for_device_room(fresh_ctx, lanes):
     one = before - ctx.room()
     srv.close()
     assert one > 0
+    # admission asks for the footprint estimate `need`; after the first scene
+    # the room is `one` smaller, so the reserve lets exactly one scene in
+    need = M.lib().mprgp_problem_bytes(qps[0].nv, qps[0].nnzb, len(qps[0].planes), 3)
     srv = M.Server(ctx, quantum_phases=-1, power_launches=1003, lanes=lanes,
-                   hbm_reserve=ctx.room() - int(1.5 * one))
+                   hbm_reserve=ctx.room() - need - one // 2)
     codes, max_scenes = _serve(srv, qps, mixed)
     srv.close()
     assert codes == {0: 0, 1: 0}
