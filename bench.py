@@ -149,6 +149,29 @@ def vector_bytes(st, qp, mixed, include_power=True):
     return int(k * n8 + PLANE_ROW_BYTES * m * (cg + 2 * ex + pr + other))
 
 
+def read_stream_peak():
+    """Read-only HBM throughput measured here and now: torch's sum over a
+    1 GiB FP32 buffer, L2 flushed before each of 6 timed runs, best run.  A
+    matrix pass reads far more than it writes, so its fraction of this figure
+    says how close it is to the stream it is bound by (the copy peak counts
+    read and write bytes alike)."""
+    import torch
+    x = torch.ones(256 << 20, dtype=torch.float32, device="cuda")
+    fl = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e30
+    for r in range(7):
+        fl.fill_(r)
+        e0.record()
+        x.sum()
+        e1.record()
+        e1.synchronize()
+        if r:
+            best = min(best, e0.elapsed_time(e1))
+    del x, fl
+    return round(4.0 * (256 << 20) / best / 1e6, 1)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -353,6 +376,7 @@ def run_gb300(args):
     passes = sum(s.power_passes for s in stats)
     power_ms = power1 - power0
     peak, peak_kind = measured_peaks()
+    read_peak = read_stream_peak()
     all_bytes = sum(s.spmv_fp64 * spmv_bytes(qp, 8) + s.spmv_fp32 * spmv_bytes(qp, 4)
                     for s in stats)
     eng_bytes = all_bytes - passes * pass_bytes
@@ -396,6 +420,7 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": dominant,
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "read_peak": read_peak, "frac_of_read_peak": round(achieved / read_peak, 4),
                      "traffic": traffic, "bytes_per_launch": int(pass_bytes),
                      "launch_ms": round(pow_launch_ms, 5), "launches": int(passes),
                      "share_of_solve": round(power_ms / max(1e-9, solver1 - solver0), 3)
@@ -1062,6 +1087,7 @@ def run_serve(args):
     # is capped by the windows' own device time
     solver_ms = min(sum(r.solver_ms for r in timed), local_ms)
     peak, peak_kind = measured_peaks()
+    read_peak = read_stream_peak()
     achieved = (alg + vec) / (solver_ms / 1e3) / 1e9
     launches = sum(r.launches for r in timed)
     its = [st.iterations for st in timed[0].stats]
@@ -1102,7 +1128,11 @@ def run_serve(args):
                                "engine's MPRGP phases; no single one dominates the stream)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "traffic": None,
+                     "read_peak": read_peak, "frac_of_read_peak": round(achieved / read_peak, 4),
+                     "traffic": committed_traffic("c4", "mixed" if mixed else "plain", "window"),
+                     "traffic_unit": "DRAM bytes read + written per window (ncu launch list, "
+                                     "profiles/dram_traffic_c4_serving.md)",
+                     "bytes_per_window": int((alg + vec) / len(timed)),
                      "bytes_per_launch": int((alg + vec) / max(1, launches)),
                      "launch_ms": round(solver_ms / max(1, launches), 5),
                      "bytes_matrix_per_step": int(alg / len(timed)),
