@@ -74,6 +74,8 @@ def parse():
                          "small/large lanes, 3 plus a lane for the large ones' power method)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the launch-shape autotuner (mprgp_gb300.autotune) before warm-up")
+    ap.add_argument("--ctas-per-sm", type=int, default=0,
+                    help="with --tuning: cap on the persistent grid's CTAs per SM (0 = all resident)")
     ap.add_argument("--single", action="store_true",
                     help="c3: one solve of the timestep beam's first QP (the c0/c1 line) instead "
                          "of the 20-timestep loop")
@@ -254,7 +256,7 @@ def autotune_ctx(args, ctx, sample, precision, power_cache=False, fixed=None):
     explicit --tuning wins).  power_cache: tune the solves that reuse a first
     solve's power method (timestep loops)."""
     if args.tuning is not None:
-        ctx.set_tuning(args.tuning, 0)
+        ctx.set_tuning(args.tuning, args.ctas_per_sm)
         return {"explicit_tuning_bits": args.tuning}
     if args.no_autotune:
         return None

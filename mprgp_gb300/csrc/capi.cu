@@ -831,7 +831,12 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   args.pst[1] = L.d_st + 2 * (size_t)L.cap;
   int per_sm = stage ? c->bps_stage : c->bps;
   if (c->ctas_per_sm > 0) per_sm = std::min(per_sm, c->ctas_per_sm);
-  const int grid = std::max(1, std::min(prefix[n_large], c->nsm * per_sm));
+  // Equally many items per CTA: a phase ends with its busiest CTA, so the
+  // grid is the fewest CTAs that give each the same count (c3's 1,360 items:
+  // 454 CTAs of 3, not 608 of 2 or 3).
+  const int e_cap = std::max(1, c->nsm * per_sm);
+  const int e_per = std::max(1, (prefix[n_large] + e_cap - 1) / e_cap);
+  const int grid = std::max(1, (prefix[n_large] + e_per - 1) / e_per);
 
   // The power method first (at most 1003 phases: the seeded start, 1001
   // iterations, the last difference), as a device-driven loop of launches of
