@@ -1739,6 +1739,37 @@ __device__ double block_reduce(double *part, RedBuf &red, int ns, bool with_min)
   return r;
 }
 
+// The finalize of an instance's item partials (stride kPart) with one warp
+// per slot and no block barrier: lane l of warp k forms what threads l,
+// l+32, ..., l+224 of the block form hold (each the identity plus its items
+// t, t+256, ..., in that order), adds them in block_reduce's order and closes
+// with the same shuffle tree -- block_reduce's operations in its order, so
+// the sums are bitwise the block form's.  For instances of up to kThreads
+// items (one item per thread at most).  Writes sums[0..kPart) (the slots the
+// phase does not produce as 0.0); the caller syncs before reading them.
+__device__ void warp_finalize(const double *pp, int nitems, int ns, bool wmin, double *sums) {
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int nrows = ns + (wmin ? 1 : 0);
+  if (threadIdx.x < kPart && threadIdx.x >= ns && !(wmin && threadIdx.x == kMinSlot))
+    sums[threadIdx.x] = 0.0;
+  if (wp >= nrows) return;
+  const bool is_min = wmin && wp == ns;
+  const int k = is_min ? kMinSlot : wp;
+  double a = 0.0;
+#pragma unroll
+  for (int i = 0; i < kThreads / 32; ++i) {
+    const int t = lane + 32 * i;
+    double th = is_min ? DBL_MAX : 0.0;
+    if (t < nitems) {
+      const double x = pp[(size_t)t * kPart + k];
+      th = is_min ? fmin(th, x) : th + x;
+    }
+    a = (i == 0) ? th : (is_min ? fmin(a, th) : a + th);
+  }
+  a = is_min ? warp_min(a) : warp_sum(a);
+  if (lane == 0) sums[k] = a;
+}
+
 // Bounded grid barrier in the style of cooperative groups' grid sync:
 // arrival is an acq_rel atomic, the last CTA publishes the next generation
 // with a release store, the others poll it with acquire loads (bounded by
@@ -1886,19 +1917,23 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kern
       }
       __syncthreads();
       if (s_last) {
-        double acc[kPart];
+        if (sD.nitems <= kThreads) {
+          warp_finalize(sD.part, sD.nitems, ns, wmin, sums);
+        } else {
+          double acc[kPart];
 #pragma unroll
-        for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-        for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
+          for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+          for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
 #pragma unroll
-          for (int k = 0; k < kPart; ++k) {
-            if (k == kMinSlot ? !wmin : k >= ns) continue;
-            const double x = sD.part[(size_t)it * kPart + k];
-            acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+            for (int k = 0; k < kPart; ++k) {
+              if (k == kMinSlot ? !wmin : k >= ns) continue;
+              const double x = sD.part[(size_t)it * kPart + k];
+              acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+            }
           }
+          const double t = block_reduce(acc, red, ns, wmin);
+          if (threadIdx.x < kPart) sums[threadIdx.x] = t;
         }
-        const double t = block_reduce(acc, red, ns, wmin);
-        if (threadIdx.x < kPart) sums[threadIdx.x] = t;
         __syncthreads();
         if (threadIdx.x == 0) {
           InstState S = sS;
@@ -1992,19 +2027,23 @@ __device__ __forceinline__ void phase_item(const EngineArgs &args, int item, Pow
   }
   __syncthreads();
   if (!s_last) return;
-  double acc[kPart];
+  if (sD.nitems <= kThreads) {
+    warp_finalize(sD.part, sD.nitems, ns, wmin, sums);
+  } else {
+    double acc[kPart];
 #pragma unroll
-  for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
-  for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
+    for (int k = 0; k < kPart; ++k) acc[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
+    for (int it = threadIdx.x; it < sD.nitems; it += kThreads) {
 #pragma unroll
-    for (int k = 0; k < kPart; ++k) {
-      if (k == kMinSlot ? !wmin : k >= ns) continue;
-      const double x = sD.part[(size_t)it * kPart + k];
-      acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+      for (int k = 0; k < kPart; ++k) {
+        if (k == kMinSlot ? !wmin : k >= ns) continue;
+        const double x = sD.part[(size_t)it * kPart + k];
+        acc[k] = (k == kMinSlot) ? fmin(acc[k], x) : acc[k] + x;
+      }
     }
+    const double t = block_reduce(acc, red, ns, wmin);
+    if (threadIdx.x < kPart) sums[threadIdx.x] = t;
   }
-  const double t = block_reduce(acc, red, ns, wmin);
-  if (threadIdx.x < kPart) sums[threadIdx.x] = t;
   __syncthreads();
   if (threadIdx.x == 0) {
     InstState S = sS;

@@ -139,3 +139,37 @@ def test_one_warp_cross_cta_reduction_is_the_block_reduction(nitems, is_min):
         vals[1] = -0.0  # the identity terms keep what the block reduction does with it
     got, want = one_warp_of_items(vals, is_min), block_reduce_of_items(vals, is_min)
     assert np.float64(got).tobytes() == np.float64(want).tobytes()
+
+
+def warp_finalize_of_items(vals, is_min=False):
+    """warp_finalize (the engine's and the phase kernel's finalize for up to
+    256 items): lane l forms, for i = 0..7, the value thread l + 32 i holds
+    in the block form (the identity, plus item l + 32 i when there is one)
+    and adds them in that order, then the tree."""
+    ident = np.finfo(np.float64).max if is_min else 0.0
+    a = np.zeros(32)
+    for lane in range(32):
+        acc = None
+        for i in range(K_THREADS // 32):
+            t = lane + 32 * i
+            th = ident
+            if t < len(vals):
+                th = min(th, vals[t]) if is_min else th + vals[t]
+            acc = th if i == 0 else (min(acc, th) if is_min else acc + th)
+        a[lane] = acc
+    if is_min:
+        v = a.copy()
+        for o in (16, 8, 4, 2, 1):
+            v = np.minimum(v, v[np.arange(32) ^ o])
+        return v[0]
+    return warp_sum(a)
+
+
+@pytest.mark.parametrize("nitems", [1, 17, 32, 33, 100, 255, 256])
+@pytest.mark.parametrize("is_min", [False, True])
+def test_warp_finalize_is_the_block_finalize(nitems, is_min):
+    vals = list(_partials(nitems)[:, 0])
+    if nitems > 40:
+        vals[40] = -0.0
+    got, want = warp_finalize_of_items(vals, is_min), block_reduce_of_items(vals, is_min)
+    assert np.float64(got).tobytes() == np.float64(want).tobytes()
