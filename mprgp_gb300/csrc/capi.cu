@@ -39,6 +39,7 @@ void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const doubl
                         float *out32, double *dinv, int *bad, cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, unsigned char *unit, cudaStream_t st);
+void launch_planes_axis(int m, const double *in, unsigned char *axis, cudaStream_t st);
 void launch_state_scatter(const InstDesc *desc, int n, InstState *states, InstState *const *home,
                           const int *fresh, cudaStream_t st);
 void launch_state_gather(const InstDesc *desc, int n, InstState *states, InstState *const *home,
@@ -142,6 +143,7 @@ struct mprgp_problem {
   int *plane_ptr = nullptr;
   double *planes_raw = nullptr, *planes = nullptr, *pl_nn = nullptr, *pl_indn = nullptr;
   unsigned char *pl_unit = nullptr;  // per vertex: its planes are orthonormal
+  unsigned char *pl_axis = nullptr;  // per plane row: its normal's unit axis (3: none)
   double *L = nullptr, *U = nullptr;
   unsigned char *face = nullptr;
   int face_len = 0;
@@ -233,7 +235,7 @@ int nitems_of(int nv) { return (nv + kThreads - 1) / kThreads; }
 void free_problem_arrays(mprgp_problem *p) {
   dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
   dfree(p->ctx, p->dinv); dfree(p->ctx, p->b); dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw);
-  dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->pl_unit); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
+  dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->pl_unit); dfree(p->ctx, p->pl_axis); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
   dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->bad); dfree(p->ctx, p->st);
   dfree(p->ctx, p->trace); dfree(p->ctx, p->stage_ptr); dfree(p->ctx, p->stage_cols); dfree(p->ctx, p->stage_vals);
   dfree(p->ctx, p->rowmap);
@@ -379,6 +381,11 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
     launch_planes_setup(p->nv, p->plane_ptr, p->planes_raw, p->planes, p->pl_nn, p->pl_indn,
                         p->dinv, p->pl_unit, st);
     CK(cudaGetLastError());
+    if (p->m > 0) {
+      p->ctx->launches++;
+      launch_planes_axis(p->m, p->planes_raw, p->pl_axis, st);
+      CK(cudaGetLastError());
+    }
     p->planes_dirty = 0;
   }
   std::memset(d, 0, sizeof(*d));
@@ -406,6 +413,7 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->pl_nn = p->pl_nn;
   d->pl_indn = p->pl_indn;
   d->pl_unit = p->pl_unit;
+  d->pl_axis = (p->cons == 1 && p->m > 0) ? p->pl_axis : nullptr;
   d->L = p->L;
   d->U = p->U;
   d->face = p->face;
@@ -1229,7 +1237,7 @@ size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {
   if (precisions & 2) by += slots * kSlice * 9 * 4;
   const size_t n = 3 * (size_t)nv;
   by += n * 8 * (kNumBuf + 3) + n * 4 * kNumBuf32;  // vectors, dinv, b, ev, FP32 shadows
-  by += (size_t)nplanes * (8 * 4 * 2 + 8 * 2 + 1) + (size_t)(nv + 1) * 4 + n * 16 + n;
+  by += (size_t)nplanes * (8 * 4 * 2 + 8 * 2 + 2) + (size_t)(nv + 1) * 4 + n * 16 + n;
   by += (size_t)nitems_of(nv) * kPart * 8 * 2 + sizeof(InstState) + 64;
   by += (size_t)nnzb * (9 * 8 + 4) + (size_t)(nv + 1) * 4 + (size_t)nv * 4;  // BSR copy, rowmap
   return by;
@@ -1344,13 +1352,14 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
   cudaStream_t s = p->ctx->stream;
   if (m != p->m || p->cons != 1) {
     dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw); dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn);
-    dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->face);
+    dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->pl_axis); dfree(p->ctx, p->face);
     int rc = dalloc(p->ctx, &p->plane_ptr, nv + 1);
     if (!rc) rc = dalloc(p->ctx, &p->planes_raw, 4 * (size_t)std::max(m, 1));
     if (!rc) rc = dalloc(p->ctx, &p->planes, 4 * (size_t)std::max(m, 1));
     if (!rc) rc = dalloc(p->ctx, &p->pl_nn, (size_t)std::max(m, 1));
     if (!rc) rc = dalloc(p->ctx, &p->pl_indn, (size_t)std::max(m, 1));
     if (!rc && !p->pl_unit) rc = dalloc(p->ctx, &p->pl_unit, (size_t)nv);
+    if (!rc) rc = dalloc(p->ctx, &p->pl_axis, (size_t)std::max(m, 1));
     if (!rc) rc = dalloc(p->ctx, &p->face, (size_t)std::max(m, 1));
     if (rc) return rc;
   }

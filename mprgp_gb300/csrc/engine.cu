@@ -411,17 +411,24 @@ __device__ __forceinline__ void spmv_any(const InstDesc &D, bool fp32, int slot,
 // --------------------------------------------------- vertex constraints --
 struct VCons {
   int k, base, unit;  // unit: the planes' Gram matrix is the identity (k >= 2)
+  int ax;             // 2 bits per plane: 0..2 the normal is that unit axis, 3 any other
   double n[kMaxPlanes][3], c[kMaxPlanes], inn[kMaxPlanes], indn[kMaxPlanes];
   double lo[3], hi[3];
 };
 
 __device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
   C.unit = 0;
+  C.ax = 0x3f;
   if (D.kind >= KIND_DECOUPLED) {
     const int b = ldro(D.plane_ptr + v), e = ldro(D.plane_ptr + v + 1);
     C.base = b;
     C.k = e - b;
     if (D.pl_unit && C.k >= 2) C.unit = D.pl_unit[v];
+    if (D.pl_axis) {
+#pragma unroll
+      for (int j = 0; j < kMaxPlanes; ++j)
+        if (j < C.k) C.ax = (C.ax & ~(3 << (2 * j))) | ((int)(__ldg(D.pl_axis + b + j) & 3) << (2 * j));
+    }
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
       if (j < C.k) {
@@ -449,6 +456,50 @@ __device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
   }
 }
 
+// Plane products.  A plane whose normal is a unit axis vector (floor and
+// walls) needs no FP64 work for them: n.v is one component of v, v += n s
+// changes one component, and 1/|n|^2 is 1.  The results are the general
+// forms' (0 * v_d and v_d + 0 * s leave v_d's value; only the sign of an
+// exact zero can differ), and every GPU path uses these same functions.
+__device__ __forceinline__ int ax_of(const VCons &C, int j) { return (C.ax >> (2 * j)) & 3; }
+__device__ __forceinline__ double ndot(const VCons &C, int j, const double v[3]) {
+  const int a = ax_of(C, j);
+  if (a == 3) return dot3(C.n[j], v);
+  return a == 0 ? v[0] : (a == 1 ? v[1] : v[2]);
+}
+// x / |n_j|^2 (C.inn is 1/|n|^2; exactly 1 for a unit axis)
+__device__ __forceinline__ double ninn(const VCons &C, int j, double x) {
+  return ax_of(C, j) == 3 ? x * C.inn[j] : x;
+}
+// v += n_j s
+__device__ __forceinline__ void nadd(const VCons &C, int j, double s, double v[3]) {
+  const int a = ax_of(C, j);
+  if (a == 3) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] += C.n[j][d] * s;
+  } else if (a == 0) {
+    v[0] += s;
+  } else if (a == 1) {
+    v[1] += s;
+  } else {
+    v[2] += s;
+  }
+}
+// v -= n_j s
+__device__ __forceinline__ void nsub(const VCons &C, int j, double s, double v[3]) {
+  const int a = ax_of(C, j);
+  if (a == 3) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] -= C.n[j][d] * s;
+  } else if (a == 0) {
+    v[0] -= s;
+  } else if (a == 1) {
+    v[1] -= s;
+  } else {
+    v[2] -= s;
+  }
+}
+
 // Face codes of the vertex's constraint rows, 2 bits each.
 __device__ __forceinline__ int load_face(const InstDesc &D, const VCons &C) {
   int f = 0;
@@ -469,7 +520,7 @@ __device__ __forceinline__ int decide_face(const InstDesc &D, const VCons &C, co
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
       if (j < C.k) {
-        const int a = fabs(dot3(C.n[j], x) - C.c[j]) < kEps ? 1 : 0;
+        const int a = fabs(ndot(C, j, x) - C.c[j]) < kEps ? 1 : 0;
         f |= a << (2 * j);
         cnt += a;
         D.face[C.base + j] = (unsigned char)a;
@@ -630,21 +681,21 @@ __device__ void project_v(const InstDesc &D, const VCons &C, const double x[3], 
     double lam[kMaxPlanes];
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
-      lam[j] = (j < C.k) ? fmax((C.c[j] - dot3(C.n[j], x)) * C.inn[j], 0.0) : 0.0;
+      lam[j] = (j < C.k) ? fmax(ninn(C, j, C.c[j] - ndot(C, j, x)), 0.0) : 0.0;
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k)
-        for (int d = 0; d < 3; ++d) y[d] += C.n[j][d] * lam[j];
+        nadd(C, j, lam[j], y);
   } else if (D.kind == KIND_PLANES) {
     if (C.k == 0) return;
     if (C.k == 1) {  // one constraint: the QP's solution is max(q, 0) / |n|^2
-      const double l = fmax((C.c[0] - dot3(C.n[0], x)) * C.inn[0], 0.0);
-      for (int d = 0; d < 3; ++d) y[d] += C.n[0][d] * l;
+      const double l = fmax(ninn(C, 0, C.c[0] - ndot(C, 0, x)), 0.0);
+      nadd(C, 0, l, y);
       return;
     }
     double G[3][3], q[3], lam[3];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) q[j] = (j < C.k) ? C.c[j] - dot3(C.n[j], x) : 0.0;
+    for (int j = 0; j < 3; ++j) q[j] = (j < C.k) ? C.c[j] - ndot(C, j, x) : 0.0;
     if (C.unit) unit_qp3(q, (1 << C.k) - 1, lam);  // what nonneg_qp3 returns for G = I
     else {
       gram(C, G);
@@ -653,7 +704,7 @@ __device__ void project_v(const InstDesc &D, const VCons &C, const double x[3], 
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       if (j < C.k)
-        for (int d = 0; d < 3; ++d) y[d] += C.n[j][d] * lam[j];
+        nadd(C, j, lam[j], y);
   } else {
 #pragma unroll
     for (int d = 0; d < 3; ++d) y[d] = fmin(fmax(x[d], C.lo[d]), C.hi[d]);
@@ -670,11 +721,11 @@ __device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3
     double lam[kMaxPlanes];
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
-      lam[j] = (j < C.k && fcode(f, j)) ? -dot3(C.n[j], g) * C.inn[j] : 0.0;
+      lam[j] = (j < C.k && fcode(f, j)) ? ninn(C, j, -ndot(C, j, g)) : 0.0;
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k)
-        for (int d = 0; d < 3; ++d) phi[d] += C.n[j][d] * lam[j];
+        nadd(C, j, lam[j], phi);
   } else if (D.kind == KIND_PLANES) {
     int act = 0;
 #pragma unroll
@@ -683,13 +734,13 @@ __device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3
     if (!act) return;
     if (__popc(act) == 1) {
       const int j = __ffs(act) - 1;
-      const double l = -dot3(C.n[j], g) * C.inn[j];
-      for (int d = 0; d < 3; ++d) phi[d] += C.n[j][d] * l;
+      const double l = ninn(C, j, -ndot(C, j, g));
+      nadd(C, j, l, phi);
       return;
     }
     double G[3][3], q[3], lam[3];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? -dot3(C.n[j], g) : 0.0;
+    for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? -ndot(C, j, g) : 0.0;
     if (C.unit) {  // what solve_subset returns for G = I
 #pragma unroll
       for (int j = 0; j < 3; ++j) lam[j] = (act & (1 << j)) ? q[j] : 0.0;
@@ -700,7 +751,7 @@ __device__ void phi_v(const InstDesc &D, const VCons &C, int f, const double g[3
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       if (act & (1 << j))
-        for (int d = 0; d < 3; ++d) phi[d] += C.n[j][d] * lam[j];
+        nadd(C, j, lam[j], phi);
   } else {
 #pragma unroll
     for (int d = 0; d < 3; ++d)
@@ -717,14 +768,14 @@ __device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[
     double lam[kMaxPlanes];
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
-      double l = (j < C.k) ? dot3(C.n[j], beta) : 0.0;
-      if (j < C.k && fcode(f, j)) l = fmax(0.0, l * C.inn[j]);
+      double l = (j < C.k) ? ndot(C, j, beta) : 0.0;
+      if (j < C.k && fcode(f, j)) l = fmax(0.0, ninn(C, j, l));
       lam[j] = l;  // rows off the face keep (J beta)_i, as the reference does
     }
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
       if (j < C.k)
-        for (int d = 0; d < 3; ++d) beta[d] -= C.n[j][d] * lam[j];
+        nsub(C, j, lam[j], beta);
   } else if (D.kind == KIND_PLANES) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) beta[d] = g[d] - phi[d];
@@ -735,13 +786,13 @@ __device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[
     if (!act) return;
     if (__popc(act) == 1) {
       const int j = __ffs(act) - 1;
-      const double l = fmax(dot3(C.n[j], beta), 0.0) * C.inn[j];
-      for (int d = 0; d < 3; ++d) beta[d] -= C.n[j][d] * l;
+      const double l = ninn(C, j, fmax(ndot(C, j, beta), 0.0));
+      nsub(C, j, l, beta);
       return;
     }
     double G[3][3], q[3], lam[3];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? dot3(C.n[j], beta) : 0.0;
+    for (int j = 0; j < 3; ++j) q[j] = (act & (1 << j)) ? ndot(C, j, beta) : 0.0;
     if (C.unit) unit_qp3(q, act, lam);
     else {
       gram(C, G);
@@ -751,7 +802,7 @@ __device__ void beta_v(const InstDesc &D, const VCons &C, int f, const double g[
 #pragma unroll
     for (int j = 0; j < 3; ++j)
       if (act & (1 << j))
-        for (int d = 0; d < 3; ++d) gp[d] += C.n[j][d] * (-lam[j]);
+        nadd(C, j, -lam[j], gp);
     beta[0] = gp[0];
     beta[1] = gp[1];
     beta[2] = gp[2];
@@ -789,8 +840,8 @@ __device__ void precond_v(const InstDesc &D, const VCons &C, int f, int v, const
 #pragma unroll
   for (int j = 0; j < kMaxPlanes; ++j) {
     if (j < C.k && fcode(f, j)) {
-      const double lam = C.indn[j] * dot3(C.n[j], Dg);
-      for (int d = 0; d < 3; ++d) t[d] += C.n[j][d] * lam;
+      const double lam = C.indn[j] * ndot(C, j, Dg);
+      nadd(C, j, lam, t);
     }
   }
 #pragma unroll
@@ -824,7 +875,7 @@ __device__ __forceinline__ int infeasible_v(const InstDesc &D, const VCons &C, c
   if (D.kind >= KIND_DECOUPLED) {
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j)
-      if (j < C.k && dot3(C.n[j], y) < C.c[j] - kEps) return 1;
+      if (j < C.k && ndot(C, j, y) < C.c[j] - kEps) return 1;
     return 0;
   }
 #pragma unroll
@@ -842,7 +893,7 @@ __device__ double ratio_v(const InstDesc &D, const VCons &C, const double x[3], 
 #pragma unroll
     for (int j = 0; j < kMaxPlanes; ++j) {
       if (j >= C.k) continue;
-      const double jd = dot3(C.n[j], p), jx = dot3(C.n[j], x);
+      const double jd = ndot(C, j, p), jx = ndot(C, j, x);
       if (jd > kEps && jx > C.c[j]) r = fmin(r, (jx - C.c[j]) / jd);
     }
     return r;
@@ -2724,6 +2775,19 @@ __global__ void planes_setup_kernel(int nv, const int *__restrict__ plane_ptr,
   }
 }
 
+// Axis code of every plane row: d when its normal (raw, before the sign
+// change of the offset) is exactly the unit vector e_d, else 3.
+__global__ void planes_axis_kernel(int m, const double *__restrict__ in, unsigned char *axis) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const double n0 = in[4 * (size_t)q], n1 = in[4 * (size_t)q + 1], n2 = in[4 * (size_t)q + 2];
+  unsigned char a = 3;
+  if (n0 == 1.0 && n1 == 0.0 && n2 == 0.0) a = 0;
+  else if (n0 == 0.0 && n1 == 1.0 && n2 == 0.0) a = 1;
+  else if (n0 == 0.0 && n1 == 0.0 && n2 == 1.0) a = 2;
+  axis[q] = a;
+}
+
 // Standalone y = A x (FixedSparseMatrix::multiply, MPRGPSolver.h:469-473).
 template <typename VT>
 __global__ void __launch_bounds__(256, MPRGP_SPMV_MIN_BLOCKS) spmv_kernel(SellMatrix A, const VT *__restrict__ vals,
@@ -2971,6 +3035,9 @@ void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double 
                          double *indn, const double *dinv, unsigned char *unit, cudaStream_t st) {
   planes_setup_kernel<<<(nv + 255) / 256, 256, 0, st>>>(nv, plane_ptr, in, out, nn, indn, dinv,
                                                         unit);
+}
+void launch_planes_axis(int m, const double *in, unsigned char *axis, cudaStream_t st) {
+  if (m > 0) planes_axis_kernel<<<(m + 255) / 256, 256, 0, st>>>(m, in, axis);
 }
 void launch_spmv(const SellMatrix &A, int nv, bool fp32, const double *x, double *y,
                  cudaStream_t st) {

@@ -105,6 +105,8 @@ struct InstDesc {
   const double *pl_nn;        // 1 / |n|^2 = 1 / diag(J J^T)
   const double *pl_indn;      // 1 / (n . D^-1 n) = 1 / diag(J D^-1 J^T)
   const unsigned char *pl_unit;  // per vertex: 2-3 planes whose Gram matrix is the identity
+  const unsigned char *pl_axis;  // per plane row: 0..2 its normal is that unit axis, 3 other
+                                 // (nullptr: every normal takes the general products)
   const double *L, *U;        // bounds kinds
   unsigned char *face;        // one per constraint row / per unknown
   double *buf[kNumBuf];
