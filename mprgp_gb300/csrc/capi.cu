@@ -103,7 +103,13 @@ constexpr int kLanes = 7;  // 0: synchronous calls; 1..6: the server's asynchron
 
 struct mprgp_context {
   int device = 0;
+  // Uploads and setup kernels; the highest priority the device offers, so
+  // that the few CTAs of a setup kernel are placed before the pending CTAs of
+  // a lane's long runs (the lanes' runs wait for this stream's work).
   cudaStream_t stream = nullptr;
+  // Device-to-host reads that must not wait for the context stream: results
+  // of a lane run that has ended, and offsets read from caller device arrays.
+  cudaStream_t io = nullptr;
   int nsm = 0, bps = 0, bps_stage = 0;
   int stage = 0;         // stage FP32 A in shared memory (1) or not (0)
   int power_kernel = 1;  // power method by the dedicated kernel (1) or the engine (0)
@@ -121,6 +127,7 @@ struct mprgp_context {
   int cluster_items = 1; // items per CTA allowed in the largest cluster (1..kClusterItems)
   int cluster_ok[kClusterClasses] = {0, 0, 0, 0, 0};  // cluster sizes 1, 2, 4, 8, 16 usable
   int ctas_per_sm = 0;   // persistent CTAs per SM (0 = all resident)
+  size_t l2_bytes = 0;   // the device's L2 size
   cudaMemPool_t pool = nullptr;      // every device array of the context's problems
   mprgp_problem *scratch = nullptr;
   int bps_power = 0;
@@ -762,6 +769,17 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
     phase_bound = std::max(phase_bound, 1100LL + 8LL * ((long long)opts[i].max_it + 2));
   }
   if (wait_s <= 0.0) wait_s = 5.0;
+  {
+    // The large instances' matrix bytes per pass (FP32 values in the mixed
+    // form): beyond three quarters of L2 the run streams them evict-first.
+    size_t mbytes = 0;
+    for (int i = 0; i < n; ++i)
+      if (R.pos[i] < n_large)
+        mbytes += (size_t)probs[i]->slots * kSlice *
+                  (9 * (desc[R.pos[i]].prec == PREC_MIXED ? 4 : 8) + 4);
+    const int stream_l2 = mbytes > c->l2_bytes / 4 * 3 ? 1 : 0;
+    for (int j = 0; j < n_large; ++j) desc[j].A.stream_l2 = stream_l2;
+  }
   for (int i = 0; i < n; ++i) {
     if (!fresh[i]) continue;
     mprgp_problem *p = probs[i];
@@ -935,6 +953,21 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   R.cluster_quantum = cluster_quantum;
   R.power_launches = power_launches;
   R.active = true;
+  return MPRGP_OK;
+}
+
+// Copies a problem's solution (3 nv doubles) and face codes into host
+// memory after an engine run that used it has ended (engine_end), on the
+// read stream: unlike mprgp_problem_get_x, it does not wait for uploads and
+// setup kernels queued on the context stream for other problems meanwhile.
+int problem_read_result(mprgp_problem *p, double *x, unsigned char *face) {
+  mprgp_context *c = p->ctx;
+  const size_t n = 3 * (size_t)p->nv;
+  CK(cudaMemcpyAsync(x, p->vec + (size_t)(B_X0 + p->xc) * n, sizeof(double) * n,
+                     cudaMemcpyDeviceToHost, c->io));
+  if (face && p->face_len > 0)
+    CK(cudaMemcpyAsync(face, p->face, p->face_len, cudaMemcpyDeviceToHost, c->io));
+  CK(cudaStreamSynchronize(c->io));
   return MPRGP_OK;
 }
 
@@ -1114,13 +1147,23 @@ int mprgp_context_create(int device, mprgp_context **out) {
   auto *c = new mprgp_context();
   c->device = device;
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+  {
+    int l2 = 0;
+    CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device));
+    c->l2_bytes = (size_t)l2;
+  }
   CK(engine_max_blocks_per_sm(&c->bps, 0));
   CK(engine_max_blocks_per_sm(&c->bps_stage, kStageBytes));
   if (c->bps < 1) {
     delete c;
     return fail(MPRGP_NO_DEVICE, "engine kernel cannot be resident");
   }
-  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  {
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, greatest));
+  }
+  CK(cudaStreamCreateWithFlags(&c->io, cudaStreamNonBlocking));
   cudaMemPoolProps props;
   std::memset(&props, 0, sizeof(props));
   props.allocType = cudaMemAllocationTypePinned;
@@ -1159,6 +1202,7 @@ int mprgp_context_destroy(mprgp_context *c) {
   for (int k = kLanes - 1; k >= 0; --k) lane_free(c, c->lane[k]);
   cudaStreamSynchronize(c->stream);
   cudaStreamDestroy(c->stream);
+  if (c->io) cudaStreamDestroy(c->io);
   if (c->pool) cudaMemPoolDestroy(c->pool);
   delete c;
   return MPRGP_OK;
@@ -1284,7 +1328,8 @@ int mprgp_problem_set_matrix(mprgp_problem *p, int nnzb, const int *row_ptr, con
   const int nv = p->nv;
   std::vector<int> h_ptr(nv + 1);
   if (on_device) {
-    CK(cudaMemcpy(h_ptr.data(), row_ptr, sizeof(int) * (nv + 1), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(h_ptr.data(), row_ptr, sizeof(int) * (nv + 1), cudaMemcpyDeviceToHost, c->io));
+    CK(cudaStreamSynchronize(c->io));
   } else {
     std::memcpy(h_ptr.data(), row_ptr, sizeof(int) * (nv + 1));
   }
@@ -1340,8 +1385,13 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
   if (!p || !plane_ptr) return fail(MPRGP_INVALID, "set_planes");
   const int nv = p->nv;
   std::vector<int> h(nv + 1);
-  if (on_device) CK(cudaMemcpy(h.data(), plane_ptr, sizeof(int) * (nv + 1), cudaMemcpyDeviceToHost));
-  else std::memcpy(h.data(), plane_ptr, sizeof(int) * (nv + 1));
+  if (on_device) {
+    CK(cudaMemcpyAsync(h.data(), plane_ptr, sizeof(int) * (nv + 1), cudaMemcpyDeviceToHost,
+                       p->ctx->io));
+    CK(cudaStreamSynchronize(p->ctx->io));
+  } else {
+    std::memcpy(h.data(), plane_ptr, sizeof(int) * (nv + 1));
+  }
   if (h[0] != 0) return fail(MPRGP_INVALID, "plane_ptr[0] != 0");
   for (int v = 0; v < nv; ++v) {
     const int k = h[v + 1] - h[v];
@@ -1524,6 +1574,7 @@ int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int
   }
   if (p->bad_host) return fail(MPRGP_INVALID, "spmv: A has a column outside 0..nv-1");
   SellMatrix A;
+  A.stream_l2 = 0;
   A.nslices = p->nslices;
   A.slice_off = p->slice_off;
   A.cols = p->cols;

@@ -112,6 +112,44 @@ __device__ __forceinline__ void ld_block(const double *vals, size_t j, int lane,
         : "=d"(m[2 * k]), "=d"(m[2 * k + 1]) : "l"(b + 64 * k + 2 * lane));
   m[8] = ldro(b + 256 + lane);
 }
+// L2 eviction policy of a matrix pass.  A run whose matrices together exceed
+// L2 gets nothing from keeping them there (each phase evicts its own first
+// rows before it reads them again), so its column and value loads are marked
+// evict-first: they then replace each other and leave the vectors, and the
+// matrices of other lanes' smaller instances, in L2.  Otherwise evict-normal,
+// the default behaviour.
+__device__ __forceinline__ unsigned long long l2_policy(int stream) {
+  unsigned long long first, normal;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(first));
+  asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(normal));
+  return stream ? first : normal;
+}
+__device__ __forceinline__ int ldro_pol(const int *p, unsigned long long pol) {
+  int r;
+  asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  return r;
+}
+__device__ __forceinline__ void ld_block(const float *vals, size_t j, int lane, float m[9],
+                                         unsigned long long pol) {
+  const float *b = vals + j * (9 * kSlice);
+  float4 p, q;
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w) : "l"(b + 4 * lane), "l"(pol));
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(q.x), "=f"(q.y), "=f"(q.z), "=f"(q.w) : "l"(b + 128 + 4 * lane), "l"(pol));
+  m[0] = p.x; m[1] = p.y; m[2] = p.z; m[3] = p.w;
+  m[4] = q.x; m[5] = q.y; m[6] = q.z; m[7] = q.w;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(m[8]) : "l"(b + 256 + lane), "l"(pol));
+}
+__device__ __forceinline__ void ld_block(const double *vals, size_t j, int lane, double m[9],
+                                         unsigned long long pol) {
+  const double *b = vals + j * (9 * kSlice);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+        : "=d"(m[2 * k]), "=d"(m[2 * k + 1]) : "l"(b + 64 * k + 2 * lane), "l"(pol));
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(m[8]) : "l"(b + 256 + lane), "l"(pol));
+}
 // The same from a shared-memory copy of whole slots.
 template <typename VT>
 __device__ __forceinline__ void ld_block_smem(const VT *vals, size_t j, int lane, VT m[9]) {
@@ -272,6 +310,7 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
                                          const Src &src, OT out[3]) {
   const int s = v >> 5, lane = v & 31;
   const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
+  const unsigned long long pol = l2_policy(A.stream_l2);
   VT a0 = 0, a1 = 0, a2 = 0;
   // Every slot below j1 is valid (padding blocks are zero and point at a
   // real row), so whole chunks of MPRGP_SPMV_CHUNK slots carry no per-slot
@@ -284,12 +323,12 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
   for (; jb < j1; jb += 8) {
     int cc[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? ldro(A.cols + (size_t)(jb + u) * kSlice + lane) : -1;
+    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol) : -1;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       if (cc[u] < 0) break;
       VT m[9];
-      ld_block(vals, (size_t)(jb + u), lane, m);
+      ld_block(vals, (size_t)(jb + u), lane, m, pol);
       VT xv[3];
       src(cc[u], xv);
       a0 = fma(m[0], xv[0], a0); a0 = fma(m[1], xv[1], a0); a0 = fma(m[2], xv[2], a0);
@@ -302,10 +341,10 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     constexpr int K = MPRGP_SPMV_CHUNK;
     int c[K];
 #pragma unroll
-    for (int u = 0; u < K; ++u) c[u] = ldro(A.cols + (size_t)(jb + u) * kSlice + lane);
+    for (int u = 0; u < K; ++u) c[u] = ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol);
     VT m[K][9];
 #pragma unroll
-    for (int u = 0; u < K; ++u) ld_block(vals, (size_t)(jb + u), lane, m[u]);
+    for (int u = 0; u < K; ++u) ld_block(vals, (size_t)(jb + u), lane, m[u], pol);
     VT xv[K][3];
 #pragma unroll
     for (int u = 0; u < K; ++u) src(c[u], xv[u]);
@@ -318,9 +357,9 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     }
   }
   for (; jb < j1; ++jb) {  // the last slots of the row
-    const int c = ldro(A.cols + (size_t)jb * kSlice + lane);
+    const int c = ldro_pol(A.cols + (size_t)jb * kSlice + lane, pol);
     VT m[9];
-    ld_block(vals, (size_t)jb, lane, m);
+    ld_block(vals, (size_t)jb, lane, m, pol);
     VT xv[3];
     src(c, xv);
     a0 = fma(m[0], xv[0], a0); a0 = fma(m[1], xv[1], a0); a0 = fma(m[2], xv[2], a0);
@@ -339,16 +378,17 @@ __device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &
                                           double o1[3], double o2[3]) {
   const int s = v >> 5, lane = v & 31;
   const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
+  const unsigned long long pol = l2_policy(A.stream_l2);
   double a0 = 0, a1 = 0, a2 = 0, b0 = 0, b1 = 0, b2 = 0;
   for (int jb = j0; jb < j1; jb += 4) {
     int c[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) c[u] = (jb + u < j1) ? ldro(A.cols + (size_t)(jb + u) * kSlice + lane) : -1;
+    for (int u = 0; u < 4; ++u) c[u] = (jb + u < j1) ? ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol) : -1;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (c[u] < 0) break;
       double m[9];
-      ld_block(A.v64, (size_t)(jb + u), lane, m);
+      ld_block(A.v64, (size_t)(jb + u), lane, m, pol);
       double x[3], y[3];
       s1(c[u], x);
       s2(c[u], y);

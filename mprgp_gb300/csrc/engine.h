@@ -78,6 +78,8 @@ struct SellMatrix {
   const double *v64;
   const float *v32;
   const int *rowmap;     // SELL row (slot) -> vertex; nullptr: slot == vertex
+  int stream_l2;         // 1: the run streams more matrix bytes than L2 holds; its
+                         // column and value loads are marked evict-first in L2
 };
 
 struct InstState {

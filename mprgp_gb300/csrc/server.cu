@@ -41,6 +41,7 @@ int engine_lane_of(const mprgp_context *c, int nv);
 int context_room(mprgp_context *c, size_t *room);
 int engine_needs_power(const mprgp_problem *p, const mprgp_options *o);
 int engine_in_power(const mprgp_problem *p);
+int problem_read_result(mprgp_problem *p, double *x, unsigned char *face);
 void set_last_error(const char *what);
 }  // namespace mprgp
 
@@ -312,8 +313,7 @@ void retire(mprgp_server *s, Request &r, const mprgp_stats &st) {
   Scene &sc = s->scenes[r.scene];
   r.stats = st;
   r.code = st.code;
-  mprgp_problem_get_x(sc.prob, r.x.data(), 0);
-  if (sc.m > 0) mprgp_problem_get_face(sc.prob, r.face.data());
+  mprgp::problem_read_result(sc.prob, r.x.data(), sc.m > 0 ? r.face.data() : nullptr);
   sc.busy = false;
   r.state = 2;
   r.t_done = now_s();
