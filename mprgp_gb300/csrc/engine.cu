@@ -93,25 +93,6 @@ __host__ __device__ __forceinline__ size_t sell_index(size_t j, int e, int lane,
   const size_t b = j * (9 * kSlice);
   return e < 8 ? b + 64 * (e >> 1) + 2 * lane + (e & 1) : b + 256 + lane;
 }
-__device__ __forceinline__ void ld_block(const float *vals, size_t j, int lane, float m[9]) {
-  const float *b = vals + j * (9 * kSlice);
-  float4 p, q;
-  asm("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
-      : "=f"(p.x), "=f"(p.y), "=f"(p.z), "=f"(p.w) : "l"(b + 4 * lane));
-  asm("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
-      : "=f"(q.x), "=f"(q.y), "=f"(q.z), "=f"(q.w) : "l"(b + 128 + 4 * lane));
-  m[0] = p.x; m[1] = p.y; m[2] = p.z; m[3] = p.w;
-  m[4] = q.x; m[5] = q.y; m[6] = q.z; m[7] = q.w;
-  m[8] = ldro(b + 256 + lane);
-}
-__device__ __forceinline__ void ld_block(const double *vals, size_t j, int lane, double m[9]) {
-  const double *b = vals + j * (9 * kSlice);
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    asm("ld.global.nc.v2.f64 {%0, %1}, [%2];"
-        : "=d"(m[2 * k]), "=d"(m[2 * k + 1]) : "l"(b + 64 * k + 2 * lane));
-  m[8] = ldro(b + 256 + lane);
-}
 // L2 eviction policy of a matrix pass.  A run whose matrices together exceed
 // L2 gets nothing from keeping them there (each phase evicts its own first
 // rows before it reads them again), so its column and value loads are marked
