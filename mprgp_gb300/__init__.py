@@ -526,9 +526,9 @@ class Problem:
 
 def load_beam(ctx: Context, qp: BeamQP, precisions=1) -> Problem:
     pr = Problem(ctx, qp.nv)
+    pr.set_planes(qp.plane_ptr, qp.planes)  # first: the matrix layout then builds once
     pr.set_matrix(qp.row_ptr, qp.cols, qp.vals, precisions)
     pr.set_rhs(qp.b)
-    pr.set_planes(qp.plane_ptr, qp.planes)
     pr.set_x(qp.x0)
     return pr
 

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <string>
 #include <utility>
@@ -101,6 +102,25 @@ struct Lane {
 };
 constexpr int kLanes = 7;  // 0: synchronous calls; 1..6: the server's asynchronous lanes
 
+// Pinned staging for the small arrays the host builds and uploads (SELL slice
+// offsets and row order, plane offsets).  A cudaMemcpyAsync from pageable
+// memory returns only after the stream's earlier work, which may wait for SM
+// room behind other lanes' runs; one from pinned memory returns at once.  A
+// ring: a region is written again only after the event recorded behind its
+// copy has completed.
+struct HostRing {
+  static constexpr size_t kBytes = 16u << 20;
+  char *base = nullptr;
+  size_t head = 0;
+  bool failed = false;  // no pinned memory: uploads stay pageable
+  struct Use {
+    size_t a, b;
+    cudaEvent_t ev;
+  };
+  std::deque<Use> uses;               // in ring order
+  std::vector<cudaEvent_t> spare;     // completed events for reuse
+};
+
 struct mprgp_context {
   int device = 0;
   // Uploads and setup kernels; the highest priority the device offers, so
@@ -132,6 +152,7 @@ struct mprgp_context {
   mprgp_problem *scratch = nullptr;
   int bps_power = 0;
   Lane lane[kLanes];
+  HostRing ring;
   long long launches = 0;  // kernels launched (each power-loop iteration counts)
   double solver_ms = 0.0;  // device time of engine runs, summed over runs (lanes overlap)
   double power_ms = 0.0;   // device time of the power loop alone
@@ -239,6 +260,48 @@ void dfree(mprgp_context *c, T *&p) {
 
 int nitems_of(int nv) { return (nv + kThreads - 1) / kThreads; }
 
+// Host -> device copy of a host-built array on stream s through the pinned
+// ring (pageable, and so ordered behind the stream's earlier work, only when
+// the array is larger than half the ring or pinned memory was refused).
+int upload(mprgp_context *c, void *dst, const void *src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return MPRGP_OK;
+  HostRing &R = c->ring;
+  if (!R.base && !R.failed) {
+    if (cudaMallocHost((void **)&R.base, HostRing::kBytes) != cudaSuccess) {
+      cudaGetLastError();
+      R.base = nullptr;
+      R.failed = true;
+    }
+  }
+  if (!R.base || bytes > HostRing::kBytes / 2) {
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return MPRGP_OK;
+  }
+  const size_t sz = (bytes + 255) & ~(size_t)255;
+  if (R.head + sz > HostRing::kBytes) R.head = 0;
+  const size_t a = R.head, b = a + sz;
+  // wait for earlier copies out of [a, b); retire every completed one
+  for (auto &u : R.uses)
+    if (u.a < b && a < u.b) CK(cudaEventSynchronize(u.ev));
+  while (!R.uses.empty() && cudaEventQuery(R.uses.front().ev) == cudaSuccess) {
+    R.spare.push_back(R.uses.front().ev);
+    R.uses.pop_front();
+  }
+  std::memcpy(R.base + a, src, bytes);
+  CK(cudaMemcpyAsync(dst, R.base + a, bytes, cudaMemcpyHostToDevice, s));
+  cudaEvent_t ev;
+  if (!R.spare.empty()) {
+    ev = R.spare.back();
+    R.spare.pop_back();
+  } else {
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  CK(cudaEventRecord(ev, s));
+  R.uses.push_back({a, b, ev});
+  R.head = b;
+  return MPRGP_OK;
+}
+
 void free_problem_arrays(mprgp_problem *p) {
   dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
   dfree(p->ctx, p->dinv); dfree(p->ctx, p->b); dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw);
@@ -315,8 +378,8 @@ int build_layout(mprgp_problem *p, unsigned long long key) {
     p->has64 = p->want64;
     p->has32 = p->want32;
   }
-  CK(cudaMemcpyAsync(p->slice_off, off.data(), sizeof(int) * (p->nslices + 1),
-                     cudaMemcpyHostToDevice, s));
+  int rc0 = upload(c, p->slice_off, off.data(), sizeof(int) * (p->nslices + 1), s);
+  if (rc0) return rc0;
   if (ident) {
     dfree(c, p->rowmap);
   } else {
@@ -324,14 +387,14 @@ int build_layout(mprgp_problem *p, unsigned long long key) {
       int rc = dalloc(c, &p->rowmap, nv);
       if (rc) return rc;
     }
-    CK(cudaMemcpyAsync(p->rowmap, order.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s));
+    rc0 = upload(c, p->rowmap, order.data(), sizeof(int) * nv, s);
+    if (rc0) return rc0;
   }
   c->launches++;
   launch_bsr_to_sell(nv, p->stage_ptr, p->stage_cols, p->stage_vals, p->slice_off, p->rowmap,
                      p->cols, p->v64, p->v32, p->dinv, p->bad, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
-  // `order` and `off` are pageable: cudaMemcpyAsync has staged them already
   p->layout = key;
   return MPRGP_OK;
 }
@@ -1205,6 +1268,9 @@ int mprgp_context_destroy(mprgp_context *c) {
   if (c->scratch) mprgp_problem_destroy(c->scratch);
   for (int k = kLanes - 1; k >= 0; --k) lane_free(c, c->lane[k]);
   cudaStreamSynchronize(c->stream);
+  for (auto &u : c->ring.uses) cudaEventDestroy(u.ev);
+  for (auto ev : c->ring.spare) cudaEventDestroy(ev);
+  if (c->ring.base) cudaFreeHost(c->ring.base);
   cudaStreamDestroy(c->stream);
   if (c->io) cudaStreamDestroy(c->io);
   if (c->pool) cudaMemPoolDestroy(c->pool);
@@ -1417,7 +1483,10 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
     if (!rc) rc = dalloc(p->ctx, &p->face, (size_t)std::max(m, 1));
     if (rc) return rc;
   }
-  CK(cudaMemcpyAsync(p->plane_ptr, h.data(), sizeof(int) * (nv + 1), cudaMemcpyHostToDevice, s));
+  {
+    const int rc = upload(p->ctx, p->plane_ptr, h.data(), sizeof(int) * (nv + 1), s);
+    if (rc) return rc;
+  }
   if (m > 0)
     CK(cudaMemcpyAsync(p->planes_raw, planes, sizeof(double) * 4 * (size_t)m,
                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
@@ -1426,7 +1495,7 @@ int mprgp_problem_set_planes(mprgp_problem *p, const int *plane_ptr, const doubl
   p->face_len = m;
   p->cons = 1;
   p->planes_dirty = 1;
-  p->h_plane_ptr.swap(h);  // (the copy above was staged from h's buffer, now kept here)
+  p->h_plane_ptr.swap(h);
   if (p->cols && p->stage_vals) {
     const unsigned long long key = layout_key(p);
     if (key != p->layout) return build_layout(p, key);
@@ -1615,12 +1684,13 @@ int mprgp_solve_bsr(mprgp_context *c, int nv, int nnzb, const int *row_ptr, cons
   }
   mprgp_problem *p = c->scratch;
   const int prec = opt->precision == MPRGP_PREC_MIXED ? 3 : 1;
-  int rc = mprgp_problem_set_matrix(p, nnzb, row_ptr, cols, vals, prec, 0);
+  // the constraints before the matrix: the SELL layout (which depends on
+  // the planes) is then built once, for the constraints of this call
+  int rc = opt->kind >= MPRGP_KIND_DECOUPLED
+               ? mprgp_problem_set_planes(p, plane_ptr, planes, 0)
+               : mprgp_problem_set_bounds(p, L, opt->kind == MPRGP_KIND_BOX ? U : nullptr);
+  if (!rc) rc = mprgp_problem_set_matrix(p, nnzb, row_ptr, cols, vals, prec, 0);
   if (!rc) rc = mprgp_problem_set_rhs(p, b, 0);
-  if (!rc) {
-    if (opt->kind >= MPRGP_KIND_DECOUPLED) rc = mprgp_problem_set_planes(p, plane_ptr, planes, 0);
-    else rc = mprgp_problem_set_bounds(p, L, opt->kind == MPRGP_KIND_BOX ? U : nullptr);
-  }
   p->xc = 0;
   if (!rc) rc = mprgp_problem_set_x(p, x, 0);
   p->ev_valid = 0;

@@ -191,17 +191,19 @@ int admit(mprgp_server *s, Request &r) {
   if (old != s->scenes.end() && !old->second.busy) release_scene(s, old);
   Scene sc;
   int rc = mprgp_problem_create(s->ctx, r.nv, &sc.prob);
+  // planes before the matrix: the SELL layout (which depends on the planes)
+  // is then built once
   if (r.mode) {
     const int dev = r.mode == 1;
+    if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.p_plane_ptr, r.p_planes, dev);
     if (!rc) rc = mprgp_problem_set_matrix(sc.prob, r.nnzb, r.p_row_ptr, r.p_cols, r.p_vals, prec, dev);
     if (!rc) rc = mprgp_problem_set_rhs(sc.prob, r.p_b, dev);
-    if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.p_plane_ptr, r.p_planes, dev);
     if (!rc) rc = mprgp_problem_set_x(sc.prob, r.p_x0, dev);
   } else {
+    if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.plane_ptr.data(), r.planes.data(), 0);
     if (!rc) rc = mprgp_problem_set_matrix(sc.prob, r.nnzb, r.row_ptr.data(), r.cols.data(),
                                            r.vals.data(), prec, 0);
     if (!rc) rc = mprgp_problem_set_rhs(sc.prob, r.b.data(), 0);
-    if (!rc) rc = mprgp_problem_set_planes(sc.prob, r.plane_ptr.data(), r.planes.data(), 0);
     if (!rc) rc = mprgp_problem_set_x(sc.prob, r.x0.data(), 0);
   }
   if (rc) {
