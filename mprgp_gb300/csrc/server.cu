@@ -21,6 +21,7 @@
 #include <deque>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -368,8 +369,9 @@ int step_sync(mprgp_server *s, int *ncomp) {
 // Takes the results of lane l's run if it has finished.  Unfinished
 // requests lead the lane's next run (a power lane's, the shared power
 // queue), except that those of a power lane that have left the power method
-// move on to the large lane.
-int finish_lane(mprgp_server *s, int l, int *ncomp) {
+// move on to the large lane.  Finished requests go to `fin` (ticket and
+// stats); the caller reads their results back.
+int finish_lane(mprgp_server *s, int l, std::vector<std::pair<long long, mprgp_stats>> &fin) {
   auto &q = s->lane[l];
   if (!q.active || mprgp::engine_ready(s->ctx, 1 + l) == 0) return MPRGP_OK;
   const int n = (int)q.in_run.size();
@@ -391,8 +393,7 @@ int finish_lane(mprgp_server *s, int l, int *ncomp) {
       }
       continue;
     }
-    retire(s, r, st[i]);
-    ++*ncomp;
+    fin.emplace_back(r.ticket, st[i]);
   }
   q.in_run.clear();
   auto &pend = l >= 2 ? s->lane[2].pending : q.pending;
@@ -429,23 +430,34 @@ int start_lane(mprgp_server *s, int l) {
   return MPRGP_OK;
 }
 
-// The asynchronous form: retire what the lanes finished, admit, start every
-// idle lane; when none of that happened, wait a little for a lane to finish
-// (the caller may have requests to submit meanwhile).
+// The asynchronous form: take what the lanes finished, admit, start every
+// idle lane, and only then read the finished requests' results back (so a
+// lane with work does not wait for the reads), admitting and starting once
+// more for follow-ups whose scene those requests held; when none of that
+// happened, wait a little for a lane to finish (the caller may have requests
+// to submit meanwhile).
 int step_async(mprgp_server *s, int *ncomp) {
   const int nl = 2 + s->npow;
+  std::vector<std::pair<long long, mprgp_stats>> fin;
   for (int l = nl - 1; l >= 0; --l) {  // the power lanes first: they feed the large lane
-    const int rc = finish_lane(s, l, ncomp);
+    const int rc = finish_lane(s, l, fin);
     if (rc) return rc;
   }
   const size_t queued = s->queue.size();
-  admit_queued(s);
   bool started = false;
-  for (int l = 0; l < nl; ++l) {
-    const bool idle = !s->lane[l].active;
-    const int rc = start_lane(s, l);
-    if (rc) return rc;
-    started |= idle && s->lane[l].active;
+  for (int pass = 0; pass < 2; ++pass) {
+    admit_queued(s);
+    for (int l = 0; l < nl; ++l) {
+      const bool idle = !s->lane[l].active;
+      const int rc = start_lane(s, l);
+      if (rc) return rc;
+      started |= idle && s->lane[l].active;
+    }
+    if (pass > 0 || fin.empty()) break;
+    for (auto &f : fin) {
+      retire(s, s->reqs[f.first], f.second);
+      ++*ncomp;
+    }
   }
   if (*ncomp || started || s->queue.size() != queued) return MPRGP_OK;
   const double until = now_s() + 5e-4;
