@@ -207,6 +207,15 @@ class ClockSampler:
         self.path = None
 
     def __enter__(self):
+        # the timed region as an NVTX range ("timed"), so that a profiler can
+        # capture exactly it (ncu --nvtx --nvtx-include "timed/")
+        self.nvtx = False
+        try:
+            import torch
+            torch.cuda.nvtx.range_push("timed")
+            self.nvtx = True
+        except Exception:
+            pass
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -220,6 +229,9 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
+        if self.nvtx:
+            import torch
+            torch.cuda.nvtx.range_pop()
         if self.proc is not None:
             self.proc.terminate()
             try:

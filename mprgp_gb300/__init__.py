@@ -14,7 +14,9 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libmprgp_gb300.so")
+# MPRGP_LIBRARY selects another build of the library, e.g. the bounds-checked
+# debug build (buildlib.build(checks=True))
+LIB_PATH = os.environ.get("MPRGP_LIBRARY") or os.path.join(HERE, "_build", "libmprgp_gb300.so")
 
 OK, NOT_CONVERGED, BREAKDOWN, OOM, TIMEOUT, INVALID, CUDA_ERROR, NO_DEVICE, BUSY = (
     0, -1, -2, -3, -4, -5, -6, -7, -8)

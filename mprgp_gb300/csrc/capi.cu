@@ -21,6 +21,7 @@
 
 #include "../../include/mprgp_gpu.h"
 #include "engine.h"
+#include "nvtx_ranges.h"
 
 namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
@@ -84,6 +85,7 @@ struct Lane {
   cudaStream_t side[kClusterClasses] = {};   // one per cluster size (run concurrently)
   cudaEvent_t fork_ev = nullptr, join_ev[kClusterClasses] = {};
   cudaEvent_t fence = nullptr;               // context-stream work the run depends on
+  nvtxRangeId_t nvtx = 0;                    // the run in flight on the host timeline
   cudaEvent_t e0 = nullptr, e1 = nullptr, e_pow = nullptr, e_end = nullptr;
   // loop graphs of the phase kernel, keyed grid * 4 + variant (they hold
   // this lane's d_args / d_pc / d_pc2)
@@ -465,6 +467,10 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->A.v64 = p->v64;
   d->A.v32 = p->v32;
   d->A.rowmap = p->rowmap;
+#ifdef MPRGP_CHECKS
+  d->A.nv = p->nv;
+  d->A.bad = p->bad;
+#endif
   d->nv = p->nv;
   d->nitems = nitems_of(p->nv);
   d->item_begin = item_begin;
@@ -1020,6 +1026,10 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
   R.cluster_quantum = cluster_quantum;
   R.power_launches = power_launches;
   R.active = true;
+  static const char *kRunNames[kLanes] = {"mprgp run", "mprgp lane small", "mprgp lane large",
+                                          "mprgp lane power", "mprgp lane power",
+                                          "mprgp lane power", "mprgp lane power"};
+  L.nvtx = nvtx_start(kRunNames[k]);
   return MPRGP_OK;
 }
 
@@ -1054,6 +1064,8 @@ int engine_end(mprgp_context *c, int k, mprgp_stats *stats, int *done) {
   Lane &L = c->lane[k];
   LaneRun &R = L.run;
   R.active = false;
+  nvtx_end(L.nvtx);
+  L.nvtx = 0;
   const int n = R.n, n_large = R.n_large;
   CK(cudaEventSynchronize(L.e_end));
   const HostIO &io = *L.io;
@@ -1146,6 +1158,7 @@ namespace {
 // Launches the engine over `n` prepared instances until all are done.
 int run_engine(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
                mprgp_stats *stats) {
+  NvtxScope range("mprgp solve");
   std::vector<int> fresh(n, 1);
   return mprgp::engine_run(c, n, probs, opts, fresh.data(), 0, 1003, 0, stats, nullptr);
 }
@@ -1654,6 +1667,10 @@ int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int
   A.rowmap = p->rowmap;
   A.v64 = p->v64;
   A.v32 = p->v32;
+#ifdef MPRGP_CHECKS
+  A.nv = p->nv;
+  A.bad = p->bad;
+#endif
   p->ctx->launches++;
   launch_spmv(A, p->nv, f32, x_dev, y_dev, p->ctx->stream);
   CK(cudaGetLastError());

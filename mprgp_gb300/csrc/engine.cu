@@ -48,6 +48,25 @@ constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:
 #endif
 
 // ------------------------------------------------------------ primitives --
+// Bounds-checked debug build (-DMPRGP_CHECKS): indices the kernels read from
+// device arrays -- block columns, SELL row order, plane offsets -- are checked
+// before use.  A bad one sets a bit in the instance's invalid-input word
+// (2: block column, 4: plane offsets, 8: SELL row) and is replaced by a safe
+// index, so nothing is read out of bounds; the solve then reports
+// MPRGP_INVALID.  The release build compiles the checks out.
+#ifdef MPRGP_CHECKS
+#define MPRGP_CHECK(cond, word, bit, fix) \
+  do {                                    \
+    if (!(cond)) {                        \
+      if (word) atomicOr(word, bit);      \
+      fix;                                \
+    }                                     \
+  } while (0)
+#else
+#define MPRGP_CHECK(cond, word, bit, fix) \
+  do {                                    \
+  } while (0)
+#endif
 __device__ __forceinline__ long long gtimer() {
   long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -286,6 +305,17 @@ __device__ __forceinline__ void st3f(float *b, int v, const double o[3]) {
   q[2] = (float)o[2];
 }
 
+// A block column and a SELL row's vertex, checked in the debug build.
+__device__ __forceinline__ int checked_col(const SellMatrix &A, int c) {
+  MPRGP_CHECK(c >= 0 && c < A.nv, A.bad, 2, c = 0);
+  return c;
+}
+__device__ __forceinline__ int row_vertex(const SellMatrix &A, int slot) {
+  int v = A.rowmap ? ldro(A.rowmap + slot) : slot;
+  MPRGP_CHECK(v >= 0 && v < A.nv, A.bad, 8, v = 0);
+  return v;
+}
+
 template <typename VT, typename Src, typename OT = double>
 __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
                                          const Src &src, OT out[3]) {
@@ -304,7 +334,7 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
   for (; jb < j1; jb += 8) {
     int cc[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol) : -1;
+    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? checked_col(A, ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol)) : -1;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       if (cc[u] < 0) break;
@@ -322,7 +352,7 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     constexpr int K = MPRGP_SPMV_CHUNK;
     int c[K];
 #pragma unroll
-    for (int u = 0; u < K; ++u) c[u] = ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol);
+    for (int u = 0; u < K; ++u) c[u] = checked_col(A, ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol));
     VT m[K][9];
 #pragma unroll
     for (int u = 0; u < K; ++u) ld_block(vals, (size_t)(jb + u), lane, m[u], pol);
@@ -338,7 +368,7 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     }
   }
   for (; jb < j1; ++jb) {  // the last slots of the row
-    const int c = ldro_pol(A.cols + (size_t)jb * kSlice + lane, pol);
+    const int c = checked_col(A, ldro_pol(A.cols + (size_t)jb * kSlice + lane, pol));
     VT m[9];
     ld_block(vals, (size_t)jb, lane, m, pol);
     VT xv[3];
@@ -364,7 +394,7 @@ __device__ __forceinline__ void spmv2_row(const SellMatrix &A, int v, const S1 &
   for (int jb = j0; jb < j1; jb += 4) {
     int c[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) c[u] = (jb + u < j1) ? ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol) : -1;
+    for (int u = 0; u < 4; ++u) c[u] = (jb + u < j1) ? checked_col(A, ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol)) : -1;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (c[u] < 0) break;
@@ -399,7 +429,7 @@ __device__ __forceinline__ void spmv_row_staged(const SellMatrix &A, int v, cons
   for (int jb = j0; jb < j1; jb += 8) {
     int c[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) c[u] = (jb + u < j1) ? cs[(jb + u - base) * kSlice + lane] : -1;
+    for (int u = 0; u < 8; ++u) c[u] = (jb + u < j1) ? checked_col(A, cs[(jb + u - base) * kSlice + lane]) : -1;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       if (c[u] < 0) break;
@@ -441,7 +471,8 @@ __device__ __forceinline__ void load_cons(const InstDesc &D, int v, VCons &C) {
   C.unit = 0;
   C.ax = 0x3f;
   if (D.kind >= KIND_DECOUPLED) {
-    const int b = ldro(D.plane_ptr + v), e = ldro(D.plane_ptr + v + 1);
+    int b = ldro(D.plane_ptr + v), e = ldro(D.plane_ptr + v + 1);
+    MPRGP_CHECK(b >= 0 && e >= b && e - b <= kMaxPlanes && e <= D.m, D.A.bad, 4, (b = 0, e = 0));
     C.base = b;
     C.k = e - b;
     if (D.pl_unit && C.k >= 2) C.unit = D.pl_unit[v];
@@ -1937,7 +1968,7 @@ __global__ void __launch_bounds__(kThreads, MPRGP_ENGINE_MIN_BLOCKS) engine_kern
       }
       const int local = item - sD.item_begin;
       const int slot = local * kThreads + threadIdx.x;
-      const int v = (slot < sD.nv && sD.A.rowmap) ? ldro(sD.A.rowmap + slot) : slot;
+      const int v = slot < sD.nv ? row_vertex(sD.A, slot) : slot;
       // Stage A for the FP32 matrix passes when the item's slice fits.
       const bool fp32_pass = sD.prec == PREC_MIXED &&
                              (sS.phase == PH_POW || sS.phase == PH_CG_SPMV ||
@@ -2084,7 +2115,7 @@ __device__ __forceinline__ void phase_item(const EngineArgs &args, int item, Pow
 #pragma unroll
   for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
   if (slot < sD.nv) {
-    const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
+    const int v = row_vertex(sD.A, slot);
     if (kAll) row_op(sD, sS, v, slot, part);
     else row_power(sD, sS, v, slot, part);
   }
@@ -2358,7 +2389,7 @@ __global__ void __launch_bounds__(kStepThreads, kMinBlocks)
     if (power_phase(phase)) {
       double part[2] = {0.0, 0.0};
       if (row) {
-        const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
+        const int v = row_vertex(sD.A, slot);
         if (phase == PH_POW_RAND) {
           row_power_rand(sD, v, part);
         } else {
@@ -2535,7 +2566,7 @@ __global__ void __launch_bounds__(kStepThreads, kMinBlocks)
       const bool f32 = D.prec == PREC_MIXED;
       double part[2] = {0.0, 0.0};
       if (row) {
-        const int v = D.A.rowmap ? ldro(D.A.rowmap + slot) : slot;
+        const int v = row_vertex(D.A, slot);
         if (phase == PH_POW_RAND) {
           row_power_rand(D, v, part);
         } else {
@@ -2657,7 +2688,7 @@ __global__ void __launch_bounds__(kThreads, MPRGP_CLUSTER_MIN_BLOCKS) cluster_ke
       for (int k = 0; k < kPart; ++k) part[k] = (k == kMinSlot) ? DBL_MAX : 0.0;
       const int slot = item * kThreads + threadIdx.x;
       if (slot < sD.nv) {
-        const int v = sD.A.rowmap ? ldro(sD.A.rowmap + slot) : slot;
+        const int v = row_vertex(sD.A, slot);
         row_op(sD, sS, v, slot, part);
       }
       const double r = block_reduce(part, red, ns, wmin);
@@ -2816,7 +2847,7 @@ __global__ void __launch_bounds__(256, MPRGP_SPMV_MIN_BLOCKS) spmv_kernel(SellMa
                                                    double *__restrict__ y) {
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= nv) return;
-  const int v = A.rowmap ? A.rowmap[slot] : slot;
+  const int v = row_vertex(A, slot);
   double o[3];
   if constexpr (sizeof(VT) == 4) spmv_row<VT>(A, vals, slot, SrcVtoF{x}, o);
   else spmv_row<VT>(A, vals, slot, SrcV{x}, o);

@@ -80,6 +80,10 @@ struct SellMatrix {
   const int *rowmap;     // SELL row (slot) -> vertex; nullptr: slot == vertex
   int stream_l2;         // 1: the run streams more matrix bytes than L2 holds; its
                          // column and value loads are marked evict-first in L2
+#ifdef MPRGP_CHECKS
+  int nv;    // vertices: every column and SELL row index must lie in 0..nv-1
+  int *bad;  // the instance's invalid-input word (bits 2, 4, 8: see MPRGP_CHECK)
+#endif
 };
 
 struct InstState {
@@ -116,7 +120,8 @@ struct InstDesc {
   double *ev;
   double *part;               // nitems * kPart
   unsigned int *cnt;          // items finished in the current phase
-  const int *bad;             // set when A held a block column outside 0..nv-1
+  const int *bad;             // set when A held a block column outside 0..nv-1 (or,
+                              // in the bounds-checked build, an index check failed)
   InstState *st;
   double *trace;              // optional step trace, 4 doubles per record
   int trace_cap, pad2;

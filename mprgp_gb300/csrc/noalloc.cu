@@ -251,6 +251,10 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   D.A.v64 = d_v64;
   D.A.v32 = d_v32;
   D.A.rowmap = nullptr;
+#ifdef MPRGP_CHECKS
+  D.A.nv = nv;
+  D.A.bad = d_bad;
+#endif
   D.nv = nv;
   D.nitems = nitems;
   D.item_begin = 0;
@@ -318,6 +322,14 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (c1.err) out.code = c1.err;
   else if (out.phase != PH_DONE) out.code = MPRGP_TIMEOUT;
+#ifdef MPRGP_CHECKS
+  {  // an index check failed during the solve
+    int bad = 0;
+    NCK(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    NCK(cudaStreamSynchronize(s));
+    if (bad) out.code = MPRGP_INVALID;
+  }
+#endif
   if (out.code >= MPRGP_NOT_CONVERGED) {  // results only for a finished solve
     NCK(cudaMemcpyAsync(x, d_vec + (size_t)(B_X0 + out.xc) * n, sizeof(double) * n,
                         cudaMemcpyDeviceToDevice, s));

@@ -28,6 +28,7 @@
 
 #include "../../include/mprgp_gpu.h"
 #include "engine.h"
+#include "nvtx_ranges.h"
 
 namespace mprgp {
 int engine_run(mprgp_context *c, int n, mprgp_problem *const *probs, const mprgp_options *opts,
@@ -110,6 +111,7 @@ struct mprgp_server {
   // three-lane form only) the admitted requests waiting for its next run and
   // those in its run in flight.  Server lane l runs on engine lane l + 1.
   int lanes = 0, npow = 0;  // npow: power lanes (lanes - 2 when lanes >= 3)
+  int unretired = 0;        // finished in this step, results not read back yet
   struct LaneQ {
     std::vector<long long> pending, in_run;
     bool active = false;
@@ -230,7 +232,7 @@ namespace {
 
 int in_flight(const mprgp_server *s) {
   if (!s->lanes) return (int)s->running.size();
-  int k = 0;
+  int k = s->unretired;  // their scenes are still busy
   for (const auto &q : s->lane) k += (int)(q.pending.size() + q.in_run.size());
   return k;
 }
@@ -239,6 +241,7 @@ int in_flight(const mprgp_server *s) {
 // does not fit while nothing else is in flight can never fit: it completes
 // with MPRGP_OOM.
 void admit_queued(mprgp_server *s) {
+  mprgp::NvtxScope range("mprgp admit");
   Room room;
   for (auto it = s->queue.begin(); it != s->queue.end();) {
     if (in_flight(s) >= s->max_slots) break;
@@ -439,25 +442,38 @@ int start_lane(mprgp_server *s, int l) {
 int step_async(mprgp_server *s, int *ncomp) {
   const int nl = 2 + s->npow;
   std::vector<std::pair<long long, mprgp_stats>> fin;
+  auto read_back = [&]() {  // every finished request, also on an error return
+    mprgp::NvtxScope range("mprgp read back");
+    for (auto &f : fin) {
+      retire(s, s->reqs[f.first], f.second);
+      ++*ncomp;
+    }
+    fin.clear();
+    s->unretired = 0;
+  };
   for (int l = nl - 1; l >= 0; --l) {  // the power lanes first: they feed the large lane
     const int rc = finish_lane(s, l, fin);
-    if (rc) return rc;
+    if (rc) {
+      read_back();
+      return rc;
+    }
   }
   const size_t queued = s->queue.size();
   bool started = false;
+  s->unretired = (int)fin.size();
   for (int pass = 0; pass < 2; ++pass) {
     admit_queued(s);
     for (int l = 0; l < nl; ++l) {
       const bool idle = !s->lane[l].active;
       const int rc = start_lane(s, l);
-      if (rc) return rc;
+      if (rc) {
+        read_back();
+        return rc;
+      }
       started |= idle && s->lane[l].active;
     }
-    if (pass > 0 || fin.empty()) break;
-    for (auto &f : fin) {
-      retire(s, s->reqs[f.first], f.second);
-      ++*ncomp;
-    }
+    if (fin.empty()) break;
+    read_back();
   }
   if (*ncomp || started || s->queue.size() != queued) return MPRGP_OK;
   const double until = now_s() + 5e-4;
