@@ -25,6 +25,9 @@ namespace mprgp {
 constexpr double kEps = 1e-9;  // ScalarUtil<double>::scalar_eps (MathBasic.cpp:9)
 
 // Resident CTAs per SM the engine is compiled for (register budget).
+#ifndef MPRGP_PREFETCH_DIST  // chunks ahead that a streaming matrix pass prefetches into L2
+#define MPRGP_PREFETCH_DIST 1  // (0: none)
+#endif
 #ifndef MPRGP_SPMV_CHUNK
 #define MPRGP_SPMV_CHUNK 4
 #endif
@@ -305,6 +308,21 @@ __device__ __forceinline__ void st3f(float *b, int v, const double o[3]) {
   q[2] = (float)o[2];
 }
 
+// Prefetch of `n` slots from slot j of a slice into L2 (one bulk prefetch for
+// the values, one for the columns; both start on 128-byte boundaries and
+// span whole slots, so address and size are multiples of 16 bytes), with
+// the pass's eviction policy.  Used only by passes that stream (A.stream_l2).
+template <typename VT>
+__device__ __forceinline__ void prefetch_slots(const SellMatrix &A, const VT *vals, int j, int n,
+                                               unsigned long long pol) {
+  const VT *pv = vals + (size_t)j * (9 * kSlice);
+  const int *pc = A.cols + (size_t)j * kSlice;
+  asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;"
+               :: "l"(pv), "r"((unsigned)(n * 9 * kSlice * sizeof(VT))), "l"(pol) : "memory");
+  asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;"
+               :: "l"(pc), "r"((unsigned)(n * kSlice * sizeof(int))), "l"(pol) : "memory");
+}
+
 // A block column and a SELL row's vertex, checked in the debug build.
 __device__ __forceinline__ int checked_col(const SellMatrix &A, int c) {
   MPRGP_CHECK(c >= 0 && c < A.nv, A.bad, 2, c = 0);
@@ -350,6 +368,12 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
 #else
   for (; jb + MPRGP_SPMV_CHUNK <= j1; jb += MPRGP_SPMV_CHUNK) {
     constexpr int K = MPRGP_SPMV_CHUNK;
+#if MPRGP_PREFETCH_DIST > 0
+    if (A.stream_l2 && lane == 0) {  // the slots this warp reads MPRGP_PREFETCH_DIST chunks on
+      const int jp = jb + K * MPRGP_PREFETCH_DIST;
+      if (jp < j1) prefetch_slots(A, vals, jp, min(K, j1 - jp), pol);
+    }
+#endif
     int c[K];
 #pragma unroll
     for (int u = 0; u < K; ++u) c[u] = checked_col(A, ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol));
