@@ -323,6 +323,29 @@ __device__ __forceinline__ void prefetch_slots(const SellMatrix &A, const VT *va
                :: "l"(pc), "r"((unsigned)(n * kSlice * sizeof(int))), "l"(pol) : "memory");
 }
 
+// The first chunk of slice `slice` into L2: a CTA of the power loops issues
+// it for the item it takes next (the next item of this launch, or its first
+// item again for the next phase) while the current item reduces, so that
+// the next item's rows do not start with a DRAM round trip.
+template <typename VT>
+__device__ __forceinline__ void prefetch_slice_head(const SellMatrix &A, const VT *vals, int slice,
+                                                    unsigned long long pol) {
+  const int j0 = ldro(A.slice_off + slice), j1 = ldro(A.slice_off + slice + 1);
+  if (j1 > j0) prefetch_slots(A, vals, j0, min(MPRGP_SPMV_CHUNK, j1 - j0), pol);
+}
+__device__ __forceinline__ void prefetch_item_head(const InstDesc &D, int local_item) {
+#if MPRGP_PREFETCH_DIST > 0
+  const int warp = threadIdx.x >> 5;
+  if (!D.A.stream_l2 || (threadIdx.x & 31) != 0 || warp >= kThreads / 32) return;
+  if (local_item < 0 || local_item >= D.nitems) return;
+  const int slice = local_item * (kThreads / 32) + warp;
+  if (slice >= D.A.nslices) return;
+  const unsigned long long pol = l2_policy(1);
+  if (D.prec == PREC_MIXED) prefetch_slice_head(D.A, D.A.v32, slice, pol);
+  else prefetch_slice_head(D.A, D.A.v64, slice, pol);
+#endif
+}
+
 // A block column and a SELL row's vertex, checked in the debug build.
 __device__ __forceinline__ int checked_col(const SellMatrix &A, int c) {
   MPRGP_CHECK(c >= 0 && c < A.nv, A.bad, 2, c = 0);
@@ -2425,6 +2448,11 @@ __global__ void __launch_bounds__(kStepThreads, kMinBlocks)
           else row_power64_fin(sD, sCur, v, wd, part);
         }
       }
+      // the item this CTA takes next: its next item of this instance in this
+      // launch, else its first item again in the next launch
+      if (item + (int)gridDim.x < sD.item_begin + sD.nitems) prefetch_item_head(sD, local + (int)gridDim.x);
+      else if (item + (int)gridDim.x >= args.total_items && (int)blockIdx.x >= sD.item_begin)
+        prefetch_item_head(sD, (int)blockIdx.x - sD.item_begin);
       const double r = block_reduce_rows(part, red, nslots(phase));
       if (threadIdx.x < 2) sD.part[(size_t)par * sD.nitems * 2 + 2 * (size_t)local + threadIdx.x] = r;
     }
@@ -2603,6 +2631,10 @@ __global__ void __launch_bounds__(kStepThreads, kMinBlocks)
           else row_power64_fin(D, sS[o], v, wd, part);
         }
       }
+      // the item this CTA takes next: its next owned item, else its first
+      // owned item in the next phase
+      if (o + 1 < nown) prefetch_item_head(sD[o + 1], (int)(blockIdx.x + (o + 1) * gridDim.x) - sD[o + 1].item_begin);
+      else prefetch_item_head(sD[0], (int)blockIdx.x - sD[0].item_begin);
       const double r = block_reduce_rows(part, red, nslots(phase));
       if (threadIdx.x < 2) D.part[(size_t)par * D.nitems * 2 + 2 * (size_t)local + threadIdx.x] = r;
     }
