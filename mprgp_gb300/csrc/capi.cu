@@ -37,8 +37,9 @@ cudaError_t launch_power_direct(int grid, int variant, int launches, const Engin
                                 PowCtl *d_pc, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
-                        const int *slice_off, const int *rowmap, int *out_cols, double *out64,
-                        float *out32, double *dinv, int *bad, cudaStream_t st);
+                        const int *slice_off, const int *rowmap, int *out_cols, short *out_cols16,
+                        int *c16ok, double *out64, float *out32, double *dinv, int *bad,
+                        cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, unsigned char *unit, cudaStream_t st);
 void launch_planes_axis(int m, const double *in, unsigned char *axis, cudaStream_t st);
@@ -167,6 +168,8 @@ struct mprgp_problem {
   int has64 = 0, has32 = 0;
   int xc = 0, ev_valid = 0, planes_dirty = 0;
   int *slice_off = nullptr, *cols = nullptr;
+  short *cols16 = nullptr;  // the columns as 16-bit offsets from the row's vertex
+  int *c16ok = nullptr;     // set by the conversion: every offset fitted in 16 bits
   double *v64 = nullptr;
   float *v32 = nullptr;
   double *dinv = nullptr, *b = nullptr;
@@ -305,7 +308,7 @@ int upload(mprgp_context *c, void *dst, const void *src, size_t bytes, cudaStrea
 }
 
 void free_problem_arrays(mprgp_problem *p) {
-  dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
+  dfree(p->ctx, p->slice_off); dfree(p->ctx, p->cols); dfree(p->ctx, p->cols16); dfree(p->ctx, p->c16ok); dfree(p->ctx, p->v64); dfree(p->ctx, p->v32);
   dfree(p->ctx, p->dinv); dfree(p->ctx, p->b); dfree(p->ctx, p->plane_ptr); dfree(p->ctx, p->planes_raw);
   dfree(p->ctx, p->planes); dfree(p->ctx, p->pl_nn); dfree(p->ctx, p->pl_indn); dfree(p->ctx, p->pl_unit); dfree(p->ctx, p->pl_axis); dfree(p->ctx, p->L); dfree(p->ctx, p->U);
   dfree(p->ctx, p->face); dfree(p->ctx, p->vec); dfree(p->ctx, p->vec32); dfree(p->ctx, p->ev); dfree(p->ctx, p->part); dfree(p->ctx, p->cnt); dfree(p->ctx, p->bad); dfree(p->ctx, p->st);
@@ -370,9 +373,11 @@ int build_layout(mprgp_problem *p, unsigned long long key) {
   const int slots = off[p->nslices];
   if (slots != p->slots || p->want64 != p->has64 || p->want32 != p->has32) {
     dfree(c, p->cols);
+    dfree(c, p->cols16);
     dfree(c, p->v64);
     dfree(c, p->v32);
     int rc = dalloc(c, &p->cols, (size_t)slots * kSlice);
+    if (!rc) rc = dalloc(c, &p->cols16, (size_t)slots * kSlice);
     if (!rc && p->want64) rc = dalloc(c, &p->v64, (size_t)slots * kSlice * 9);
     if (!rc && p->want32) rc = dalloc(c, &p->v32, (size_t)slots * kSlice * 9);
     if (rc) return rc;
@@ -392,9 +397,10 @@ int build_layout(mprgp_problem *p, unsigned long long key) {
     rc0 = upload(c, p->rowmap, order.data(), sizeof(int) * nv, s);
     if (rc0) return rc0;
   }
+  CK(cudaMemsetAsync(p->c16ok, 1, sizeof(int), s));  // nonzero until an offset does not fit
   c->launches++;
   launch_bsr_to_sell(nv, p->stage_ptr, p->stage_cols, p->stage_vals, p->slice_off, p->rowmap,
-                     p->cols, p->v64, p->v32, p->dinv, p->bad, s);
+                     p->cols, p->cols16, p->c16ok, p->v64, p->v32, p->dinv, p->bad, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "bsr_to_sell");
   p->layout = key;
@@ -464,6 +470,8 @@ int prepare(mprgp_problem *p, const mprgp_options *o, int item_begin, InstDesc *
   d->A.nslices = p->nslices;
   d->A.slice_off = p->slice_off;
   d->A.cols = p->cols;
+  d->A.cols16 = p->cols16;
+  d->A.c16ok = p->c16ok;
   d->A.v64 = p->v64;
   d->A.v32 = p->v32;
   d->A.rowmap = p->rowmap;
@@ -1358,8 +1366,9 @@ int mprgp_context_room(mprgp_context *c, size_t *bytes) {
 
 size_t mprgp_problem_bytes(int nv, int nnzb, int nplanes, int precisions) {
   const size_t nsl = (size_t)(nv + kSlice - 1) / kSlice;
-  const size_t slots = (size_t)nnzb / 1 + nsl * 8;  // padding allowance
-  size_t by = (nsl + 1) * 4 + slots * kSlice * 4;
+  // SELL slots of 32 rows: the blocks plus a padding allowance of 8 slots a slice
+  const size_t slots = ((size_t)nnzb + kSlice - 1) / kSlice + nsl * 8;
+  size_t by = (nsl + 1) * 4 + slots * kSlice * (4 + 2);  // 32- and 16-bit columns
   if (precisions & 1) by += slots * kSlice * 9 * 8;
   if (precisions & 2) by += slots * kSlice * 9 * 4;
   const size_t n = 3 * (size_t)nv;
@@ -1383,7 +1392,7 @@ int mprgp_problem_create(mprgp_context *c, int nv, mprgp_problem **out) {
   if ((rc = dalloc(p->ctx, &p->vec, n * kNumBuf)) || (rc = dalloc(p->ctx, &p->vec32, n * kNumBuf32)) ||
       (rc = dalloc(p->ctx, &p->ev, n)) ||
       (rc = dalloc(p->ctx, &p->b, n)) || (rc = dalloc(p->ctx, &p->dinv, n)) ||
-      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart * 2)) || (rc = dalloc(p->ctx, &p->cnt, 1)) || (rc = dalloc(p->ctx, &p->bad, 1)) ||
+      (rc = dalloc(p->ctx, &p->part, (size_t)nitems_of(nv) * kPart * 2)) || (rc = dalloc(p->ctx, &p->cnt, 1)) || (rc = dalloc(p->ctx, &p->bad, 1)) || (rc = dalloc(p->ctx, &p->c16ok, 1)) ||
       (rc = dalloc(p->ctx, &p->st, 1)) || (rc = dalloc(p->ctx, &p->slice_off, p->nslices + 1))) {
     free_problem_arrays(p);
     delete p;
@@ -1664,6 +1673,8 @@ int mprgp_problem_spmv(mprgp_problem *p, const double *x_dev, double *y_dev, int
   A.nslices = p->nslices;
   A.slice_off = p->slice_off;
   A.cols = p->cols;
+  A.cols16 = p->cols16;
+  A.c16ok = p->c16ok;
   A.rowmap = p->rowmap;
   A.v64 = p->v64;
   A.v32 = p->v32;

@@ -127,6 +127,11 @@ __device__ __forceinline__ unsigned long long l2_policy(int stream) {
   asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(normal));
   return stream ? first : normal;
 }
+__device__ __forceinline__ int ldro16_pol(const short *p, unsigned long long pol) {
+  short r;
+  asm("ld.global.nc.L2::cache_hint.s16 %0, [%1], %2;" : "=h"(r) : "l"(p), "l"(pol));
+  return (int)r;
+}
 __device__ __forceinline__ int ldro_pol(const int *p, unsigned long long pol) {
   int r;
   asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
@@ -312,15 +317,21 @@ __device__ __forceinline__ void st3f(float *b, int v, const double o[3]) {
 // the values, one for the columns; both start on 128-byte boundaries and
 // span whole slots, so address and size are multiples of 16 bytes), with
 // the pass's eviction policy.  Used only by passes that stream (A.stream_l2).
-template <typename VT>
+template <bool k16, typename VT>
 __device__ __forceinline__ void prefetch_slots(const SellMatrix &A, const VT *vals, int j, int n,
                                                unsigned long long pol) {
   const VT *pv = vals + (size_t)j * (9 * kSlice);
-  const int *pc = A.cols + (size_t)j * kSlice;
   asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;"
                :: "l"(pv), "r"((unsigned)(n * 9 * kSlice * sizeof(VT))), "l"(pol) : "memory");
-  asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;"
-               :: "l"(pc), "r"((unsigned)(n * kSlice * sizeof(int))), "l"(pol) : "memory");
+  if (k16) {  // 64 bytes per slot
+    asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;"
+                 :: "l"(A.cols16 + (size_t)j * kSlice), "r"((unsigned)(n * kSlice * sizeof(short))),
+                 "l"(pol) : "memory");
+  } else {
+    asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;"
+                 :: "l"(A.cols + (size_t)j * kSlice), "r"((unsigned)(n * kSlice * sizeof(int))),
+                 "l"(pol) : "memory");
+  }
 }
 
 // The first chunk of slice `slice` into L2: a CTA of the power loops issues
@@ -331,7 +342,9 @@ template <typename VT>
 __device__ __forceinline__ void prefetch_slice_head(const SellMatrix &A, const VT *vals, int slice,
                                                     unsigned long long pol) {
   const int j0 = ldro(A.slice_off + slice), j1 = ldro(A.slice_off + slice + 1);
-  if (j1 > j0) prefetch_slots(A, vals, j0, min(MPRGP_SPMV_CHUNK, j1 - j0), pol);
+  if (j1 <= j0) return;
+  if (A.cols16 && ldro(A.c16ok)) prefetch_slots<true>(A, vals, j0, min(MPRGP_SPMV_CHUNK, j1 - j0), pol);
+  else prefetch_slots<false>(A, vals, j0, min(MPRGP_SPMV_CHUNK, j1 - j0), pol);
 }
 __device__ __forceinline__ void prefetch_item_head(const InstDesc &D, int local_item) {
 #if MPRGP_PREFETCH_DIST > 0
@@ -357,25 +370,33 @@ __device__ __forceinline__ int row_vertex(const SellMatrix &A, int slot) {
   return v;
 }
 
-template <typename VT, typename Src, typename OT = double>
-__device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
-                                         const Src &src, OT out[3]) {
-  const int s = v >> 5, lane = v & 31;
-  const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
-  const unsigned long long pol = l2_policy(A.stream_l2);
-  VT a0 = 0, a1 = 0, a2 = 0;
-  // Every slot below j1 is valid (padding blocks are zero and point at a
-  // real row), so whole chunks of MPRGP_SPMV_CHUNK slots carry no per-slot
-  // condition and all their column, value and neighbour loads can be in
-  // flight together (0: columns of 8 slots fetched together, then one slot
-  // at a time).  The products are accumulated slot by slot in order either
-  // way, so the results are the same.
+// Block column of slot j, lane `lane`: the 16-bit offset from the row's
+// vertex vrow (k16) or the 32-bit column.
+template <bool k16>
+__device__ __forceinline__ int col_of(const SellMatrix &A, size_t j, int lane, int vrow,
+                                      unsigned long long pol) {
+  const size_t i = j * kSlice + lane;
+  if constexpr (k16) return checked_col(A, vrow + ldro16_pol(A.cols16 + i, pol));
+  else return checked_col(A, ldro_pol(A.cols + i, pol));
+}
+
+// Every slot below j1 is valid (padding blocks are zero and point at a real
+// row), so whole chunks of MPRGP_SPMV_CHUNK slots carry no per-slot condition
+// and all their column, value and neighbour loads can be in flight together
+// (0: columns of 8 slots fetched together, then one slot at a time).  The
+// products are accumulated slot by slot in order either way, so the results
+// are the same -- and the same whichever column form is read.
+template <bool k16, typename VT, typename Src>
+__device__ __forceinline__ void spmv_row_body(const SellMatrix &A, const VT *__restrict__ vals,
+                                              int lane, int vrow, int j0, int j1,
+                                              unsigned long long pol, const Src &src, VT &a0,
+                                              VT &a1, VT &a2) {
   int jb = j0;
 #if MPRGP_SPMV_CHUNK == 0
   for (; jb < j1; jb += 8) {
     int cc[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? checked_col(A, ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol)) : -1;
+    for (int u = 0; u < 8; ++u) cc[u] = (jb + u < j1) ? col_of<k16>(A, (size_t)(jb + u), lane, vrow, pol) : -1;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       if (cc[u] < 0) break;
@@ -394,12 +415,12 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
 #if MPRGP_PREFETCH_DIST > 0
     if (A.stream_l2 && lane == 0) {  // the slots this warp reads MPRGP_PREFETCH_DIST chunks on
       const int jp = jb + K * MPRGP_PREFETCH_DIST;
-      if (jp < j1) prefetch_slots(A, vals, jp, min(K, j1 - jp), pol);
+      if (jp < j1) prefetch_slots<k16>(A, vals, jp, min(K, j1 - jp), pol);
     }
 #endif
     int c[K];
 #pragma unroll
-    for (int u = 0; u < K; ++u) c[u] = checked_col(A, ldro_pol(A.cols + (size_t)(jb + u) * kSlice + lane, pol));
+    for (int u = 0; u < K; ++u) c[u] = col_of<k16>(A, (size_t)(jb + u), lane, vrow, pol);
     VT m[K][9];
 #pragma unroll
     for (int u = 0; u < K; ++u) ld_block(vals, (size_t)(jb + u), lane, m[u], pol);
@@ -415,7 +436,7 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     }
   }
   for (; jb < j1; ++jb) {  // the last slots of the row
-    const int c = checked_col(A, ldro_pol(A.cols + (size_t)jb * kSlice + lane, pol));
+    const int c = col_of<k16>(A, (size_t)jb, lane, vrow, pol);
     VT m[9];
     ld_block(vals, (size_t)jb, lane, m, pol);
     VT xv[3];
@@ -425,6 +446,24 @@ __device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restri
     a2 = fma(m[6], xv[0], a2); a2 = fma(m[7], xv[1], a2); a2 = fma(m[8], xv[2], a2);
   }
 #endif
+}
+
+// One row's product with a source vector; v is the row's SELL slot.  The
+// columns come from the 16-bit offsets when the matrix has them and every
+// offset fitted (A.c16ok), else from the 32-bit columns.
+template <typename VT, typename Src, typename OT = double>
+__device__ __forceinline__ void spmv_row(const SellMatrix &A, const VT *__restrict__ vals, int v,
+                                         const Src &src, OT out[3]) {
+  const int s = v >> 5, lane = v & 31;
+  const int j0 = ldro(A.slice_off + s), j1 = ldro(A.slice_off + s + 1);
+  const unsigned long long pol = l2_policy(A.stream_l2);
+  VT a0 = 0, a1 = 0, a2 = 0;
+  if (A.cols16 && ldro(A.c16ok)) {
+    const int vrow = A.rowmap ? ldro(A.rowmap + v) : v;
+    spmv_row_body<true>(A, vals, lane, vrow, j0, j1, pol, src, a0, a1, a2);
+  } else {
+    spmv_row_body<false>(A, vals, lane, 0, j0, j1, pol, src, a0, a1, a2);
+  }
   out[0] = (OT)a0;
   out[1] = (OT)a1;
   out[2] = (OT)a2;
@@ -2809,7 +2848,8 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
                                    const int *__restrict__ cols, const double *__restrict__ vals,
                                    const int *__restrict__ slice_off,
                                    const int *__restrict__ rowmap, int *out_cols,
-                                   double *out64, float *out32, double *dinv, int *bad) {
+                                   short *out_cols16, int *c16ok, double *out64, float *out32,
+                                   double *dinv, int *bad) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;  // SELL row (slot)
   const int s = q >> 5, lane = q & 31;
   const int nslices = (nv + kSlice - 1) / kSlice;
@@ -2840,6 +2880,12 @@ __global__ void bsr_to_sell_kernel(int nv, const int *__restrict__ row_ptr,
       for (int e = 0; e < 9; ++e) m[e] = 0.0;
     }
     out_cols[slot * kSlice + lane] = c;
+    if (out_cols16) {  // the offset from the row's vertex; one that does not fit
+      const int d = c - ((q < nv) ? r : 0);  // sends every pass to the 32-bit columns
+      const bool fits = d >= -32768 && d <= 32767;
+      out_cols16[slot * kSlice + lane] = fits ? (short)d : (short)0;
+      if (!fits) *c16ok = 0;
+    }
     for (int e = 0; e < 9; ++e) {
       if (out64) out64[sell_index(slot, e, lane, double())] = m[e];
       if (out32) out32[sell_index(slot, e, lane, float())] = (float)m[e];
@@ -3131,13 +3177,15 @@ cudaError_t power_max_blocks_per_sm(int variant, int *n) {
                                                        power_block_threads(variant), 0);
 }
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
-                        const int *slice_off, const int *rowmap, int *out_cols, double *out64,
-                        float *out32, double *dinv, int *bad, cudaStream_t st) {
+                        const int *slice_off, const int *rowmap, int *out_cols, short *out_cols16,
+                        int *c16ok, double *out64, float *out32, double *dinv, int *bad,
+                        cudaStream_t st) {
   const int nslices = (nv + kSlice - 1) / kSlice;
   const int threads = nslices * kSlice;
+  // (the caller sets *c16ok = 1 before the conversion)
   bsr_to_sell_kernel<<<(threads + 255) / 256, 256, 0, st>>>(nv, row_ptr, cols, vals, slice_off,
-                                                            rowmap, out_cols, out64, out32, dinv,
-                                                            bad);
+                                                            rowmap, out_cols, out_cols16, c16ok,
+                                                            out64, out32, dinv, bad);
 }
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, unsigned char *unit, cudaStream_t st) {

@@ -75,6 +75,8 @@ struct SellMatrix {
   int nslices;
   const int *slice_off;  // nslices + 1, in slots
   const int *cols;       // vertex index; padding points at a valid row, value 0
+  const short *cols16;   // the same as 16-bit offsets from the row's vertex; read when
+  const int *c16ok;      // *c16ok: every offset fitted (nullptr: cols only)
   const double *v64;
   const float *v32;
   const int *rowmap;     // SELL row (slot) -> vertex; nullptr: slot == vertex

@@ -45,8 +45,9 @@ namespace mprgp {
 cudaError_t launch_engine(const EngineArgs &args, int grid, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(int *n, int stage_bytes);
 void launch_bsr_to_sell(int nv, const int *row_ptr, const int *cols, const double *vals,
-                        const int *slice_off, const int *rowmap, int *out_cols, double *out64,
-                        float *out32, double *dinv, int *bad, cudaStream_t st);
+                        const int *slice_off, const int *rowmap, int *out_cols, short *out_cols16,
+                        int *c16ok, double *out64, float *out32, double *dinv, int *bad,
+                        cudaStream_t st);
 void launch_planes_setup(int nv, const int *plane_ptr, const double *in, double *out, double *nn,
                          double *indn, const double *dinv, unsigned char *unit, cudaStream_t st);
 void set_last_error(const char *what);
@@ -227,7 +228,7 @@ extern "C" int mprgp_solve_noalloc(void *stream, int nv, int nnzb, const int *ro
   NCK(cudaMemcpyAsync(d_soff, off.data(), sizeof(int) * (nslices + 1), cudaMemcpyHostToDevice, s));
   int *d_bad = reinterpret_cast<int *>(base + o_bad);
   NCK(cudaMemsetAsync(d_bad, 0, sizeof(int), s));
-  launch_bsr_to_sell(nv, row_ptr, cols, vals, d_soff, nullptr, d_cols, d_v64, d_v32, d_dinv, d_bad,
+  launch_bsr_to_sell(nv, row_ptr, cols, vals, d_soff, nullptr, d_cols, nullptr, nullptr, d_v64, d_v32, d_dinv, d_bad,
                      s);
   NCK(cudaGetLastError());
   {  // the conversion checks the block columns; no solve on an invalid A
