@@ -645,3 +645,49 @@ def test_invalid_column_reports_invalid(ctx):
     pr.close()
     x, face, st = ctx.solve_bsr(qp, opt, qp.x0)
     assert st.code == 0
+
+
+@pytest.mark.parametrize("far", [False, True])
+def test_spmv_column_forms(ctx, far):
+    """The matrix passes read 16-bit column offsets from the row's vertex
+    when every offset fits, else the 32-bit columns.  A block-tridiagonal
+    matrix of 40,000 vertices has offsets of at most 1; a symmetric pair of
+    blocks coupling the first and the last vertex (offset 39,999) sends every
+    pass to the 32-bit columns.  Both products match numpy's."""
+    torch = pytest.importorskip("torch")
+    nv = 40000
+    rng = np.random.default_rng(7)
+    rows, cols = [], []
+    for v in range(nv):
+        for u in (v - 1, v, v + 1):
+            if 0 <= u < nv:
+                rows.append(v)
+                cols.append(u)
+    if far:
+        rows += [0, nv - 1]
+        cols += [nv - 1, 0]
+    order = np.lexsort((np.array(cols), np.array(rows)))
+    rows = np.array(rows)[order]
+    cols = np.array(cols, dtype=np.int32)[order]
+    nnzb = len(rows)
+    row_ptr = np.zeros(nv + 1, dtype=np.int32)
+    np.add.at(row_ptr, rows + 1, 1)
+    row_ptr = np.cumsum(row_ptr).astype(np.int32)
+    vals = rng.standard_normal((nnzb, 3, 3))
+    vals[rows == cols] += 8.0 * np.eye(3)  # a dominant diagonal block
+    x = rng.standard_normal(3 * nv)
+    y_ref = np.zeros((nv, 3))  # y = A x block by block
+    np.add.at(y_ref, rows, np.einsum("kij,kj->ki", vals, x.reshape(nv, 3)[cols]))
+    y_ref = y_ref.reshape(-1)
+    pr = M.Problem(ctx, nv)
+    pr.set_matrix(row_ptr, cols, np.ascontiguousarray(vals.reshape(-1)), precisions=3)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.zeros(3 * nv, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    pr.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_FP64)
+    ctx.sync()
+    assert rel(yd.cpu().numpy(), y_ref) < 1e-14
+    pr.spmv(xd.data_ptr(), yd.data_ptr(), M.PREC_MIXED)
+    ctx.sync()
+    assert rel(yd.cpu().numpy(), y_ref) < 1e-5
+    pr.close()
