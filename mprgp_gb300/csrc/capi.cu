@@ -857,7 +857,7 @@ int engine_begin(mprgp_context *c, int k, int n, mprgp_problem *const *probs,
     for (int i = 0; i < n; ++i)
       if (R.pos[i] < n_large)
         mbytes += (size_t)probs[i]->slots * kSlice *
-                  (9 * (desc[R.pos[i]].prec == PREC_MIXED ? 4 : 8) + 4);
+                  (9 * (desc[R.pos[i]].prec == PREC_MIXED ? 4 : 8) + (probs[i]->cols16 ? 2 : 4));
     const int stream_l2 = (k >= 2 || mbytes > c->l2_bytes / 4 * 3) ? 1 : 0;
     for (int j = 0; j < n_large; ++j) desc[j].A.stream_l2 = stream_l2;
   }
