@@ -111,8 +111,10 @@ def workload_desc(name, qp):
 
 def spmv_bytes(qp, s_a):
     """Algorithmic bytes of one y = A x at matrix precision s_a (8 or 4 bytes):
-    A (values + block column), row pointers, x and y at the same precision."""
-    return qp.nnzb * (9 * s_a + 4) + (qp.nv + 1) * 4 + 2 * qp.n * s_a
+    A (values + block column), row pointers, x and y at the same precision.
+    The block column counts 2 bytes: the matrix passes read 16-bit offsets
+    from the row's vertex, which every beam's offsets fit."""
+    return qp.nnzb * (9 * s_a + 2) + (qp.nv + 1) * 4 + 2 * qp.n * s_a
 
 
 # n-vector traffic of the solver phases beyond the matrix pass, in FP64
@@ -439,7 +441,7 @@ def run_gb300(args):
                      "launch_ms": round(pow_launch_ms, 5), "launches": int(passes),
                      "share_of_solve": round(power_ms / max(1e-9, solver1 - solver0), 3)
                      if power_ms > 0 else 1.0,
-                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+2) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
         "roofline_engine": {"kernel": "mprgp::engine_kernel (MPRGP phases)",
                             "achieved": None if eng_achieved is None else round(eng_achieved, 2),
                             "frac": None if eng_achieved is None else round(eng_achieved / peak, 4),
@@ -874,7 +876,7 @@ def run_timesteps(args):
                      "traffic": None,
                      "bytes_per_launch": int(alg / max(1, launches)),
                      "launch_ms": round(dev_ms / max(1, launches), 5),
-                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+2) + (nv+1)*4 + 2*n*s, s = 8 (FP64) or 4 (FP32)"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": None,
@@ -1152,7 +1154,7 @@ def run_serve(args):
                      "bytes_matrix_per_step": int(alg / len(timed)),
                      "bytes_vectors_per_step": int(vec / len(timed)),
                      "achieved_matrix_only": round(alg / (solver_ms / 1e3) / 1e9, 2),
-                     "bytes_rule": "per matrix pass: nnzb*(9*s+4) + (nv+1)*4 + 2*n*s, s = 8 (FP64) "
+                     "bytes_rule": "per matrix pass: nnzb*(9*s+2) + (nv+1)*4 + 2*n*s, s = 8 (FP64) "
                                    "or 4 (FP32); plus k*n*8 of vector traffic per phase (VEC_K "
                                    "in bench.py) and 49 B per constraint row read"},
         "gpu_launches": int(launches),
