@@ -168,7 +168,8 @@ typedef struct mprgp_problem mprgp_problem;
 int mprgp_problem_create(mprgp_context *ctx, int nv, mprgp_problem **out);
 int mprgp_problem_destroy(mprgp_problem *prob);
 /* precisions: bit 0 keep FP64 values, bit 1 keep an FP32 copy. on_device: the
- * pointers are device pointers (0 = host). */
+ * pointers are device pointers (0 = host), holding their data when the call is
+ * made (work on another stream that writes them has completed). */
 int mprgp_problem_set_matrix(mprgp_problem *prob, int nnzb, const int *row_ptr, const int *cols,
                              const double *vals, int precisions, int on_device);
 int mprgp_problem_set_rhs(mprgp_problem *prob, const double *b, int on_device);
