@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 def _start(qp):
     A, b, J, c = H.qp_from_beam(qp)
     As = sp.csr_matrix((A.val, A.idx, A.ptr), shape=(A.rows, A.cols))
-    return spl.spsolve(As.tocsc(), b)  # the driver starts from the unconstrained solve
+    return spl.spsolve(As.tocsc(), b)  # the reference's FEM loop starts from the unconstrained solve
 
 
 @pytest.mark.parametrize("dims,extra,seed,max_it,tol", [

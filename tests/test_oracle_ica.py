@@ -37,7 +37,7 @@ def test_ica_matches_golden_quadprog(path):
     qp = M.BeamQP(int(d["nv"]), d["row_ptr"], d["cols"], d["vals"], d["b"], d["x0"],
                   d["plane_ptr"], d["planes"], {})
     As, b, Js, c = _mats(qp)
-    x0 = spl.spsolve(As.tocsc(), b)  # the driver starts ICA from the unconstrained solve
+    x0 = spl.spsolve(As.tocsc(), b)  # the reference's FEM loop starts ICA from the unconstrained solve
     x, lam, st = H.oracle_ica(qp, x0, max_it=100000, tol=1e-11 * np.linalg.norm(b),
                               gs_max_it=20, gs_tol=1e-14)
     assert st["converged"] == 1 and st["code"] == 0
