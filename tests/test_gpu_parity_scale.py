@@ -14,7 +14,8 @@
    cores): the same DECIDE_FACE active set at the reference's stopping test
    1e-8 ||b|| and at 1e-10 ||b||, and ||x - x_ref|| / ||x_ref|| <= 1e-8 at
    1e-10 ||b|| (at 1e-8 ||b|| both iterates are only within ~kappa * tol of
-   the solution).
+   the solution).  The mixed form on the same QP: the same active set at both
+   tolerances and within 1e-8 of the oracle at 1e-10 ||b||.
 """
 import os
 
@@ -150,6 +151,19 @@ def test_c1_fp64_matches_oracle(ctx, c1_qp):
             assert (sg.iterations, sg.num_cg, sg.num_exp, sg.num_prop) == (
                 int(ss["iterations"]), int(ss["num_cg"]), int(ss["num_exp"]),
                 int(ss["num_prop"]))
+            # the mixed form (FP32 A, FP64 steps and projection) on the same QP:
+            # the oracle's active set, feasible, and at the tight tolerance
+            # within 1e-8 of the oracle's solution
+            optm = M.default_options(tol=tol, max_it=20000, kind=M.KIND_PLANES, project_x0=1,
+                                     seed=SEED, precision=M.PREC_MIXED)
+            xm, _, sm = ctx.solve_bsr(qp, optm, qp.x0)
+            print(f"c1 mixed tol {rel_tol:g}||b||: {sm.iterations} iterations, rel x err vs "
+                  f"oracle {rel(xm, xr):.3e}")
+            assert sm.code == 0
+            assert np.array_equal(H.decide_face_planes(J, c, xm), face_r)
+            assert (J.matvec(xm) - c).min() >= -1e-9
+            if rel_tol <= 1e-10:
+                assert rel(xm, xr) <= 1e-8
         xr, _, xs, _, xg, _ = out[1e-10]
         assert rel(xg, xr) <= 1e-8
         assert rel(xg, xs) <= 1e-8
